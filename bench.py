@@ -1,0 +1,423 @@
+#!/usr/bin/env python3
+"""Escape-time throughput on GB300: Gpixel-iter/s of one frame workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one step = one frame): Mandelbrot, 3840x2160, span 1e-10 (plane
+width), centre = a seeded point on the set boundary found by bisection along a
+seeded ray from inside the main cardioid to |c| = 2.5, maxIter 20000, 4
+jittered samples per pixel (seeded uniform offsets), coloured through a seeded
+256-entry RGBA8 palette with linear interpolation.  Unit of work: one
+pixel-iteration (one z <- z^2 + c step of one sample; an interior sample
+counts maxIter), counted by the kernel itself.
+
+Timed region: K frames, each bracketed by CUDA events on the launching stream,
+with a 256 MiB write between frames to flush L2; barrier + synchronize on both
+sides; max over ranks.  N > 1 runs independent replicas (one process per GPU,
+no collective on the data path).
+
+--impl reference times the reference's own per-sample function
+(computeFractal<double>, src/main/cuda/fractals/mandelbrot.cu, host-built by
+oracle/build_ref.sh) on the host cores over a bounded sample of the same
+frame's sample points; the oracle's C restatement stands in when the
+reference build is unavailable.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "chaos-ultra_gb300")
+for _p in (PKG_DIR, ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+WORKLOAD_SEED = 2
+W, H, SPAN, MAX_ITER, SPP = 3840, 2160, 1e-10, 20000, 4
+METRIC = "Gpixel-iter/s at <=0.1% escape-count mismatch vs FP64 oracle"
+MISMATCH_SAMPLE_PIXELS = 4096
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+def _escapes(cx, cy, max_iter):
+    x = y = 0.0
+    for _ in range(max_iter):
+        xx, yy = x * x, y * y
+        if xx + yy >= 4.0:
+            return True
+        y = 2.0 * x * y + cy
+        x = xx - yy + cx
+    return False
+
+
+def boundary_point(seed, max_iter=MAX_ITER, steps=200):
+    """Bisection between a seeded interior point of the main cardioid
+    (c = mu/2 - mu^2/4, |mu| < 1) and a seeded point on |c| = 2.5."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    r, t, s = rng.uniform(0.3, 0.95), rng.uniform(0, 2 * math.pi), rng.uniform(0, 2 * math.pi)
+    mu = complex(r * math.cos(t), r * math.sin(t))
+    c_in = mu / 2 - mu * mu / 4
+    c_out = complex(2.5 * math.cos(s), 2.5 * math.sin(s))
+    for _ in range(steps):
+        mid = (c_in + c_out) / 2
+        if mid == c_in or mid == c_out:
+            break
+        if _escapes(mid.real, mid.imag, max_iter):
+            c_out = mid
+        else:
+            c_in = mid
+    return c_in.real, c_in.imag
+
+
+def workload(seed=WORKLOAD_SEED):
+    from chaos_gb300.palette import seeded_palette
+    cx, cy = boundary_point(seed)
+    return {"center": (cx, cy), "pixel_size": SPAN / W, "palette": seeded_palette(256, seed=seed),
+            "jitter_seed": 1000 + seed, "interior_rgba": 0xFF000000}
+
+
+def frame_desc(cg, wl, tier, arith):
+    return cg.FrameDesc(width=W, height=H, max_iterations=MAX_ITER, samples_per_pixel=SPP,
+                        sample_mode=cg.SAMPLES_JITTER, tier=tier, arith=arith, fractal=cg.MANDELBROT,
+                        seed=wl["jitter_seed"], center_x=wl["center"][0], center_y=wl["center"][1],
+                        pixel_size=wl["pixel_size"])
+
+
+def sample_pixels(n, seed=7):
+    """Seeded pixel indices spread over the frame."""
+    import numpy as np
+    return np.sort(np.random.default_rng(seed).choice(W * H, size=n, replace=False))
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], None, set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax = float(parts[2])
+                    power.append(float(parts[3]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+# ---------------------------------------------------------------------------
+# CPU leg: the reference's per-sample function (or the oracle port) on the host
+# ---------------------------------------------------------------------------
+
+def _cpu_impl():
+    """(kind, runner): runner(xs, ys) -> (total pixel-iterations, counts)."""
+    from oracle import build_oracle
+    from oracle.oracle import REF_LIB, Oracle, Reference
+    build_oracle.build_oracle()
+    try:
+        build_oracle.build_reference()
+    except RuntimeError:
+        pass
+    if os.path.exists(REF_LIB):
+        try:
+            ref = Reference()
+            return "reference", ref.max_threads(), lambda xs, ys: ref.points_d(xs, ys, MAX_ITER)
+        except OSError:
+            pass
+    o = Oracle()
+    # the oracle's restatement of computeFractal<double> (rounded arithmetic), OpenMP over points
+    return "port", o.max_threads(), lambda xs, ys: o.mandelbrot_points_d(xs, ys, MAX_ITER)
+
+
+def cpu_sample_points(wl, n_pixels, seed=11):
+    from oracle.oracle import Oracle
+    import numpy as np
+    o = Oracle()
+    pix = sample_pixels(n_pixels, seed)
+    xs, ys = [], []
+    for p in pix:
+        x, y = o.frame_points(W, H, SPP, 1, wl["jitter_seed"], wl["center"], wl["pixel_size"], int(p), 1)
+        xs.append(x)
+        ys.append(y)
+    return pix, np.concatenate(xs), np.concatenate(ys)
+
+
+def cpu_baseline(wl, budget_s=12.0):
+    """Time the CPU implementation on a bounded sample of the frame's points."""
+    kind, threads, run = _cpu_impl()
+    n = 256
+    while True:
+        _, xs, ys = cpu_sample_points(wl, n, seed=11 + n)
+        t0 = time.perf_counter()
+        total, _ = run(xs, ys)
+        dt = time.perf_counter() - t0
+        if dt >= budget_s / 4 or n >= (1 << 17):
+            break
+        n = min(1 << 17, int(n * max(2.0, (budget_s / 4) / max(dt, 1e-3))))
+    return {"value": total / dt / 1e9, "unit": "Gpixel-iter/s", "cores": threads, "kind": kind,
+            "sample": f"{n} seeded pixels x {SPP} jittered samples of the frame, maxIter {MAX_ITER}, FP64, "
+                      f"{total} pixel-iterations in {dt:.2f} s"}
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    wl = workload()
+    kind, threads, run = _cpu_impl()
+    # size one step at ~8 s of host work
+    n = 512
+    _, xs, ys = cpu_sample_points(wl, n, seed=101)
+    t0 = time.perf_counter()
+    run(xs, ys)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    n = max(256, min(1 << 18, int(n * 8.0 / dt)))
+    pts = [cpu_sample_points(wl, n, seed=200 + k) for k in range(args.warmup + args.steps)]
+    for k in range(args.warmup):
+        run(pts[k][1], pts[k][2])
+    total, elapsed, lat = 0, 0.0, []
+    for k in range(args.steps):
+        _, xs, ys = pts[args.warmup + k]
+        t0 = time.perf_counter()
+        t, _ = run(xs, ys)
+        d = time.perf_counter() - t0
+        total += t
+        elapsed += d
+        lat.append(d * 1e3)
+    value = total / elapsed / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Gpixel-iter/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded boundary centre, seeded jitter offsets",
+            "config": {"workload": f"Mandelbrot {W}x{H} span {SPAN} maxIter {MAX_ITER} {SPP} jittered spp "
+                                   f"(each step: {n} seeded pixels of that frame on the host cores)",
+                       "parallelism": "host threads"},
+            "cpu_baseline": {"value": value, "unit": "Gpixel-iter/s", "cores": threads, "kind": kind,
+                             "sample": f"{n} seeded pixels x {SPP} samples per step"},
+            "e2e": {"value": value, "unit": "Gpixel-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import chaos_gb300 as cg
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    wl = workload()
+    # The headline tier is the one that meets the metric's mismatch bar: at this
+    # depth (pixel 2.6e-14, maxIter 20000, centre on the boundary) any change of
+    # rounding flips ~30% of escape counts, so only binary64 with the
+    # reference's rounding (no contraction) is within 0.1% of the FP64 oracle.
+    tier, arith = cg.TIER_F64, cg.ARITH_PARITY
+    desc = frame_desc(cg, wl, tier, arith)
+    dev = torch.device("cuda", local)
+    pal = torch.from_numpy(wl["palette"].view(np.int32)).to(dev)
+    rgba = torch.zeros(W * H, dtype=torch.int32, device=dev)
+    total = torch.zeros(1, dtype=torch.int64, device=dev)
+    out = cg.FrameOut(rgba=rgba.data_ptr(), palette=pal.data_ptr(), palette_len=len(wl["palette"]),
+                      interior_rgba=wl["interior_rgba"], total_iterations=total.data_ptr())
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def frame():
+        total.zero_()
+        cg.render_frame(desc, out, stream=stream, sync=False)
+
+    for _ in range(args.warmup):
+        frame()
+    torch.cuda.synchronize()
+    iters_per_frame = int(total.item())
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(k & 255)
+        starts[k].record(stream)
+        frame()
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    if world > 1:
+        dist.barrier()
+    lat = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    kernel_ms = sum(lat)
+    t = torch.tensor([kernel_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    max_ms = float(t.item())
+    value = iters_per_frame * args.steps * world / (max_ms / 1e3) / 1e9
+
+    # end to end: the host-buffer call a caller without device memory makes
+    host_rgba = np.zeros(W * H, dtype=np.uint32)
+    try:
+        host_rgba = torch.empty(W * H, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    except RuntimeError:
+        pass
+    cg.render_frame_host(desc, wl["palette"], wl["interior_rgba"], host_rgba)  # warm the workspace
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    e2e_iters = 0
+    for _ in range(args.steps):
+        e2e_iters += cg.render_frame_host(desc, wl["palette"], wl["interior_rgba"], host_rgba)
+    e2e_s = time.perf_counter() - e0
+    e2e_value = e2e_iters / e2e_s / 1e9
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    # roofline: FP64 pipe
+    peak = cg.measure_fma_peak(cg.TIER_F64)  # FLOP/s with an FMA = 2
+    # rounded arithmetic: x*x, y*y, xx-yy, +cx, x+x, *y, +cy = 7 FP64-pipe
+    # instructions per untested step; the escape test adds 1 add per 16 steps
+    ops_per_iter = 7
+    achieved_ops = iters_per_frame / (kernel_ms / args.steps / 1e3) * ops_per_iter
+    roof = {"bound": "fp64-pipe", "achieved": achieved_ops / 1e12, "peak": peak / 2 / 1e12, "unit": "Top/s",
+            "frac": achieved_ops / (peak / 2), "traffic": None,
+            "peak_source": "measured in this run: chaos_measure_fma_peak (full-occupancy DFMA chains)",
+            "ops_per_iteration": ops_per_iter, "kernel": "k_frame<double,PARITY,mandelbrot>",
+            "note": "one FP64-pipe instruction = 1 op; achieved = pixel-iterations/s x ops_per_iteration"}
+
+    # CPU leg: reference per-sample function on host cores + FP64-oracle mismatch
+    base = cpu_baseline(wl)
+    kind, _, run = _cpu_impl()
+    pix = sample_pixels(MISMATCH_SAMPLE_PIXELS)
+    counts = torch.zeros(W * H * SPP, dtype=torch.int32, device=dev)
+    chk = cg.FrameOut(counts=counts.data_ptr())
+    cg.render_frame(desc, chk, stream=stream)
+    gpu_counts = counts.cpu().numpy().view(np.uint32).reshape(W * H, SPP)[pix].ravel()
+    _, xs, ys = cpu_sample_points(wl, MISMATCH_SAMPLE_PIXELS, seed=7)
+    _, ref_counts = run(xs, ys)
+    mismatch = float((gpu_counts != ref_counts).mean())
+
+    # the other binary64 arithmetic, for reference: throughput and mismatch
+    tiers = {}
+    for name, t_, a_ in (("f64-fma", cg.TIER_F64, cg.ARITH_FMA),):
+        d2 = frame_desc(cg, wl, t_, a_)
+        o2 = cg.FrameOut(counts=counts.data_ptr(), total_iterations=total.data_ptr())
+        total.zero_()
+        cg.render_frame(d2, o2, stream=stream)  # warm
+        total.zero_()
+        e_s, e_e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e_s.record(stream)
+        cg.render_frame(d2, o2, stream=stream, sync=False)
+        e_e.record(stream)
+        torch.cuda.synchronize()
+        ms = e_s.elapsed_time(e_e)
+        c2 = counts.cpu().numpy().view(np.uint32).reshape(W * H, SPP)[pix].ravel()
+        tiers[name] = {"value": int(total.item()) / (ms / 1e3) / 1e9, "unit": "Gpixel-iter/s", "ms_per_frame": ms,
+                       "escape_count_mismatch_rate": float((c2 != ref_counts).mean())}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "Gpixel-iter/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded boundary centre, seeded jitter offsets, seeded palette",
+        "config": {"workload": f"Mandelbrot {W}x{H} span {SPAN} maxIter {MAX_ITER} {SPP} jittered spp, "
+                               f"256-entry palette with linear interpolation",
+                   "center": list(wl["center"]), "tier": "f64", "arith": "fma",
+                   "l2": "flushed between steps (256 MiB write, outside the events)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "pixel_iterations_per_step": iters_per_frame,
+        "frame_latency_ms": {"p50": statistics.median(lat), "p99": float(np.percentile(lat, 99)),
+                             "max": max(lat)},
+        "mismatch": {"vs": f"FP64 oracle ({kind}: computeFractal<double>, rounded arithmetic)",
+                     "samples": int(len(ref_counts)), "escape_count_mismatch_rate": mismatch},
+        "tiers": tiers,
+        "roofline": roof,
+        "cpu_baseline": base,
+        "e2e": {"value": e2e_value, "unit": "Gpixel-iter/s", "h2d_bytes_per_step": 4 * len(wl["palette"]),
+                "d2h_bytes_per_step": 4 * W * H + 8, "call": "chaos_render_frame_host"},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+        "wall_s_timed": wall,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,22 @@
+"""chaos_gb300 -- GB300 (sm_103a) escape-time renderer, a drop-in for
+chaos-ultra's fractal-kernel path.
+
+Python face of libchaos_gb300.so: `Module` mirrors FractalRenderingModule and
+its kernels, `Renderer` mirrors CudaFractalRenderer (renderQuality /
+renderFast), `render_frame` is the jittered-supersampling frame path.  Device
+buffers are passed as raw device pointers (e.g. torch tensor data_ptr()).
+"""
+from ._native import (ARITH_FMA, ARITH_PARITY, DROPIN_DIR, DROPIN_PARITY_DIR, FLAG_ADAPTIVE_SS, FLAG_FOVEATION,
+                      FLAG_IS_ZOOMING, FLAG_SAMPLE_REUSE, FLAG_VISUALIZE_SAMPLE_COUNT, FLAG_ZOOMING_IN, JULIA,
+                      LIB_PATH, MANDELBROT, PRECISION_DOUBLE, PRECISION_SINGLE, PRECISION_TOO_BIG, SAMPLES_CENTER,
+                      SAMPLES_JITTER, TIER_F32, TIER_F64, ChaosError, FrameDesc, FrameOut, RenderingModel, lib)
+from .api import (Module, Renderer, available_fractals, measure_fma_peak, render_frame, render_frame_host,
+                  select_precision, version)
+
+__all__ = [
+    "ARITH_FMA", "ARITH_PARITY", "DROPIN_DIR", "DROPIN_PARITY_DIR", "FLAG_ADAPTIVE_SS", "FLAG_FOVEATION",
+    "FLAG_IS_ZOOMING", "FLAG_SAMPLE_REUSE", "FLAG_VISUALIZE_SAMPLE_COUNT", "FLAG_ZOOMING_IN", "JULIA", "LIB_PATH",
+    "MANDELBROT", "PRECISION_DOUBLE", "PRECISION_SINGLE", "PRECISION_TOO_BIG", "SAMPLES_CENTER", "SAMPLES_JITTER",
+    "TIER_F32", "TIER_F64", "ChaosError", "FrameDesc", "FrameOut", "RenderingModel", "lib", "Module", "Renderer",
+    "available_fractals", "measure_fma_peak", "render_frame", "render_frame_host", "select_precision", "version",
+]

@@ -1,0 +1,155 @@
+"""ctypes declarations of libchaos_gb300.so (include/chaos_gb300.h).
+
+The library is built in-tree by chaos-ultra_gb300/build_native.py.  There is
+no Python or CPU fallback: if the shared library is missing, loading fails
+with ChaosError.
+"""
+import ctypes as C
+import os
+import threading
+
+PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_ROOT, "lib", "libchaos_gb300.so")
+DROPIN_DIR = os.path.join(PKG_ROOT, "cudaKernels")
+DROPIN_PARITY_DIR = os.path.join(PKG_ROOT, "cudaKernels_parity")
+
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_CUDA = 2
+ERR_UNKNOWN_FRACTAL = 3
+ERR_NOT_FOUND = 4
+ERR_STATE = 5
+ERR_OUT_OF_MEMORY = 6
+ERR_TIMEOUT = 7
+ERR_UNSUPPORTED = 8
+
+FLAG_ADAPTIVE_SS = 1 << 0
+FLAG_VISUALIZE_SAMPLE_COUNT = 1 << 1
+FLAG_FOVEATION = 1 << 2
+FLAG_SAMPLE_REUSE = 1 << 3
+FLAG_IS_ZOOMING = 1 << 4
+FLAG_ZOOMING_IN = 1 << 5
+
+ARITH_FMA = 0
+ARITH_PARITY = 1
+
+PRECISION_SINGLE = 0
+PRECISION_DOUBLE = 1
+PRECISION_TOO_BIG = 2
+
+SAMPLES_CENTER = 0
+SAMPLES_JITTER = 1
+TIER_F32 = 0
+TIER_F64 = 1
+
+MANDELBROT = 0
+JULIA = 1
+
+
+class ChaosError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"chaos_gb300 error {code}: {message}")
+        self.code = code
+        self.message = message
+
+
+class RenderingModel(C.Structure):
+    _fields_ = [
+        ("left_bottom_x", C.c_double), ("left_bottom_y", C.c_double),
+        ("right_top_x", C.c_double), ("right_top_y", C.c_double),
+        ("max_iterations", C.c_uint32), ("max_super_sampling", C.c_float),
+        ("use_adaptive_super_sampling", C.c_uint8), ("visualise_sample_count", C.c_uint8),
+        ("use_foveated_rendering", C.c_uint8), ("use_sample_reuse", C.c_uint8),
+        ("zooming", C.c_uint8), ("zooming_in", C.c_uint8), ("sample_reuse_cache_dirty", C.c_uint8),
+        ("pad_", C.c_uint8),
+        ("mouse_focus_x", C.c_int32), ("mouse_focus_y", C.c_int32),
+        ("arith", C.c_int32), ("floating_point_precision", C.c_int32),
+    ]
+
+
+class FrameDesc(C.Structure):
+    _fields_ = [
+        ("width", C.c_uint32), ("height", C.c_uint32), ("max_iterations", C.c_uint32),
+        ("samples_per_pixel", C.c_uint32), ("sample_mode", C.c_uint32), ("tier", C.c_uint32),
+        ("arith", C.c_int32), ("fractal", C.c_uint32), ("seed", C.c_uint64),
+        ("center_x", C.c_double), ("center_y", C.c_double), ("pixel_size", C.c_double),
+        ("julia_cx", C.c_double), ("julia_cy", C.c_double),
+    ]
+
+
+class FrameOut(C.Structure):
+    _fields_ = [
+        ("counts", C.c_void_p), ("smooth", C.c_void_p), ("pixels", C.c_void_p), ("pixels_pitch", C.c_long),
+        ("rgba", C.c_void_p), ("palette", C.c_void_p), ("palette_len", C.c_uint32),
+        ("interior_rgba", C.c_uint32), ("total_iterations", C.c_void_p),
+    ]
+
+
+_F4 = C.c_float * 4
+_D4 = C.c_double * 4
+_vp = C.c_void_p
+_u32 = C.c_uint32
+_int = C.c_int
+_long = C.c_long
+
+# name -> (restype, argtypes); every symbol declared in include/chaos_gb300.h
+SIGNATURES = {
+    "chaos_last_error": (C.c_char_p, []),
+    "chaos_version": (C.c_char_p, []),
+    "chaos_available_fractals": (C.c_char_p, []),
+    "chaos_module_open": (_int, [C.c_char_p, C.POINTER(_vp)]),
+    "chaos_module_close": (_int, [_vp]),
+    "chaos_module_fractal_name": (C.c_char_p, [_vp]),
+    "chaos_module_write_constant": (_int, [_vp, C.c_char_p, _vp, C.c_size_t]),
+    "chaos_module_set_custom_params": (_int, [_vp, C.c_char_p]),
+    "chaos_module_default_view": (_int, [_vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                         C.POINTER(C.c_double), C.POINTER(_u32), C.POINTER(C.c_float)]),
+    "chaos_render_main_f32": (_int, [_vp, _vp, _long, _u32, _u32, _F4, _u32, C.c_float, _u32, _int, _vp]),
+    "chaos_render_main_f64": (_int, [_vp, _vp, _long, _u32, _u32, _D4, _u32, C.c_float, _u32, _int, _vp]),
+    "chaos_render_advanced_f32": (_int, [_vp, _vp, _long, _u32, _u32, _F4, _u32, C.c_float, _u32, _F4, _vp, _long,
+                                         _u32, _u32, _int, _vp]),
+    "chaos_render_advanced_f64": (_int, [_vp, _vp, _long, _u32, _u32, _D4, _u32, C.c_float, _u32, _D4, _vp, _long,
+                                         _u32, _u32, _int, _vp]),
+    "chaos_compose": (_int, [_vp, _vp, _long, _vp, _long, _u32, _u32, _vp, _u32, C.c_float, _vp]),
+    "chaos_render_under_sampled": (_int, [_vp, _vp, _long, _u32, _u32, _F4, _u32, _u32, _vp]),
+    "chaos_debug": (_int, [_vp]),
+    "chaos_select_precision": (_int, [_D4, _u32, _u32]),
+    "chaos_renderer_create": (_int, [_vp, C.POINTER(_vp)]),
+    "chaos_renderer_initialize": (_int, [_vp, _u32, _u32, _vp, _u32]),
+    "chaos_renderer_free_resources": (_int, [_vp]),
+    "chaos_renderer_render_quality": (_int, [_vp, C.POINTER(RenderingModel)]),
+    "chaos_renderer_render_fast": (_int, [_vp, C.POINTER(RenderingModel)]),
+    "chaos_renderer_output": (_int, [_vp, C.POINTER(_vp), C.POINTER(_long), C.POINTER(_vp), C.POINTER(_long)]),
+    "chaos_renderer_read_output": (_int, [_vp, _vp]),
+    "chaos_renderer_destroy": (_int, [_vp]),
+    "chaos_render_frame_async": (_int, [C.POINTER(FrameDesc), C.POINTER(FrameOut), _vp]),
+    "chaos_render_frame": (_int, [C.POINTER(FrameDesc), C.POINTER(FrameOut), _vp]),
+    "chaos_render_frame_host": (_int, [C.POINTER(FrameDesc), _vp, _u32, _u32, _vp, C.POINTER(C.c_ulonglong), _vp]),
+    "chaos_measure_fma_peak": (_int, [_u32, C.POINTER(C.c_double)]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib():
+    """The loaded library (loaded once).  Raises ChaosError if it is not built."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise ChaosError(ERR_UNSUPPORTED, f"{LIB_PATH} is not built; run __graft_entry__.build()")
+            L = C.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != OK:
+        msg = lib().chaos_last_error().decode(errors="replace")
+        raise ChaosError(rc, msg)
+    return rc

@@ -1,0 +1,174 @@
+"""Thin object layer over the C ABI (names follow the reference's Java classes)."""
+import ctypes as C
+
+from ._native import (ARITH_FMA, FrameDesc, FrameOut, RenderingModel, _D4, _F4, check, lib)
+
+
+def version():
+    return lib().chaos_version().decode()
+
+
+def available_fractals():
+    return lib().chaos_available_fractals().decode().split(",")
+
+
+def select_precision(rect, width, height):
+    """RenderingKernel.isSegmentBoundsAt{Float,Double}Limit -> PRECISION_*."""
+    return lib().chaos_select_precision(_D4(*rect), width, height)
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    return C.c_void_p(int(getattr(stream, "cuda_stream", stream)))
+
+
+class Module:
+    """FractalRenderingModule of one fractal (J/cudarenderer/FractalRenderingModule.java)."""
+
+    def __init__(self, fractal_name):
+        h = C.c_void_p()
+        check(lib().chaos_module_open(fractal_name.encode(), C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().chaos_module_close(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def fractal_name(self):
+        return lib().chaos_module_fractal_name(self.handle).decode()
+
+    def write_constant(self, name, data: bytes):
+        buf = C.create_string_buffer(bytes(data), len(data))
+        check(lib().chaos_module_write_constant(self.handle, name.encode(), buf, len(data)))
+
+    def set_custom_params(self, text):
+        check(lib().chaos_module_set_custom_params(self.handle, text.encode()))
+
+    def default_view(self):
+        cx, cy, z = C.c_double(), C.c_double(), C.c_double()
+        mi, ss = C.c_uint32(), C.c_float()
+        check(lib().chaos_module_default_view(self.handle, C.byref(cx), C.byref(cy), C.byref(z), C.byref(mi),
+                                              C.byref(ss)))
+        return cx.value, cy.value, z.value, mi.value, ss.value
+
+    # fractalRenderMain{Float,Double}
+    def render_main(self, out_ptr, pitch, width, height, rect, max_iter, max_ss, flags, double=False,
+                    arith=ARITH_FMA, stream=None):
+        L = lib()
+        if double:
+            check(L.chaos_render_main_f64(self.handle, out_ptr, pitch, width, height, _D4(*rect), max_iter, max_ss,
+                                          flags, arith, _stream(stream)))
+        else:
+            check(L.chaos_render_main_f32(self.handle, out_ptr, pitch, width, height, _F4(*rect), max_iter, max_ss,
+                                          flags, arith, _stream(stream)))
+
+    # fractalRenderAdvanced{Float,Double}
+    def render_advanced(self, out_ptr, pitch, width, height, rect, max_iter, max_ss, flags, rect_reused, in_ptr,
+                        in_pitch, focus, double=False, arith=ARITH_FMA, stream=None):
+        L = lib()
+        if double:
+            check(L.chaos_render_advanced_f64(self.handle, out_ptr, pitch, width, height, _D4(*rect), max_iter,
+                                              max_ss, flags, _D4(*rect_reused), in_ptr, in_pitch, focus[0], focus[1],
+                                              arith, _stream(stream)))
+        else:
+            check(L.chaos_render_advanced_f32(self.handle, out_ptr, pitch, width, height, _F4(*rect), max_iter,
+                                              max_ss, flags, _F4(*rect_reused), in_ptr, in_pitch, focus[0], focus[1],
+                                              arith, _stream(stream)))
+
+    def compose(self, in_ptr, pitch, out_ptr, out_pitch, width, height, palette_ptr, palette_len, max_ss,
+                stream=None):
+        check(lib().chaos_compose(self.handle, in_ptr, pitch, out_ptr, out_pitch, width, height, palette_ptr,
+                                  palette_len, max_ss, _stream(stream)))
+
+    def render_under_sampled(self, out_ptr, pitch, width, height, rect, max_iter, level, stream=None):
+        check(lib().chaos_render_under_sampled(self.handle, out_ptr, pitch, width, height, _F4(*rect), max_iter,
+                                               level, _stream(stream)))
+
+    def debug(self):
+        check(lib().chaos_debug(self.handle))
+
+
+class Renderer:
+    """CudaFractalRenderer with a headless RGBA8 output (J/cudarenderer/CudaFractalRenderer.java)."""
+
+    def __init__(self, module: Module):
+        h = C.c_void_p()
+        check(lib().chaos_renderer_create(module.handle, C.byref(h)))
+        self.handle = h
+        self.module = module
+
+    def initialize(self, width, height, palette):
+        import numpy as np
+        pal = np.ascontiguousarray(palette, dtype=np.uint32)
+        check(lib().chaos_renderer_initialize(self.handle, width, height, pal.ctypes.data_as(C.c_void_p), len(pal)))
+        self.width, self.height = width, height
+
+    def free_resources(self):
+        check(lib().chaos_renderer_free_resources(self.handle))
+
+    def render_quality(self, model: RenderingModel):
+        check(lib().chaos_renderer_render_quality(self.handle, C.byref(model)))
+
+    def render_fast(self, model: RenderingModel):
+        check(lib().chaos_renderer_render_fast(self.handle, C.byref(model)))
+
+    def output(self):
+        rgba, rp, prim, pp = C.c_void_p(), C.c_long(), C.c_void_p(), C.c_long()
+        check(lib().chaos_renderer_output(self.handle, C.byref(rgba), C.byref(rp), C.byref(prim), C.byref(pp)))
+        return rgba.value, rp.value, prim.value, pp.value
+
+    def read_output(self):
+        import numpy as np
+        out = np.zeros((self.height, self.width), dtype=np.uint32)
+        check(lib().chaos_renderer_read_output(self.handle, out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def close(self):
+        if self.handle:
+            lib().chaos_renderer_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def render_frame(desc: FrameDesc, out: FrameOut, stream=None, sync=True):
+    fn = lib().chaos_render_frame if sync else lib().chaos_render_frame_async
+    check(fn(C.byref(desc), C.byref(out), _stream(stream)))
+
+
+def render_frame_host(desc: FrameDesc, palette, interior_rgba, rgba_host, stream=None):
+    """chaos_render_frame_host: palette and image in host memory (numpy arrays).
+    Returns the frame's pixel-iteration count."""
+    import numpy as np
+    pal = np.ascontiguousarray(palette, dtype=np.uint32)
+    assert rgba_host.dtype == np.uint32 and rgba_host.flags.c_contiguous
+    total = C.c_ulonglong()
+    check(lib().chaos_render_frame_host(C.byref(desc), pal.ctypes.data_as(C.c_void_p), len(pal), interior_rgba,
+                                        rgba_host.ctypes.data_as(C.c_void_p), C.byref(total), _stream(stream)))
+    return total.value
+
+
+def measure_fma_peak(tier):
+    """Measured FMA throughput (FLOP/s, FMA = 2) of the current device for TIER_F32 / TIER_F64."""
+    v = C.c_double()
+    check(lib().chaos_measure_fma_peak(tier, C.byref(v)))
+    return v.value

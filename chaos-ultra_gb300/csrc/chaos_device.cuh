@@ -1,0 +1,502 @@
+// chaos_device.cuh -- device building blocks of the escape-time path (sm_103a).
+//
+// Shared by the drop-in module (dropin_module.cu, the seven kernels the Java
+// host loads by name) and by the library kernels (chaos_kernels.cu).
+//
+// Reference behaviour restated here (paths relative to the chaos-ultra root,
+// gen.cu = src/main/cuda/fractalRendererGeneric.cu):
+//   escape loop ........ src/main/cuda/fractals/mandelbrot.cu:11-25, julia.cu:5-17
+//   sample pattern ..... gen.cu:85-155 (sampleTheFractal), gen.cu:24-34 (computeDispersion)
+//   warp tile .......... gen.cu:36-53 (getImageIndexes: one warp = one 8x4 pixel tile)
+//   sample reuse ....... gen.cu:194-203, 259-302, 307-368
+//   foveation .......... gen.cu:209-257
+//   compose / colorize . gen.cu:455-475, 67-77, mandelbrot.cu:27-35
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace chaos {
+
+// 16-byte per-pixel record, identical in layout to pixel_info_t
+// (src/main/cuda/helpers.cuh:106-130): value@0, weight@4, isReused@8, weightOfNewSamples@12.
+struct PixelInfo {
+    float value;
+    float weight;
+    uint8_t is_reused;
+    uint8_t pad[3];
+    float weight_of_new_samples;
+};
+static_assert(sizeof(PixelInfo) == 16, "pixel_info_t is 16 bytes");
+
+enum Arith { ARITH_PARITY = 0, ARITH_FMA = 1 };
+enum FractalKind { FRACTAL_MANDELBROT = 0, FRACTAL_JULIA = 1 };
+
+// kernel flag bits, gen.cu:157-161 (bit 1 is the Java-side "visualise" flag)
+constexpr uint32_t FLAG_ADAPTIVE_SS = 1u << 0;
+constexpr uint32_t FLAG_FOVEATION = 1u << 2;
+constexpr uint32_t FLAG_SAMPLE_REUSE = 1u << 3;
+constexpr uint32_t FLAG_IS_ZOOMING = 1u << 4;
+constexpr uint32_t FLAG_ZOOMING_IN = 1u << 5;
+
+constexpr uint32_t MAX_SUPER_SAMPLING = 64;  // gen.cu:12
+constexpr uint32_t ADAPTIVE_THRESHOLD = 10;  // gen.cu:93
+
+// Iterations run between two escape tests on the fast path (see escape()).
+constexpr int ESCAPE_BLOCK = 16;
+
+// ---------------------------------------------------------------------------
+// Correctly rounded scalar operations.  Every product and sum is rounded on its
+// own unless an fma is written out, so the compiler cannot contract (the
+// parity arithmetic matches the reference built with --fmad=false).
+// ---------------------------------------------------------------------------
+template <class R> struct Op;
+template <> struct Op<float> {
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+    static __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+};
+template <> struct Op<double> {
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+    static __device__ __forceinline__ double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+};
+
+// |z|^2 as the escape test computes it.
+template <class R, int A> __device__ __forceinline__ R radius2(R x, R y)
+{
+    using O = Op<R>;
+    if (A == ARITH_PARITY) return O::add(O::mul(x, x), O::mul(y, y));
+    return O::fma(x, x, O::mul(y, y));
+}
+
+// One step of z <- z^2 + c.
+//   parity: x' = (x*x - y*y) + cx, y' = (2*x)*y + cy  (mandelbrot.cu:17-18 order)
+//   fma:    x' = fma(x, x, fma(-y, y, cx)), y' = fma(x + x, y, cy)  (4 FP32-pipe ops)
+template <class R, int A> __device__ __forceinline__ void step(R &x, R &y, R cx, R cy)
+{
+    using O = Op<R>;
+    if (A == ARITH_PARITY) {
+        R xx = O::mul(x, x), yy = O::mul(y, y);
+        R xn = O::add(O::sub(xx, yy), cx);
+        y = O::add(O::mul(O::mul(R(2), x), y), cy);
+        x = xn;
+    } else {
+        R t = O::fma(-y, y, cx);
+        R xn = O::fma(x, x, t);
+        y = O::fma(O::add(x, x), y, cy);
+        x = xn;
+    }
+}
+
+// Escape loop with the reference's semantics:
+//     i = 0; while (i < max_iter && r2(z) < 4) { z = z^2 + c; ++i; }  return i
+// run as blocks of ESCAPE_BLOCK untested steps.  A block is kept when its last
+// state still tests below 4; otherwise the state rolls back to the block start
+// and the steps are redone one test at a time.  This is exact when |c| <= 1.9:
+// once a computed |z|^2 reaches 4, |z'| >= 4 - 1.9 = 2.1 and |z| keeps growing
+// until it overflows to inf/NaN, and neither tests below 4, so a block whose
+// last state tests below 4 contains no escape.  For |c| > 1.9 `blockable` is
+// false and every step is tested.  r2_exit is r2 of the final state.
+template <class R, int A>
+__device__ __forceinline__ uint32_t escape(uint32_t max_iter, R x, R y, R cx, R cy, bool blockable, R &r2_exit)
+{
+    R r2 = radius2<R, A>(x, y);
+    if (max_iter == 0 || !(r2 < R(4))) {
+        r2_exit = r2;
+        return 0;
+    }
+    uint32_t i = 0;
+    if (blockable) {
+        while (max_iter - i >= (uint32_t)ESCAPE_BLOCK) {
+            R sx = x, sy = y;
+#pragma unroll
+            for (int k = 0; k < ESCAPE_BLOCK; k++) step<R, A>(x, y, cx, cy);
+            if (!(radius2<R, A>(x, y) < R(4))) {
+                x = sx;
+                y = sy;
+                break;
+            }
+            i += ESCAPE_BLOCK;
+        }
+    }
+    while (i < max_iter) {
+        step<R, A>(x, y, cx, cy);
+        ++i;
+        r2 = radius2<R, A>(x, y);
+        if (!(r2 < R(4))) break;
+    }
+    r2_exit = r2;
+    return i;
+}
+
+template <class R> __device__ __forceinline__ bool blockable_c(R cx, R cy)
+{
+    return radius2<R, ARITH_PARITY>(cx, cy) <= R(3.61);
+}
+
+// computeFractal (mandelbrot.cu:11-25, julia.cu:5-17) as an unsigned escape
+// value: Mandelbrot maps an interior point (i == maxIterations) to 0, Julia
+// returns i.  `jc` is julia_c already converted to Real.
+template <class R, int A, int F> __device__ __forceinline__ uint32_t compute_fractal(uint32_t max_iter, R px, R py, R jcx, R jcy)
+{
+    R r2;
+    if (F == FRACTAL_MANDELBROT) {
+        uint32_t i = escape<R, A>(max_iter, R(0), R(0), px, py, blockable_c(px, py), r2);
+        return i == max_iter ? 0u : i;
+    }
+    return escape<R, A>(max_iter, px, py, jcx, jcy, blockable_c(jcx, jcy), r2);
+}
+
+// ---------------------------------------------------------------------------
+// Reference-mode sampling (sampleTheFractal, gen.cu:85-155)
+// ---------------------------------------------------------------------------
+
+// Plane rectangle as the kernel receives it (Rectangle<Real>): left-bottom and
+// right-top corners.  4-byte (float) or 8-byte (double) aligned, as in the
+// reference's parameter layout.
+template <class R> struct Rect {
+    R lbx, lby, rtx, rty;
+};
+
+struct UInt2 {
+    uint32_t x, y;
+};
+
+template <class R> struct SampleGeometry {
+    R lbx, rty;  // image left-top corner
+    R psx, psy;  // pixel size, image.size() / gridSize (gen.cu:97)
+    uint32_t max_iter;
+    R jcx, jcy;
+};
+
+template <class R>
+__device__ __forceinline__ SampleGeometry<R> make_geometry(const Rect<R> &r, UInt2 size, uint32_t max_iter, double jcx,
+                                                            double jcy)
+{
+    using O = Op<R>;
+    SampleGeometry<R> g;
+    g.lbx = r.lbx;
+    g.rty = r.rty;
+    g.psx = O::div(O::sub(r.rtx, r.lbx), (R)size.x);
+    g.psy = O::div(O::sub(r.rty, r.lby), (R)size.y);
+    g.max_iter = max_iter;
+    g.jcx = (R)jcx;
+    g.jcy = (R)jcy;
+    return g;
+}
+
+// Sample offset i (gen.cu:104-117) and plane point (gen.cu:119-124).
+template <class R> __device__ __forceinline__ void sample_point(const SampleGeometry<R> &g, uint32_t px, uint32_t py,
+                                                                uint32_t i, float sample_count_f, R &cx, R &cy)
+{
+    using O = Op<R>;
+    const uint32_t skip_first = 2;
+    R dx, dy;
+    if (i <= skip_first) {
+        dx = dy = O::div((R)i, (R)(skip_first + 1));
+    } else {
+        float spr_f = __fsqrt_rn(__fsub_rn(sample_count_f, (float)skip_first));
+        uint32_t spr = (uint32_t)roundf(spr_f);
+        dx = (R)__fdiv_rn((float)((i - skip_first) % spr), spr_f);
+        dy = (R)__fdiv_rn((float)((i - skip_first) / spr), spr_f);
+    }
+    cx = O::add(g.lbx, O::mul(O::add((R)px, dx), g.psx));
+    cy = O::add(g.rty, O::mul(-O::add((R)py, dy), g.psy));
+}
+
+// computeDispersion (gen.cu:24-34) over the first data_length stored samples.
+// The reference stores 10 samples and reads past them when data_length > 10;
+// those reads are skipped here.
+__device__ __forceinline__ float dispersion(const float *data, uint32_t data_length, float mean)
+{
+    float variance = 0.f;
+    uint32_t m = data_length < ADAPTIVE_THRESHOLD ? data_length : ADAPTIVE_THRESHOLD;
+    for (uint32_t k = 0; k < m; k++) {
+        float d = __fsub_rn(data[k], mean);
+        variance = __fadd_rn(variance, __fmul_rn(d, d));
+    }
+    variance = __fdiv_rn(variance, (float)(uint32_t)(data_length - 1u));
+    return __fdiv_rn(variance, mean);
+}
+
+// sampleTheFractal for the lanes of `mask`, which call it together with the
+// same sample_count_f.  Lanes with valid == false (pixels outside the image)
+// take part in the votes as "yes" and compute nothing, which is how the
+// reference's exited lanes drop out of __activemask().
+template <class R, int A, int F>
+__device__ uint32_t sample_the_fractal(const SampleGeometry<R> &g, uint32_t px, uint32_t py, float &sample_count_f,
+                                       bool adaptive, bool valid, uint32_t mask)
+{
+    if (sample_count_f < 1.f) {  // gen.cu:87-90
+        sample_count_f = 0.f;
+        return 0;
+    }
+    uint32_t sc = (uint32_t)roundf(sample_count_f);
+    sc = sc < MAX_SUPER_SAMPLING ? sc : MAX_SUPER_SAMPLING;
+    float samples[ADAPTIVE_THRESHOLD];
+    uint32_t sum = 0;
+    for (uint32_t i = 0; i < sc; i++) {
+        uint32_t e = 0;
+        if (valid) {
+            R cx, cy;
+            sample_point(g, px, py, i, sample_count_f, cx, cy);
+            e = compute_fractal<R, A, F>(g.max_iter, cx, cy, g.jcx, g.jcy);
+        }
+        sum += e;
+        if (i < ADAPTIVE_THRESHOLD) samples[i] = (float)e;
+        if ((adaptive && (i > 0 && i < ADAPTIVE_THRESHOLD)) || (i == sc / 2)) {
+            float mean = (float)(sum / (i + 1));
+            float disp = dispersion(samples, i, mean);
+            if (i == 1 && __all_sync(mask, !valid || fabsf(__fsub_rn(samples[0], samples[1])) < 1.19209290e-7f))
+                sc = i + 1;
+            else if (__all_sync(mask, !valid || disp < 0.01f))
+                sc = i + 1;
+            else if (__all_sync(mask, !valid || disp <= 1.f) && i >= sc / 2)
+                sc = i + 1;
+        }
+    }
+    sample_count_f = (float)sc;
+    return sum / sc;
+}
+
+// Pixel of lane `lane` in the 8x4 warp tile whose top-left pixel is (x0, y0):
+// the lane order of getImageIndexes (gen.cu:43-53) with blockDim.x == 32.
+__device__ __forceinline__ UInt2 tile_pixel(uint32_t x0, uint32_t y0, uint32_t lane)
+{
+    UInt2 p;
+    p.x = x0 + 4 * (lane >> 4) + (lane & 3);
+    p.y = y0 + ((lane >> 2) & 3);
+    return p;
+}
+
+__device__ __forceinline__ PixelInfo *pixel_ptr(void *base, long pitch, uint32_t x, uint32_t y)
+{
+    return reinterpret_cast<PixelInfo *>(static_cast<char *>(base) + (size_t)y * (size_t)pitch) + x;
+}
+__device__ __forceinline__ const PixelInfo *pixel_ptr(const void *base, long pitch, uint32_t x, uint32_t y)
+{
+    return reinterpret_cast<const PixelInfo *>(static_cast<const char *>(base) + (size_t)y * (size_t)pitch) + x;
+}
+
+// Store a whole 16-byte record (padding bytes zero) with one vector store when
+// the address allows it.
+__device__ __forceinline__ void store_pixel(PixelInfo *p, const PixelInfo &v)
+{
+    uint32_t w2 = (uint32_t)v.is_reused;
+    if ((reinterpret_cast<uintptr_t>(p) & 15u) == 0) {
+        uint4 u = make_uint4(__float_as_uint(v.value), __float_as_uint(v.weight), w2,
+                             __float_as_uint(v.weight_of_new_samples));
+        *reinterpret_cast<uint4 *>(p) = u;
+    } else {
+        uint32_t *q = reinterpret_cast<uint32_t *>(p);
+        q[0] = __float_as_uint(v.value);
+        q[1] = __float_as_uint(v.weight);
+        q[2] = w2;
+        q[3] = __float_as_uint(v.weight_of_new_samples);
+    }
+}
+
+__device__ __forceinline__ PixelInfo load_pixel(const PixelInfo *p)
+{
+    PixelInfo v;
+    uint4 u;
+    if ((reinterpret_cast<uintptr_t>(p) & 15u) == 0) {
+        u = __ldg(reinterpret_cast<const uint4 *>(p));
+    } else {
+        const uint32_t *q = reinterpret_cast<const uint32_t *>(p);
+        u = make_uint4(q[0], q[1], q[2], q[3]);
+    }
+    v.value = __uint_as_float(u.x);
+    v.weight = __uint_as_float(u.y);
+    v.is_reused = (uint8_t)(u.z & 0xffu);
+    v.pad[0] = v.pad[1] = v.pad[2] = 0;
+    v.weight_of_new_samples = __uint_as_float(u.w);
+    return v;
+}
+
+__device__ __forceinline__ PixelInfo make_pixel(float value, float weight)
+{
+    PixelInfo p;
+    p.value = value;
+    p.weight = weight;
+    p.is_reused = 0;
+    p.pad[0] = p.pad[1] = p.pad[2] = 0;
+    p.weight_of_new_samples = 0.f;
+    return p;
+}
+
+// fractalRenderMain for one lane of an 8x4 warp tile (gen.cu:168-181).
+template <class R, int A, int F>
+__device__ __forceinline__ void render_main_tile(const SampleGeometry<R> &g, void *out, long pitch, UInt2 size,
+                                                 uint32_t x0, uint32_t y0, uint32_t lane, float max_ss, uint32_t flags)
+{
+    UInt2 p = tile_pixel(x0, y0, lane);
+    bool valid = p.x < size.x && p.y < size.y;
+    float sc = max_ss;
+    uint32_t result = sample_the_fractal<R, A, F>(g, p.x, p.y, sc, (flags & FLAG_ADAPTIVE_SS) != 0, valid, 0xffffffffu);
+    if (valid) store_pixel(pixel_ptr(out, pitch, p.x, p.y), make_pixel((float)result, sc));
+}
+
+// ---------------------------------------------------------------------------
+// Sample reuse and foveation (fractalRenderAdvanced, gen.cu:194-368)
+// ---------------------------------------------------------------------------
+
+// getWarpingOriginOfSampleReuse, gen.cu:194-203
+template <class R>
+__device__ __forceinline__ void warping_origin(UInt2 p, UInt2 grid, const Rect<R> &cur, const Rect<R> &old, float &ox,
+                                               float &oy)
+{
+    using O = Op<R>;
+    uint32_t qy = grid.y - p.y;
+    R ppx = O::add(O::mul(O::div((R)p.x, (R)grid.x), O::sub(cur.rtx, cur.lbx)), cur.lbx);
+    R ppy = O::add(O::mul(O::div((R)qy, (R)grid.y), O::sub(cur.rty, cur.lby)), cur.lby);
+    R rx = O::div(O::sub(ppx, old.lbx), O::sub(old.rtx, old.lbx));
+    R ry = O::div(O::sub(ppy, old.lby), O::sub(old.rty, old.lby));
+    ox = __fmul_rn((float)rx, (float)grid.x);
+    float oyv = __fmul_rn((float)ry, (float)grid.y);
+    oy = __fsub_rn((float)grid.y, oyv);
+}
+
+// readFromArrayUsingFiltering<float>, gen.cu:259-302
+__device__ __forceinline__ void read_filtered(const void *in, long pitch, float x, float y, float &value, float &weight)
+{
+    uint32_t i = (uint32_t)floorf(x), j = (uint32_t)floorf(y);
+    float alpha = __fsub_rn(x, (float)i), beta = __fsub_rn(y, (float)j);
+    PixelInfo a = load_pixel(pixel_ptr(in, pitch, i, j));
+    PixelInfo b = load_pixel(pixel_ptr(in, pitch, i + 1, j));
+    PixelInfo c = load_pixel(pixel_ptr(in, pitch, i, j + 1));
+    PixelInfo d = load_pixel(pixel_ptr(in, pitch, i + 1, j + 1));
+    float oa = __fsub_rn(1.f, alpha), ob = __fsub_rn(1.f, beta);
+    float w00 = __fmul_rn(oa, ob), w10 = __fmul_rn(alpha, ob), w01 = __fmul_rn(oa, beta), w11 = __fmul_rn(alpha, beta);
+    float r = __fadd_rn(__fmul_rn(w00, a.value), __fmul_rn(w10, b.value));
+    r = __fadd_rn(r, __fmul_rn(w01, c.value));
+    r = __fadd_rn(r, __fmul_rn(w11, d.value));
+    float w = __fadd_rn(__fmul_rn(w00, a.weight), __fmul_rn(w10, b.weight));
+    w = __fadd_rn(w, __fmul_rn(w01, c.weight));
+    w = __fadd_rn(w, __fmul_rn(w11, d.weight));
+    value = r;
+    weight = w;
+}
+
+// getFoveationAdvisedSampleCount + linearMapping<float>, gen.cu:209-257.
+// Uniform over the 8x4 warp tile (the pixel is snapped to the tile corner).
+__device__ __forceinline__ void foveation(UInt2 p, UInt2 focus, float max_ss, float &advised, bool &inside)
+{
+    const float pi_f = 3.14159265358979f;
+    const float screen_distance = 60.f, pixel_cm = 0.02652f;
+    uint32_t nx = p.x - p.x % 8u, ny = p.y - p.y % 4u;
+    float foveal = max_ss >= 1.f ? 5.5f : (float)__dmul_rn(5.5, (double)max_ss);
+    float peripheral = 60.f;
+    float ddx = __fsub_rn((float)focus.x, (float)nx), ddy = __fsub_rn((float)focus.y, (float)ny);
+    float dist = __fmul_rn(__fsqrt_rn(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy))), pixel_cm);
+    float angle = __fdiv_rn(__fmul_rn(atanf(__fdiv_rn(dist, screen_distance)), 180.f), pi_f);
+    float k = __fdiv_rn(__fsub_rn(0.f, 1.f), __fsub_rn(peripheral, foveal));
+    float q = __fdiv_rn(__fsub_rn(__fmul_rn(peripheral, 1.f), __fmul_rn(0.f, foveal)), __fsub_rn(peripheral, foveal));
+    float lin = __fadd_rn(__fmul_rn(k, angle), q);
+    float rel = (float)fmin(1.0, (double)lin);
+    float adv = __fmul_rn(max_ss, rel);
+    inside = false;
+    if (angle <= foveal) {
+        adv = (float)fmax(1.0, (double)adv);
+        inside = true;
+    }
+    advised = adv;
+}
+
+// fractalRenderAdvanced for one lane of an 8x4 warp tile (gen.cu:307-368).
+// Lanes that reach the same sampleTheFractal call site vote together.
+template <class R, int A, int F>
+__device__ __forceinline__ void render_advanced_tile(const SampleGeometry<R> &g, const Rect<R> &image,
+                                                     const Rect<R> &image_reused, void *out, long pitch, UInt2 size,
+                                                     const void *in, long in_pitch, UInt2 focus, uint32_t x0,
+                                                     uint32_t y0, uint32_t lane, float max_ss, uint32_t flags)
+{
+    UInt2 p = tile_pixel(x0, y0, lane);
+    bool valid = p.x < size.x && p.y < size.y;
+    float advised = max_ss;
+    bool inside = false;
+    bool reusing = false;
+    float reused_v = 0.f, reused_w = 0.f;
+    if (valid) {
+        if ((flags & FLAG_FOVEATION) && (flags & FLAG_IS_ZOOMING) && (flags & FLAG_ZOOMING_IN))
+            foveation(p, focus, max_ss, advised, inside);
+        if (flags & FLAG_SAMPLE_REUSE) {
+            float ox, oy;
+            warping_origin(p, size, image, image_reused, ox, oy);
+            int oix = (int)roundf(ox), oiy = (int)roundf(oy);
+            if (!(oix < 2 || (uint32_t)oix >= size.x - 2 || oiy < 2 || (uint32_t)oiy >= size.y - 2)) {
+                read_filtered(in, in_pitch, ox, oy, reused_v, reused_w);
+                reusing = !(reused_w < 0.1f);
+            }
+        }
+    }
+    bool group_a = valid && reusing && (flags & FLAG_ZOOMING_IN) && inside;
+    bool group_b = valid && !reusing;
+    uint32_t mask_a = __ballot_sync(0xffffffffu, group_a);
+    uint32_t mask_b = __ballot_sync(0xffffffffu, group_b);
+    bool adaptive = (flags & FLAG_ADAPTIVE_SS) != 0;
+    PixelInfo res = make_pixel(0.f, 0.f);
+    if (reusing) {
+        res.value = reused_v;
+        res.weight = reused_w;
+        res.is_reused = 1;
+    }
+    if (group_a) {
+        float sc = advised;
+        float samples = (float)sample_the_fractal<R, A, F>(g, p.x, p.y, sc, adaptive, true, mask_a);
+        float rw = __fmul_rn(reused_w, 0.75f);
+        res.weight_of_new_samples = sc;
+        res.weight = __fadd_rn(rw, sc);
+        res.value = __fdiv_rn(__fadd_rn(__fmul_rn(reused_v, rw), __fmul_rn(samples, sc)), res.weight);
+    }
+    if (group_b) {
+        float sc = advised < 1.f ? 1.f : advised;
+        res.value = (float)sample_the_fractal<R, A, F>(g, p.x, p.y, sc, adaptive, true, mask_b);
+        res.weight = sc;
+    }
+    if (valid) store_pixel(pixel_ptr(out, pitch, p.x, p.y), res);
+}
+
+// ---------------------------------------------------------------------------
+// Compose (gen.cu:455-475)
+// ---------------------------------------------------------------------------
+
+// colorizeSampleCount, gen.cu:67-77.  The channels are `char`: built with the
+// reference's x86-64 toolchain (signed char) the float-to-char conversion
+// saturates at 127, which is what this reproduces.
+__device__ __forceinline__ uint32_t colorize_sample_count(uint32_t sample_count, uint32_t full)
+{
+    sample_count = sample_count < full ? sample_count : full;
+    float rel = __fdiv_rn((float)sample_count, (float)full);
+    float f = __fmul_rn(255.f, rel);
+    int c = (int)f;
+    c = c > 127 ? 127 : c;
+    uint32_t b = (uint32_t)(uint8_t)(int8_t)c;
+    return b | (b << 8) | (b << 16) | 0xff000000u;
+}
+
+// colorize, mandelbrot.cu:27-35 / julia.cu:19-27
+__device__ __forceinline__ uint32_t palette_index(float value, uint32_t palette_len)
+{
+    uint32_t vi = (uint32_t)roundf(value);
+    return palette_len - (vi % palette_len) - 1u;
+}
+
+__device__ __forceinline__ uint32_t compose_pixel(const PixelInfo &p, const uint32_t *palette, uint32_t palette_len,
+                                                  float max_ss, bool visualize)
+{
+    if (visualize) {
+        uint32_t full = (uint32_t)fmax(1.0, (double)max_ss);
+        uint32_t c = colorize_sample_count((uint32_t)p.weight, full);
+        if (p.is_reused) c = colorize_sample_count((uint32_t)p.weight_of_new_samples, full);
+        return c;
+    }
+    return palette[palette_index(p.value, palette_len)];
+}
+
+}  // namespace chaos

@@ -1,0 +1,454 @@
+// chaos_kernels.cu -- library kernels of the escape-time path (sm_103a).
+//
+//   k_main / k_advanced   reference-mode frames (fractalRenderMain/Advanced,
+//                         gen.cu:168-181, 307-368): persistent warps take 8x4
+//                         tiles from a work counter, one tile = one vote group
+//   k_frame               independent samples (pixel centres or jittered):
+//                         persistent warps with per-lane refill, so a lane whose
+//                         sample escaped takes the next one without waiting for
+//                         the slowest lane of its warp
+//   k_compose             palette compose (gen.cu:455-475), HBM-bound
+//   k_under_sampled       fractalRenderUnderSampled (gen.cu:478-503)
+#include <cstdio>
+
+#include "chaos_kernels.cuh"
+
+namespace chaos {
+
+constexpr uint32_t FULL = 0xffffffffu;
+constexpr int PERSIST_THREADS = 256;
+constexpr uint32_t PALETTE_SMEM = 4096;
+
+// ---------------------------------------------------------------------------
+// Reference-mode persistent kernels
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t next_tile(uint32_t *counter, uint32_t lane)
+{
+    uint32_t t = 0;
+    if (lane == 0) t = atomicAdd(counter, 1u);
+    return __shfl_sync(FULL, t, 0);
+}
+
+template <class R, int A, int F> __global__ void __launch_bounds__(PERSIST_THREADS) k_main(MainArgs<R> a)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const SampleGeometry<R> g = make_geometry(a.image, a.size, a.max_iter, a.jcx, a.jcy);
+    for (;;) {
+        uint32_t t = next_tile(a.counter, lane);
+        if (t >= a.n_tiles) break;
+        uint32_t x0 = 8u * (t % a.tiles_x), y0 = 4u * (t / a.tiles_x);
+        render_main_tile<R, A, F>(g, a.out, a.pitch, a.size, x0, y0, lane, a.max_ss, a.flags);
+    }
+}
+
+template <class R, int A, int F> __global__ void __launch_bounds__(PERSIST_THREADS) k_advanced(AdvancedArgs<R> a)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const SampleGeometry<R> g = make_geometry(a.m.image, a.m.size, a.m.max_iter, a.m.jcx, a.m.jcy);
+    for (;;) {
+        uint32_t t = next_tile(a.m.counter, lane);
+        if (t >= a.m.n_tiles) break;
+        uint32_t x0 = 8u * (t % a.m.tiles_x), y0 = 4u * (t / a.m.tiles_x);
+        render_advanced_tile<R, A, F>(g, a.m.image, a.image_reused, a.m.out, a.m.pitch, a.m.size, a.in, a.in_pitch,
+                                      a.focus, x0, y0, lane, a.m.max_ss, a.m.flags);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Independent-sample frames with per-lane refill
+// ---------------------------------------------------------------------------
+
+template <class R> __device__ __forceinline__ R unit_interval(uint64_t h);
+template <> __device__ __forceinline__ float unit_interval<float>(uint64_t h)
+{
+    return (float)(uint32_t)(h >> 40) * 0x1p-24f;
+}
+template <> __device__ __forceinline__ double unit_interval<double>(uint64_t h)
+{
+    return (double)(h >> 11) * 0x1p-53;
+}
+
+template <class R>
+__device__ __forceinline__ void frame_point(const FrameArgs<R> &a, uint32_t pix, uint32_t s, R &cx, R &cy)
+{
+    using O = Op<R>;
+    uint32_t px = pix % a.w, py = pix / a.w;
+    R ox = R(0.5), oy = R(0.5);
+    if (a.mode == SAMPLES_JITTER) {
+        ox = unit_interval<R>(sample_hash(a.seed, pix, s, 0));
+        oy = unit_interval<R>(sample_hash(a.seed, pix, s, 1));
+    }
+    R dxp = O::sub(O::add((R)px, ox), a.half_w);
+    R dyp = O::sub(O::add((R)py, oy), a.half_h);
+    cx = O::fma(dxp, a.ps, a.center_x);
+    cy = O::fma(-dyp, a.ps, a.center_y);
+}
+
+// n + 1 - log2(log2|z_n|) for an escaped sample, max_iter for an interior one.
+__device__ __forceinline__ float smooth_value(uint32_t i, float r2, uint32_t max_iter)
+{
+    if (i >= max_iter) return (float)max_iter;
+    if (!(r2 < 3.0e38f)) return (float)i;
+    float l = __fmul_rn(0.5f, log2f(r2));
+    return __fsub_rn((float)(i + 1u), log2f(l));
+}
+
+// Palette sampled with linear interpolation at t = nu mod len.
+__device__ __forceinline__ void palette_lerp(const uint32_t *pal, uint32_t len, float nu, float ch[4])
+{
+    float fl = (float)len;
+    float t = fmodf(nu, fl);
+    if (t < 0.f) t = __fadd_rn(t, fl);
+    uint32_t i0 = (uint32_t)t;
+    if (i0 >= len) i0 = len - 1u;
+    float f = __fsub_rn(t, (float)i0);
+    uint32_t i1 = i0 + 1u == len ? 0u : i0 + 1u;
+    uint32_t c0 = pal[i0], c1 = pal[i1];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        float a0 = (float)((c0 >> (8 * k)) & 255u), a1 = (float)((c1 >> (8 * k)) & 255u);
+        ch[k] = __fmaf_rn(__fsub_rn(a1, a0), f, a0);
+    }
+}
+
+__device__ __forceinline__ uint32_t pack_mean_rgba(const float acc[4], uint32_t spp)
+{
+    uint32_t out = 0;
+    float n = (float)spp;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        float v = __fadd_rn(__fdiv_rn(acc[k], n), 0.5f);
+        v = v < 255.f ? v : 255.f;
+        out |= ((uint32_t)v & 255u) << (8 * k);
+    }
+    return out;
+}
+
+template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIST_THREADS) k_frame(FrameArgs<R> a)
+{
+    __shared__ uint32_t s_pal[PALETTE_SMEM];
+    const uint32_t *pal = a.palette;
+    if (a.rgba && a.palette_len <= PALETTE_SMEM) {
+        for (uint32_t k = threadIdx.x; k < a.palette_len; k += blockDim.x) s_pal[k] = a.palette[k];
+        pal = s_pal;
+    }
+    __syncthreads();
+
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    uint32_t pix = 0xffffffffu, s = 0, i = 0;
+    R x = R(0), y = R(0), cx = R(0), cy = R(0);
+    bool blk = false, need = true, begin = false;
+    float acc_v = 0.f, acc[4] = {0.f, 0.f, 0.f, 0.f};
+    unsigned long long iters = 0;
+
+    for (;;) {
+        uint32_t need_mask = __ballot_sync(FULL, need);
+        if (need_mask) {
+            uint32_t leader = __ffs(need_mask) - 1u;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(a.counter, (uint32_t)__popc(need_mask));
+            base = __shfl_sync(FULL, base, leader);
+            if (need) {
+                pix = base + (uint32_t)__popc(need_mask & lt_mask);
+                need = false;
+                begin = true;
+                s = 0;
+                acc_v = 0.f;
+                acc[0] = acc[1] = acc[2] = acc[3] = 0.f;
+            }
+        }
+        const bool active = pix < a.n_pix;
+        if (!__any_sync(FULL, active)) break;
+
+        bool done = false;
+        R r2 = R(0);
+        if (active) {
+            if (begin) {
+                begin = false;
+                R px, py;
+                frame_point(a, pix, s, px, py);
+                if (F == FRACTAL_MANDELBROT) {
+                    x = R(0);
+                    y = R(0);
+                    cx = px;
+                    cy = py;
+                } else {
+                    x = px;
+                    y = py;
+                    cx = a.jcx;
+                    cy = a.jcy;
+                }
+                blk = blockable_c(cx, cy);
+                i = 0;
+                r2 = radius2<R, A>(x, y);
+                if (a.max_iter == 0 || !(r2 < R(4))) done = true;
+            }
+            if (!done) {
+                if (blk && a.max_iter - i >= (uint32_t)K) {
+                    R sx = x, sy = y;
+#pragma unroll
+                    for (int k = 0; k < K; k++) step<R, A>(x, y, cx, cy);
+                    r2 = radius2<R, A>(x, y);
+                    if (r2 < R(4)) {
+                        i += (uint32_t)K;
+                        if (i == a.max_iter) done = true;
+                    } else {
+                        // An escape happened inside the block: redo it with a
+                        // test after every step (it ends within K steps).
+                        x = sx;
+                        y = sy;
+                        for (int k = 0; k < K; k++) {
+                            step<R, A>(x, y, cx, cy);
+                            ++i;
+                            r2 = radius2<R, A>(x, y);
+                            if (!(r2 < R(4))) break;
+                        }
+                        done = true;
+                    }
+                } else {
+                    uint32_t rest = a.max_iter - i;
+                    uint32_t lim = rest < (uint32_t)K ? rest : (uint32_t)K;
+                    for (uint32_t k = 0; k < lim; k++) {
+                        step<R, A>(x, y, cx, cy);
+                        ++i;
+                        r2 = radius2<R, A>(x, y);
+                        if (!(r2 < R(4))) {
+                            done = true;
+                            break;
+                        }
+                    }
+                    if (i == a.max_iter) done = true;
+                }
+            }
+        }
+        if (done) {
+            const bool escaped = i < a.max_iter;
+            const float nu = smooth_value(i, (float)r2, a.max_iter);
+            const size_t sidx = (size_t)pix * a.spp + s;
+            if (a.counts) a.counts[sidx] = i;
+            if (a.smooth) a.smooth[sidx] = nu;
+            iters += i;
+            float v = escaped ? nu : (F == FRACTAL_MANDELBROT ? 0.f : (float)a.max_iter);
+            acc_v = __fadd_rn(acc_v, v);
+            if (a.rgba) {
+                float ch[4];
+                if (escaped) {
+                    palette_lerp(pal, a.palette_len, nu, ch);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) ch[k] = (float)((a.interior_rgba >> (8 * k)) & 255u);
+                }
+#pragma unroll
+                for (int k = 0; k < 4; k++) acc[k] = __fadd_rn(acc[k], ch[k]);
+            }
+            ++s;
+            if (s == a.spp) {
+                uint32_t px = pix % a.w, py = pix / a.w;
+                if (a.pixels)
+                    store_pixel(pixel_ptr(a.pixels, a.pixels_pitch, px, py),
+                                make_pixel(__fdiv_rn(acc_v, (float)a.spp), (float)a.spp));
+                if (a.rgba) a.rgba[pix] = pack_mean_rgba(acc, a.spp);
+                need = true;
+            } else {
+                begin = true;
+            }
+        }
+    }
+    if (a.total) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) iters += __shfl_down_sync(FULL, iters, o);
+        if (lane == 0 && iters) atomicAdd(a.total, iters);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Compose, under-sampled preview, debug
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_compose(ComposeArgs a)
+{
+    __shared__ uint32_t s_pal[PALETTE_SMEM];
+    const uint32_t *pal = a.palette;
+    if (!a.visualize && a.palette_len <= PALETTE_SMEM) {
+        for (uint32_t k = threadIdx.x; k < a.palette_len; k += blockDim.x) s_pal[k] = a.palette[k];
+        pal = s_pal;
+    }
+    __syncthreads();
+    const uint32_t wq = (a.w + 3u) / 4u;
+    const size_t n = (size_t)wq * a.h;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        uint32_t y = (uint32_t)(q / wq), x = 4u * (uint32_t)(q % wq);
+        uint32_t c[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (x + k < a.w) c[k] = compose_pixel(load_pixel(pixel_ptr(a.in, a.pitch, x + k, y)), pal, a.palette_len,
+                                                  a.max_ss, a.visualize);
+        uint32_t *row = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(a.out) + (size_t)y * (size_t)a.out_pitch);
+        if (x + 3u < a.w && (reinterpret_cast<uintptr_t>(row + x) & 15u) == 0) {
+            *reinterpret_cast<uint4 *>(row + x) = make_uint4(c[0], c[1], c[2], c[3]);
+        } else {
+            for (int k = 0; k < 4; k++)
+                if (x + k < a.w) row[x + k] = c[k];
+        }
+    }
+}
+
+template <int F>
+__global__ void k_under_sampled(void *out, long pitch, uint32_t w, uint32_t h, Rect<float> r, uint32_t max_iter,
+                                uint32_t level, float jcx, float jcy)
+{
+    const uint32_t ix = (blockDim.x * blockIdx.x + threadIdx.x) * level;
+    const uint32_t iy = (blockDim.y * blockIdx.y + threadIdx.y) * level;
+    if (ix >= w - level || iy >= h - level) return;
+    float pw = __fdiv_rn(__fsub_rn(r.rtx, r.lbx), (float)w);
+    float ph = __fdiv_rn(__fsub_rn(r.rty, r.lby), (float)h);
+    float cx = __fadd_rn(r.lbx, __fmul_rn((float)ix, pw));
+    float cy = __fsub_rn(r.rty, __fmul_rn((float)iy, ph));
+    uint32_t e = compute_fractal<float, ARITH_PARITY, F>(max_iter, cx, cy, jcx, jcy);
+    store_pixel(pixel_ptr(out, pitch, ix, iy), make_pixel((float)e, __fdiv_rn(1.f, (float)level)));
+}
+
+template <int F> __global__ void k_debug()
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) printf("hello from %s\n", F == FRACTAL_MANDELBROT ? "mandelbrot" : "julia");
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+
+template <class KernelPtr> static int occupancy(KernelPtr k, int threads)
+{
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads, 0) != cudaSuccess || n < 1) n = 1;
+    return n;
+}
+
+static unsigned grid_for(unsigned long long work_warps, int occ, int sms)
+{
+    unsigned long long blocks = (work_warps + (PERSIST_THREADS / 32) - 1) / (PERSIST_THREADS / 32);
+    unsigned long long cap = (unsigned long long)occ * (unsigned long long)sms;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    return (unsigned)blocks;
+}
+
+template <class R, int A, int F> static cudaError_t launch_main_t(const MainArgs<R> &a, int sms, cudaStream_t s)
+{
+    static const int occ = occupancy(k_main<R, A, F>, PERSIST_THREADS);
+    k_main<R, A, F><<<grid_for(a.n_tiles, occ, sms), PERSIST_THREADS, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t launch_main(const MainArgs<R> &a, int arith, int fractal, int sms, cudaStream_t s)
+{
+    if (arith == ARITH_PARITY)
+        return fractal == FRACTAL_JULIA ? launch_main_t<R, ARITH_PARITY, FRACTAL_JULIA>(a, sms, s)
+                                        : launch_main_t<R, ARITH_PARITY, FRACTAL_MANDELBROT>(a, sms, s);
+    return fractal == FRACTAL_JULIA ? launch_main_t<R, ARITH_FMA, FRACTAL_JULIA>(a, sms, s)
+                                    : launch_main_t<R, ARITH_FMA, FRACTAL_MANDELBROT>(a, sms, s);
+}
+
+template <class R, int A, int F> static cudaError_t launch_advanced_t(const AdvancedArgs<R> &a, int sms, cudaStream_t s)
+{
+    static const int occ = occupancy(k_advanced<R, A, F>, PERSIST_THREADS);
+    k_advanced<R, A, F><<<grid_for(a.m.n_tiles, occ, sms), PERSIST_THREADS, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t launch_advanced(const AdvancedArgs<R> &a, int arith, int fractal, int sms, cudaStream_t s)
+{
+    if (arith == ARITH_PARITY)
+        return fractal == FRACTAL_JULIA ? launch_advanced_t<R, ARITH_PARITY, FRACTAL_JULIA>(a, sms, s)
+                                        : launch_advanced_t<R, ARITH_PARITY, FRACTAL_MANDELBROT>(a, sms, s);
+    return fractal == FRACTAL_JULIA ? launch_advanced_t<R, ARITH_FMA, FRACTAL_JULIA>(a, sms, s)
+                                    : launch_advanced_t<R, ARITH_FMA, FRACTAL_MANDELBROT>(a, sms, s);
+}
+
+template <class R, int A, int F> static cudaError_t launch_frame_t(const FrameArgs<R> &a, int sms, cudaStream_t s)
+{
+    static const int occ = occupancy(k_frame<R, A, F, ESCAPE_BLOCK>, PERSIST_THREADS);
+    unsigned long long warps = ((unsigned long long)a.n_pix + 31ull) / 32ull;
+    k_frame<R, A, F, ESCAPE_BLOCK><<<grid_for(warps, occ, sms), PERSIST_THREADS, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t launch_frame(const FrameArgs<R> &a, int arith, int fractal, int sms, cudaStream_t s)
+{
+    if (arith == ARITH_PARITY)
+        return fractal == FRACTAL_JULIA ? launch_frame_t<R, ARITH_PARITY, FRACTAL_JULIA>(a, sms, s)
+                                        : launch_frame_t<R, ARITH_PARITY, FRACTAL_MANDELBROT>(a, sms, s);
+    return fractal == FRACTAL_JULIA ? launch_frame_t<R, ARITH_FMA, FRACTAL_JULIA>(a, sms, s)
+                                    : launch_frame_t<R, ARITH_FMA, FRACTAL_MANDELBROT>(a, sms, s);
+}
+
+cudaError_t launch_compose(const ComposeArgs &a, cudaStream_t s)
+{
+    unsigned long long quads = (unsigned long long)((a.w + 3u) / 4u) * a.h;
+    unsigned long long blocks = (quads + 255ull) / 256ull;
+    if (blocks > 152ull * 16ull) blocks = 152ull * 16ull;
+    if (blocks < 1) blocks = 1;
+    k_compose<<<(unsigned)blocks, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_under_sampled(void *out, long pitch, uint32_t w, uint32_t h, Rect<float> rect, uint32_t max_iter,
+                                 uint32_t level, int fractal, double jcx, double jcy, cudaStream_t s)
+{
+    dim3 block(32, 32);
+    dim3 grid((w + 31u) / 32u, (h + 31u) / 32u);
+    if (fractal == FRACTAL_JULIA)
+        k_under_sampled<FRACTAL_JULIA><<<grid, block, 0, s>>>(out, pitch, w, h, rect, max_iter, level, (float)jcx,
+                                                              (float)jcy);
+    else
+        k_under_sampled<FRACTAL_MANDELBROT><<<grid, block, 0, s>>>(out, pitch, w, h, rect, max_iter, level, 0.f, 0.f);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_debug(int fractal, cudaStream_t s)
+{
+    if (fractal == FRACTAL_JULIA)
+        k_debug<FRACTAL_JULIA><<<1, 1, 0, s>>>();
+    else
+        k_debug<FRACTAL_MANDELBROT><<<1, 1, 0, s>>>();
+    return cudaGetLastError();
+}
+
+template <class R> __global__ void __launch_bounds__(256) k_fma_peak(uint32_t iters, double *sink)
+{
+    R a[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) a[k] = R(threadIdx.x + k) * R(1e-3);
+    const R m = R(0.999999), c = R(1e-7);
+    for (uint32_t i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) a[k] = Op<R>::fma(a[k], m, c);
+    }
+    R t = R(0);
+#pragma unroll
+    for (int k = 0; k < 8; k++) t += a[k];
+    if (t == R(-1)) sink[0] = (double)t;  // never true; keeps the chains live
+}
+
+cudaError_t launch_fma_peak(bool dbl, int blocks, uint32_t iters, double *sink, cudaStream_t s)
+{
+    if (dbl)
+        k_fma_peak<double><<<blocks, 256, 0, s>>>(iters, sink);
+    else
+        k_fma_peak<float><<<blocks, 256, 0, s>>>(iters, sink);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_main<float>(const MainArgs<float> &, int, int, int, cudaStream_t);
+template cudaError_t launch_main<double>(const MainArgs<double> &, int, int, int, cudaStream_t);
+template cudaError_t launch_advanced<float>(const AdvancedArgs<float> &, int, int, int, cudaStream_t);
+template cudaError_t launch_advanced<double>(const AdvancedArgs<double> &, int, int, int, cudaStream_t);
+template cudaError_t launch_frame<float>(const FrameArgs<float> &, int, int, int, cudaStream_t);
+template cudaError_t launch_frame<double>(const FrameArgs<double> &, int, int, int, cudaStream_t);
+
+}  // namespace chaos

@@ -1,0 +1,274 @@
+/*
+ * chaos_gb300.h -- C ABI of libchaos_gb300.so, the GB300 (sm_103a) escape-time
+ * renderer that stands in for chaos-ultra's fractal-kernel path.
+ *
+ * Two ways in:
+ *   1. The drop-in CUDA module files cudaKernels/<fractal>.ptx (cubin images;
+ *      cuModuleLoad reads cubin as well as PTX).  They export the seven kernels
+ *      the Java host resolves by name, with the reference's parameter layout and
+ *      __constant__ symbols, so FractalRenderingModule loads them unchanged.
+ *   2. This library: plain C functions (pointers, sizes, a cudaStream_t passed as
+ *      void*), int status returns, no exceptions and no device traps.  A JNI or
+ *      Panama shim binds them.
+ *
+ * Reference paths are relative to the chaos-ultra root; J/ stands for
+ * src/main/java/cz/cuni/mff/cgg/teichmaa/chaosultra/ and gen.cu for
+ * src/main/cuda/fractalRendererGeneric.cu.
+ *
+ * Threading: calls on one chaos_module / chaos_renderer are not thread-safe
+ * (the reference makes every CUDA call from one thread, J/cudarenderer/
+ * CudaHelpers.java:47-49).  Kernels are enqueued on the stream passed in
+ * (NULL = the legacy default stream); functions without "_async" in their name
+ * synchronise that stream before returning, as the reference does after every
+ * launch (J/cudarenderer/CudaFractalRenderer.java:255-261).
+ */
+#ifndef CHAOS_GB300_H
+#define CHAOS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define CHAOS_OK 0
+#define CHAOS_ERR_INVALID_ARGUMENT 1 /* bad size, pointer, NaN/inf plane bound, ... */
+#define CHAOS_ERR_CUDA 2             /* a CUDA runtime call failed; see chaos_last_error() */
+#define CHAOS_ERR_UNKNOWN_FRACTAL 3  /* CudaFractalRendererProvider.getRenderer: "Unknown fractal" */
+#define CHAOS_ERR_NOT_FOUND 4        /* unknown constant name (cuModuleGetGlobal NOT_FOUND) */
+#define CHAOS_ERR_STATE 5            /* renderer not initialised / already initialised */
+#define CHAOS_ERR_OUT_OF_MEMORY 6    /* allocation or HBM budget refused */
+#define CHAOS_ERR_TIMEOUT 7          /* a bounded device wait gave up */
+#define CHAOS_ERR_UNSUPPORTED 8      /* valid request this build does not implement */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *chaos_last_error(void);
+/* Library version string. */
+const char *chaos_version(void);
+
+/* ---- shared types ------------------------------------------------------- */
+
+/* pixel_info_t, src/main/cuda/helpers.cuh:106-130: 16 bytes, 4-byte aligned. */
+typedef struct chaos_pixel_info {
+    float value;                 /* averaged escape value */
+    float weight;                /* number of samples (may decay under reuse) */
+    uint8_t is_reused;           /* set when sample reuse produced the value */
+    uint8_t pad_[3];
+    float weight_of_new_samples; /* freshly computed weight when is_reused */
+} chaos_pixel_info;
+
+/* Kernel flag bits, gen.cu:157-161 / J/cudarenderer/KernelMain.java:12-13,
+ * KernelAdvanced.java:17-20 (bit 1, "visualise sample count", is host-side). */
+#define CHAOS_FLAG_ADAPTIVE_SS (1u << 0)
+#define CHAOS_FLAG_VISUALIZE_SAMPLE_COUNT (1u << 1)
+#define CHAOS_FLAG_FOVEATION (1u << 2)
+#define CHAOS_FLAG_SAMPLE_REUSE (1u << 3)
+#define CHAOS_FLAG_IS_ZOOMING (1u << 4)
+#define CHAOS_FLAG_ZOOMING_IN (1u << 5)
+
+/* Arithmetic of the escape loop.
+ * CHAOS_ARITH_PARITY rounds every product and sum (the reference kernel built
+ * with nvcc --fmad=false): escape counts are bit-identical to it.
+ * CHAOS_ARITH_FMA uses fused multiply-adds, 4 FP ops per iteration; counts are
+ * bit-identical to the oracle's fma restatement and differ from PARITY only
+ * where rounding decides an escape. */
+#define CHAOS_ARITH_FMA 0
+#define CHAOS_ARITH_PARITY 1
+
+/* ---- module level: FractalRenderingModule + its seven kernels ----------- */
+
+typedef struct chaos_module chaos_module;
+
+/* Open the module of a registered fractal ("mandelbrot", "julia").
+ * Replaces FractalRenderingModule.initialize (J/cudarenderer/
+ * FractalRenderingModule.java:73-100) + CudaFractalRendererProvider.getRenderer
+ * (J/cudarenderer/CudaFractalRendererProvider.java:47-66). */
+int chaos_module_open(const char *fractal_name, chaos_module **out);
+int chaos_module_close(chaos_module *m);
+/* Registered fractal names, comma separated (getAvailableFractals, :37-39). */
+const char *chaos_available_fractals(void);
+/* Fractal name of an open module (getFractalName). */
+const char *chaos_module_fractal_name(const chaos_module *m);
+
+/* Write a module constant by name, size must equal the symbol's size
+ * ("VISUALIZE_SAMPLE_COUNT": 1 byte, gen.cu:14; "julia_c": 2 doubles,
+ * julia.cu:3).  Replaces writeToConstantMemory (FractalRenderingModule.java:163-227). */
+int chaos_module_write_constant(chaos_module *m, const char *name, const void *src, size_t size);
+/* Fractal custom parameters as the GUI sends them, e.g. "-0.4;0.6" for Julia
+ * (ModuleJulia.setFractalCustomParameters, J/cudarenderer/modules/ModuleJulia.java:28-37). */
+int chaos_module_set_custom_params(chaos_module *m, const char *text);
+/* Default view of the module (supplyDefaultValues, ModuleMandelbrot.java:20-25,
+ * ModuleJulia.java:40-49): centre, zoom (plane height), maxIterations, maxSS. */
+int chaos_module_default_view(const chaos_module *m, double *center_x, double *center_y, double *zoom,
+                              uint32_t *max_iterations, float *max_super_sampling);
+
+/* fractalRenderMainFloat / fractalRenderMainDouble, gen.cu:384-405.
+ * out: pitched width x height array of chaos_pixel_info (device memory, pitch
+ * in bytes, >= 16*width).  rect = {left_bottom.x, left_bottom.y, right_top.x,
+ * right_top.y}.  max_super_sampling in [1, 64].  Persistent warps take 8x4
+ * pixel tiles from a work counter (each warp one tile at a time, the vote
+ * group of the reference's adaptive super-sampling). */
+int chaos_render_main_f32(chaos_module *m, chaos_pixel_info *out, long pitch, uint32_t width, uint32_t height,
+                          const float rect[4], uint32_t max_iterations, float max_super_sampling, uint32_t flags,
+                          int arith, void *stream);
+int chaos_render_main_f64(chaos_module *m, chaos_pixel_info *out, long pitch, uint32_t width, uint32_t height,
+                          const double rect[4], uint32_t max_iterations, float max_super_sampling, uint32_t flags,
+                          int arith, void *stream);
+
+/* fractalRenderAdvancedFloat / fractalRenderAdvancedDouble, gen.cu:423-448:
+ * foveation + sample reuse from `in` (the previous frame, plane rect_reused).
+ * in and out must not overlap. */
+int chaos_render_advanced_f32(chaos_module *m, chaos_pixel_info *out, long pitch, uint32_t width, uint32_t height,
+                              const float rect[4], uint32_t max_iterations, float max_super_sampling, uint32_t flags,
+                              const float rect_reused[4], const chaos_pixel_info *in, long in_pitch, uint32_t focus_x,
+                              uint32_t focus_y, int arith, void *stream);
+int chaos_render_advanced_f64(chaos_module *m, chaos_pixel_info *out, long pitch, uint32_t width, uint32_t height,
+                              const double rect[4], uint32_t max_iterations, float max_super_sampling, uint32_t flags,
+                              const double rect_reused[4], const chaos_pixel_info *in, long in_pitch,
+                              uint32_t focus_x, uint32_t focus_y, int arith, void *stream);
+
+/* compose, gen.cu:455-475, with a headless output: out_rgba is a pitched
+ * width x height array of RGBA8 words (R in the low byte), the palette a device
+ * array of palette_len words (the one-row palette surface of the reference).
+ * The module's VISUALIZE_SAMPLE_COUNT constant selects the sample-count ramp. */
+int chaos_compose(chaos_module *m, const chaos_pixel_info *in, long pitch, uint32_t *out_rgba, long out_pitch,
+                  uint32_t width, uint32_t height, const uint32_t *palette, uint32_t palette_len,
+                  float max_super_sampling, void *stream);
+
+/* fractalRenderUnderSampled, gen.cu:478-503 (float plane, every level-th pixel). */
+int chaos_render_under_sampled(chaos_module *m, chaos_pixel_info *out, long pitch, uint32_t width, uint32_t height,
+                               const float rect[4], uint32_t max_iterations, uint32_t level, void *stream);
+
+/* debug, gen.cu:505-512: prints the fractal's greeting from the device. */
+int chaos_debug(chaos_module *m);
+
+/* ---- precision selection (RenderingKernel.isSegmentBoundsAt*Limit) ----- */
+
+#define CHAOS_PRECISION_SINGLE 0
+#define CHAOS_PRECISION_DOUBLE 1
+#define CHAOS_PRECISION_TOO_BIG 2
+/* J/cudarenderer/RenderingKernel.java:124-138 + CudaFractalRenderer.updateFloatPrecision
+ * (:409-419): single while the pixel is at least ulp((float)left_bottom) on both
+ * axes, double below that, "too big" below ulp((double)left_bottom). */
+int chaos_select_precision(const double rect[4], uint32_t width, uint32_t height);
+
+/* ---- renderer level: CudaFractalRenderer (renderQuality / renderFast) --- */
+
+/* RenderingModel fields the renderer reads (J/rendering/model/*.java). */
+typedef struct chaos_rendering_model {
+    double left_bottom_x, left_bottom_y, right_top_x, right_top_y; /* PlaneSegment */
+    uint32_t max_iterations;
+    float max_super_sampling;
+    uint8_t use_adaptive_super_sampling;
+    uint8_t visualise_sample_count;
+    uint8_t use_foveated_rendering;
+    uint8_t use_sample_reuse;
+    uint8_t zooming;
+    uint8_t zooming_in;
+    uint8_t sample_reuse_cache_dirty;
+    uint8_t pad_;
+    int32_t mouse_focus_x, mouse_focus_y;
+    int32_t arith; /* CHAOS_ARITH_* for this frame */
+    int32_t floating_point_precision; /* out: CHAOS_PRECISION_* chosen for the frame */
+} chaos_rendering_model;
+
+typedef struct chaos_renderer chaos_renderer;
+
+/* new CudaFractalRenderer(module) (J/cudarenderer/CudaFractalRenderer.java:65-77). */
+int chaos_renderer_create(chaos_module *m, chaos_renderer **out);
+/* initializeRendering(GLParams) with a headless output: allocates the two
+ * pitched sample-reuse buffers (DeviceMemoryDoubleBuffer2D.reallocate,
+ * J/cudarenderer/DeviceMemoryDoubleBuffer2D.java:37-41) and a width x height
+ * RGBA8 output, and copies the palette (host array) to the device. */
+int chaos_renderer_initialize(chaos_renderer *r, uint32_t width, uint32_t height, const uint32_t *palette,
+                              uint32_t palette_len);
+int chaos_renderer_free_resources(chaos_renderer *r);
+/* renderQuality (CudaFractalRenderer.java:187-206): main kernel + compose. */
+int chaos_renderer_render_quality(chaos_renderer *r, chaos_rendering_model *model);
+/* renderFast (CudaFractalRenderer.java:159-184): advanced kernel reusing the
+ * previous frame, buffer swap, compose; falls back to renderQuality when the
+ * reuse cache is dirty. */
+int chaos_renderer_render_fast(chaos_renderer *r, chaos_rendering_model *model);
+/* Device pointers of the current output (RGBA8, pitch in bytes) and of the
+ * primary reuse buffer. */
+int chaos_renderer_output(const chaos_renderer *r, const uint32_t **rgba, long *rgba_pitch,
+                          const chaos_pixel_info **primary, long *primary_pitch);
+/* Copy the RGBA8 output to host memory (width*height words, row-major). */
+int chaos_renderer_read_output(const chaos_renderer *r, uint32_t *host_rgba);
+int chaos_renderer_destroy(chaos_renderer *r);
+
+/* ---- frame level: per-sample escape counts, jittered supersampling ------ */
+
+#define CHAOS_SAMPLES_CENTER 0 /* one sample at each pixel centre */
+#define CHAOS_SAMPLES_JITTER 1 /* samples_per_pixel seeded uniform offsets */
+
+#define CHAOS_TIER_F32 0  /* escape loop in binary32 */
+#define CHAOS_TIER_F64 1  /* escape loop in binary64 */
+
+/* One frame of the plain escape-time renderer.  Sample s of pixel (px, py)
+ * sits at plane point
+ *   c = (center_x + ((px + ox) - width/2) * pixel_size,
+ *        center_y - ((py + oy) - height/2) * pixel_size)
+ * with (ox, oy) = (0.5, 0.5) for CHAOS_SAMPLES_CENTER and a counter-based hash
+ * of (seed, pixel, sample) in [0,1)^2 for CHAOS_SAMPLES_JITTER. */
+typedef struct chaos_frame_desc {
+    uint32_t width, height;
+    uint32_t max_iterations;
+    uint32_t samples_per_pixel; /* 1..64 */
+    uint32_t sample_mode;       /* CHAOS_SAMPLES_* */
+    uint32_t tier;              /* CHAOS_TIER_* */
+    int32_t arith;              /* CHAOS_ARITH_* */
+    uint32_t fractal;           /* 0 mandelbrot, 1 julia */
+    uint64_t seed;
+    double center_x, center_y;
+    double pixel_size;
+    double julia_cx, julia_cy;
+} chaos_frame_desc;
+
+/* Outputs (device pointers, each optional):
+ *   counts  [height][width][spp] uint32 iterations taken (max_iterations = interior)
+ *   smooth  [height][width][spp] float  n + 1 - log2(log2|z_n|), interior = max_iterations
+ *   pixels  pitched chaos_pixel_info: value = mean over samples of (smooth, 0 for interior), weight = spp
+ *   rgba    [height][width] RGBA8: mean of the sample colours, palette[] sampled with linear
+ *           interpolation at smooth mod palette_len, interior samples = interior_rgba
+ *   total_iterations: one uint64 the kernel adds the frame's pixel-iterations to. */
+typedef struct chaos_frame_out {
+    uint32_t *counts;
+    float *smooth;
+    chaos_pixel_info *pixels;
+    long pixels_pitch;
+    uint32_t *rgba;
+    const uint32_t *palette;
+    uint32_t palette_len;
+    uint32_t interior_rgba;
+    unsigned long long *total_iterations;
+} chaos_frame_out;
+
+/* Enqueue one frame (does not synchronise). */
+int chaos_render_frame_async(const chaos_frame_desc *desc, const chaos_frame_out *out, void *stream);
+/* Same, then synchronise the stream. */
+int chaos_render_frame(const chaos_frame_desc *desc, const chaos_frame_out *out, void *stream);
+
+/* A whole frame through host memory, for callers that hold no device buffers:
+ * copies the palette (host array) to the device, renders the RGBA8 image, and
+ * copies the image (width*height words, row-major) and the frame's
+ * pixel-iteration count back to host memory.  Device buffers are kept per
+ * calling thread and grown as needed; the stream is synchronised before return. */
+int chaos_render_frame_host(const chaos_frame_desc *desc, const uint32_t *palette, uint32_t palette_len,
+                            uint32_t interior_rgba, uint32_t *rgba_host, unsigned long long *total_host,
+                            void *stream);
+
+/* ---- diagnostics -------------------------------------------------------- */
+
+/* Measured fused-multiply-add throughput of the current device in FLOP/s
+ * (an FMA counts 2), binary32 (tier CHAOS_TIER_F32) or binary64
+ * (CHAOS_TIER_F64): every thread of a full-occupancy grid runs 8 independent
+ * FMA chains.  The roofline denominator of the escape-time kernels. */
+int chaos_measure_fma_peak(uint32_t tier, double *flops_per_second);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CHAOS_GB300_H */

@@ -1,0 +1,106 @@
+/*
+ * ref_host.cpp -- host build of the reference's own per-pixel fractal code.
+ *
+ * TEST INFRASTRUCTURE ONLY.  oracle/build_ref.sh compiles this file with
+ * -I <reference>/src/main/cuda, so the #includes below pull in the reference's
+ * unmodified src/main/cuda/fractals/mandelbrot.cu and julia.cu (each inside its
+ * own namespace, because both define computeFractal/colorize).  The exported
+ * C functions are what the tests use to pin the CPU restatement
+ * (oracle/chaos_oracle.c) and what bench.py's reference arm times.
+ */
+#include "ref_prelude.h"
+
+#include <omp.h>
+
+namespace ref_mandelbrot {
+#include "fractals/mandelbrot.cu"
+}
+/* helpers.cuh is guarded by HELPERS; clear the guard so the second
+ * namespace gets its own copy of Point/Rectangle. */
+#undef HELPERS
+namespace ref_julia {
+#include "fractals/julia.cu"
+}
+
+extern "C" {
+
+float ref_mandelbrot_f(unsigned max_iter, float cx, float cy)
+{
+    return ref_mandelbrot::computeFractal<float>(max_iter, ref_mandelbrot::Point<float>(cx, cy));
+}
+
+float ref_mandelbrot_d(unsigned max_iter, double cx, double cy)
+{
+    return ref_mandelbrot::computeFractal<double>(max_iter, ref_mandelbrot::Point<double>(cx, cy));
+}
+
+/* julia.cu reads the __constant__ double julia_c[2] that the Java host writes. */
+void ref_julia_set_c(double cx, double cy)
+{
+    ref_julia::julia_c[0] = cx;
+    ref_julia::julia_c[1] = cy;
+}
+
+float ref_julia_f(unsigned max_iter, float zx, float zy)
+{
+    return ref_julia::computeFractal<float>(max_iter, ref_julia::Point<float>(zx, zy));
+}
+
+float ref_julia_d(unsigned max_iter, double zx, double zy)
+{
+    return ref_julia::computeFractal<double>(max_iter, ref_julia::Point<double>(zx, zy));
+}
+
+unsigned ref_mandelbrot_colorize(const unsigned *palette, unsigned len, float value)
+{
+    return ref_mandelbrot::colorize((cudaSurfaceObject_t)(uintptr_t)palette, len, value);
+}
+
+/* Escape counts of a w x h grid of points c = (x0 + px*dx, y0 - py*dy) through
+ * the reference's computeFractal<Real>, one OpenMP thread per row
+ * (schedule(dynamic)), threads = n_threads (0: the OpenMP default).  The count
+ * of a pixel is what computeFractal returns, except that Mandelbrot's interior
+ * value 0 is counted as max_iter (the pixel-iteration metric).  Returns the sum
+ * of the counts; counts may be NULL. */
+unsigned long long ref_mandelbrot_grid(int dbl, unsigned w, unsigned h, double x0, double y0, double dx, double dy,
+                                       unsigned max_iter, int n_threads, unsigned *counts)
+{
+    unsigned long long total = 0;
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic) reduction(+ : total)
+    for (long y = 0; y < (long)h; y++) {
+        for (unsigned x = 0; x < w; x++) {
+            unsigned e;
+            if (dbl) {
+                double cx = x0 + (double)x * dx, cy = y0 - (double)y * dy;
+                e = (unsigned)ref_mandelbrot_d(max_iter, cx, cy);
+            } else {
+                float cx = (float)x0 + (float)x * (float)dx, cy = (float)y0 - (float)y * (float)dy;
+                e = (unsigned)ref_mandelbrot_f(max_iter, cx, cy);
+            }
+            if (e == 0) e = max_iter;
+            if (counts) counts[(size_t)y * w + x] = e;
+            total += e;
+        }
+    }
+    return total;
+}
+
+/* Same for an explicit list of sample points (x[k], y[k]) in double. */
+unsigned long long ref_mandelbrot_points_d(size_t n, const double *x, const double *y, unsigned max_iter,
+                                           int n_threads, unsigned *counts)
+{
+    unsigned long long total = 0;
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : total)
+    for (long k = 0; k < (long)n; k++) {
+        unsigned e = (unsigned)ref_mandelbrot_d(max_iter, x[k], y[k]);
+        if (e == 0) e = max_iter;
+        if (counts) counts[k] = e;
+        total += e;
+    }
+    return total;
+}
+
+int ref_max_threads(void) { return omp_get_max_threads(); }
+}

@@ -1,0 +1,202 @@
+"""The drop-in CUDA module files, loaded the way the Java host loads them.
+
+tests/gpu_util.Driver replays JCuda's calls: cuModuleLoad of
+<cudaKernelsDir>/<fractal>.ptx, cuModuleGetFunction for the seven kernels,
+cuModuleGetGlobal + memcpy for the __constant__ symbols, cuLaunchKernel with a
+void** parameter array and the 32x32 block shape.  Results are compared with
+the oracle; where the reference's own kernels were built for sm_103a
+(oracle/_ref/ref_<fractal>[_nofma].cubin) they are run the same way, which pins
+the oracle's lock-step restatement to the reference itself."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+from oracle.oracle import JULIA, MANDELBROT  # noqa: E402
+from tests.gpu_util import (MODULE_KERNELS, Driver, advanced_params, java_grid, main_params, pitched,  # noqa: E402
+                            read_pixels, same_pixels, upload_pixels)
+from tests.test_gpu_reference_mode import M1, rect_for, zoom_at  # noqa: E402
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF_DIR = os.path.join(ROOT, "oracle", "_ref")
+
+# Parameter offsets and sizes (CUDA parameter ABI) of the reference's entry
+# points, from the Java marshalling (RenderingKernel/KernelMain/KernelAdvanced/
+# KernelCompose): (offset, size) per parameter.
+LAYOUT = {
+    "fractalRenderMainFloat": [(0, 8), (8, 8), (16, 8), (24, 16), (40, 4), (44, 4), (48, 4)],
+    "fractalRenderMainDouble": [(0, 8), (8, 8), (16, 8), (24, 32), (56, 4), (60, 4), (64, 4)],
+    "fractalRenderAdvancedFloat": [(0, 8), (8, 8), (16, 8), (24, 16), (40, 4), (44, 4), (48, 4), (52, 16), (72, 8),
+                                   (80, 8), (88, 8)],
+    "fractalRenderAdvancedDouble": [(0, 8), (8, 8), (16, 8), (24, 32), (56, 4), (60, 4), (64, 4), (72, 32), (104, 8),
+                                    (112, 8), (120, 8)],
+    "compose": [(0, 8), (8, 8), (16, 8), (24, 8), (32, 8), (40, 4), (44, 4), (48, 8), (56, 4), (60, 4)],
+    "fractalRenderUnderSampled": [(0, 8), (8, 8), (16, 4), (20, 4), (24, 4), (28, 4), (32, 4), (36, 4), (40, 4),
+                                  (44, 4)],
+}
+
+
+@pytest.fixture(scope="module")
+def drv(cuda, native):
+    return Driver()
+
+
+def module_path(fractal, parity):
+    import chaos_gb300 as cg
+    return os.path.join(cg.DROPIN_PARITY_DIR if parity else cg.DROPIN_DIR, fractal + ".ptx")
+
+
+def param_layout(drv, fn, n):
+    import ctypes as C
+    out = []
+    for i in range(n):
+        off, size = C.c_size_t(), C.c_size_t()
+        rc = drv.cu.cuFuncGetParamInfo(fn, C.c_size_t(i), C.byref(off), C.byref(size))
+        assert rc == 0, (i, rc)
+        out.append((off.value, size.value))
+    return out
+
+
+@pytest.mark.parametrize("fractal", ["mandelbrot", "julia"])
+@pytest.mark.parametrize("parity", [False, True])
+def test_module_exports_reference_interface(drv, fractal, parity):
+    mod = drv.load(module_path(fractal, parity))
+    try:
+        fns = {k: drv.function(mod, k) for k in MODULE_KERNELS}
+        for name, layout in LAYOUT.items():
+            assert param_layout(drv, fns[name], len(layout)) == layout, name
+        assert drv.global_(mod, "VISUALIZE_SAMPLE_COUNT")[1] == 1
+        if fractal == "julia":
+            assert drv.global_(mod, "julia_c")[1] == 16
+    finally:
+        drv.unload(mod)
+
+
+def replay_main(drv, cuda, path, w, h, rect, max_iter, max_ss, flags, dbl, julia_c=None):
+    mod = drv.load(path)
+    try:
+        if julia_c is not None:
+            drv.write_constant(mod, "julia_c", np.array(julia_c, dtype=np.float64).tobytes())
+        drv.write_constant(mod, "VISUALIZE_SAMPLE_COUNT", b"\0")
+        fn = drv.function(mod, "fractalRenderMainDouble" if dbl else "fractalRenderMainFloat")
+        buf, pitch = pitched(cuda, w, h)
+        grid, block = java_grid(w, h)
+        drv.launch(fn, grid, block, main_params(buf.data_ptr(), pitch, w, h, rect, max_iter, max_ss, flags, dbl))
+        return read_pixels(buf, w)
+    finally:
+        drv.unload(mod)
+
+
+def replay_advanced(drv, cuda, path, w, h, rect, max_iter, max_ss, flags, old, prev, focus, dbl):
+    mod = drv.load(path)
+    try:
+        fn = drv.function(mod, "fractalRenderAdvancedDouble" if dbl else "fractalRenderAdvancedFloat")
+        inbuf, in_pitch = upload_pixels(cuda, prev)
+        buf, pitch = pitched(cuda, w, h)
+        grid, block = java_grid(w, h)
+        drv.launch(fn, grid, block, advanced_params(buf.data_ptr(), pitch, w, h, rect, max_iter, max_ss, flags, old,
+                                                    inbuf.data_ptr(), in_pitch, focus, dbl))
+        return read_pixels(buf, w)
+    finally:
+        drv.unload(mod)
+
+
+MAIN_CASES = [(96, 64, 1.0, 1), (100, 37, 4.6, 1), (70, 45, 3.0, 0), (65, 66, 9.0, 1)]
+
+
+@pytest.mark.parametrize("w,h,max_ss,flags", MAIN_CASES)
+@pytest.mark.parametrize("dbl", [False, True])
+@pytest.mark.parametrize("parity", [True, False])
+def test_dropin_main_matches_oracle(drv, cuda, oracle, w, h, max_ss, flags, dbl, parity):
+    import chaos_gb300 as cg
+    rect = rect_for(M1[:2], M1[2], w, h)
+    got = replay_main(drv, cuda, module_path("mandelbrot", parity), w, h, rect, 600, max_ss, flags, dbl)
+    arith = cg.ARITH_PARITY if parity else cg.ARITH_FMA
+    want = oracle.render_main(MANDELBROT, dbl, arith, w, h, rect, 600, max_ss, flags)
+    assert not same_pixels(got, want).any()
+
+
+def test_dropin_julia_constant(drv, cuda, oracle):
+    import chaos_gb300 as cg
+    w, h = 90, 60
+    rect = rect_for((0.0, 0.0), 2.0, w, h)
+    got = replay_main(drv, cuda, module_path("julia", True), w, h, rect, 900, 2.0, 1, False, julia_c=(0.285, 0.01))
+    want = oracle.render_main(JULIA, False, cg.ARITH_PARITY, w, h, rect, 900, 2.0, 1, julia_c=(0.285, 0.01))
+    assert not same_pixels(got, want).any()
+
+
+@pytest.mark.parametrize("dbl", [False, True])
+def test_dropin_advanced_matches_oracle(drv, cuda, oracle, dbl):
+    import chaos_gb300 as cg
+    w, h, focus = 128, 80, (40, 50)
+    old = rect_for(M1[:2], M1[2], w, h)
+    new = zoom_at(old, focus, w, h)
+    prev = oracle.render_main(MANDELBROT, dbl, cg.ARITH_PARITY, w, h, old, 600, 3.0, 1)
+    got = replay_advanced(drv, cuda, module_path("mandelbrot", True), w, h, new, 600, 3.0, 8 | 16 | 32 | 1, old, prev,
+                          focus, dbl)
+    want = oracle.render_advanced(MANDELBROT, dbl, cg.ARITH_PARITY, w, h, new, 600, 3.0, 8 | 16 | 32 | 1, old, prev,
+                                  focus)
+    assert not same_pixels(got, want).any()
+
+
+def ref_cubin(fractal, nofma=True):
+    p = os.path.join(REF_DIR, f"ref_{fractal}{'_nofma' if nofma else ''}.cubin")
+    if not os.path.exists(p):
+        pytest.skip(f"reference cubin not built ({p})")
+    return p
+
+
+def test_reference_cubin_interface_matches(drv):
+    """The reference's own module has the parameter layout the drop-in copies."""
+    mod = drv.load(ref_cubin("mandelbrot"))
+    try:
+        fns = {k: drv.function(mod, k) for k in MODULE_KERNELS}
+        for name, layout in LAYOUT.items():
+            assert param_layout(drv, fns[name], len(layout)) == layout, name
+    finally:
+        drv.unload(mod)
+
+
+@pytest.mark.parametrize("w,h,max_ss,flags", MAIN_CASES + [(48, 40, 12.0, 1), (33, 29, 17.0, 1)])
+@pytest.mark.parametrize("dbl", [False, True])
+def test_reference_kernel_pins_oracle_main(drv, cuda, oracle, w, h, max_ss, flags, dbl):
+    """The reference's fractalRenderMain (built --fmad=false) = the oracle = our parity module."""
+    import chaos_gb300 as cg
+    rect = rect_for(M1[:2], M1[2], w, h)
+    ref = replay_main(drv, cuda, ref_cubin("mandelbrot"), w, h, rect, 600, max_ss, flags, dbl)
+    want = oracle.render_main(MANDELBROT, dbl, cg.ARITH_PARITY, w, h, rect, 600, max_ss, flags)
+    bad = same_pixels(ref, want)
+    assert not bad.any(), (int(bad.sum()), ref[bad][:3], want[bad][:3])
+    ours = replay_main(drv, cuda, module_path("mandelbrot", True), w, h, rect, 600, max_ss, flags, dbl)
+    assert not same_pixels(ours, ref).any()
+
+
+@pytest.mark.parametrize("flags", [8 | 16 | 32 | 1, 8 | 1, 4 | 8 | 16 | 32 | 1])
+@pytest.mark.parametrize("dbl", [False, True])
+def test_reference_kernel_pins_oracle_advanced(drv, cuda, oracle, flags, dbl):
+    import chaos_gb300 as cg
+    w, h, focus = 128, 80, (40, 50)
+    old = rect_for(M1[:2], M1[2], w, h)
+    new = zoom_at(old, focus, w, h)
+    prev = oracle.render_main(MANDELBROT, dbl, cg.ARITH_PARITY, w, h, old, 600, 3.0, 1)
+    ref = replay_advanced(drv, cuda, ref_cubin("mandelbrot"), w, h, new, 600, 3.0, flags, old, prev, focus, dbl)
+    ours = replay_advanced(drv, cuda, module_path("mandelbrot", True), w, h, new, 600, 3.0, flags, old, prev, focus,
+                           dbl)
+    assert not same_pixels(ours, ref).any()  # same CUDA atanf on both sides: exact even with foveation
+    want = oracle.render_advanced(MANDELBROT, dbl, cg.ARITH_PARITY, w, h, new, 600, 3.0, flags, old, prev, focus)
+    bad = same_pixels(ref, want)
+    if flags & 4:
+        assert bad.mean() < 0.02
+    else:
+        assert not bad.any(), (int(bad.sum()), ref[bad][:3], want[bad][:3])
+
+
+def test_reference_julia_pins_oracle(drv, cuda, oracle):
+    import chaos_gb300 as cg
+    w, h = 90, 60
+    rect = rect_for((0.0, 0.0), 2.0, w, h)
+    ref = replay_main(drv, cuda, ref_cubin("julia"), w, h, rect, 900, 4.0, 1, True, julia_c=(-0.4, 0.6))
+    want = oracle.render_main(JULIA, True, cg.ARITH_PARITY, w, h, rect, 900, 4.0, 1, julia_c=(-0.4, 0.6))
+    assert not same_pixels(ref, want).any()

@@ -1,0 +1,92 @@
+"""The oracle against the reference's own outputs (committed golden vectors).
+
+tests/golden/reference_golden.json was produced by the reference's
+src/main/cuda/fractals/{mandelbrot,julia}.cu host-built by oracle/build_ref.sh
+(tests/golden/make_golden.py).  These tests run on any CPU."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle.oracle import ARITH_PARITY, JULIA, MANDELBROT
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "reference_golden.json")
+
+
+@pytest.fixture(scope="module")
+def golden():
+    with open(GOLDEN) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("dbl,tag", [(0, "f32"), (1, "f64")])
+def test_c1_known_answer(oracle, golden, dbl, tag):
+    c1 = golden["c1"]
+    total, counts = oracle.escape_grid(MANDELBROT, dbl, ARITH_PARITY, c1["w"], c1["h"], c1["x0"], c1["y0"], c1["dx"],
+                                       c1["dy"], c1["max_iter"])
+    assert int(total) == c1[f"total_{tag}"]
+    assert int((counts == c1["max_iter"]).sum()) == c1[f"interior_{tag}"]
+    assert hashlib.sha256(counts.astype("<u4").tobytes()).hexdigest() == c1[f"sha256_{tag}"]
+    assert counts[300:332, 600:632].tolist() == c1[f"crop_{tag}"]
+
+
+def test_c1_survey_numbers(golden):
+    # the figures the survey measured with the reference's code (FP32 and FP64, no contraction)
+    assert golden["c1"]["total_f32"] == 181_032_650 and golden["c1"]["interior_f32"] == 175_986
+    assert golden["c1"]["total_f64"] == 181_040_256 and golden["c1"]["interior_f64"] == 176_008
+
+
+def test_mandelbrot_points(oracle, golden):
+    bad = []
+    for p in golden["mandelbrot_points"]:
+        f = oracle.compute_fractal(MANDELBROT, 0, ARITH_PARITY, p["max_iter"], np.float32(p["x"]), np.float32(p["y"]))
+        d = oracle.compute_fractal(MANDELBROT, 1, ARITH_PARITY, p["max_iter"], p["x"], p["y"])
+        if f != p["f32"] or d != p["f64"]:
+            bad.append((p, f, d))
+    assert not bad, bad[:5]
+
+
+def test_julia_points(oracle, golden):
+    bad = []
+    for p in golden["julia_points"]:
+        c = tuple(p["c"])
+        f = oracle.compute_fractal(JULIA, 0, ARITH_PARITY, p["max_iter"], np.float32(p["x"]), np.float32(p["y"]), c)
+        d = oracle.compute_fractal(JULIA, 1, ARITH_PARITY, p["max_iter"], p["x"], p["y"], c)
+        if f != p["f32"] or d != p["f64"]:
+            bad.append((p, f, d))
+    assert not bad, bad[:5]
+
+
+def test_colorize_default_palette(oracle, golden):
+    from chaos_gb300.palette import default_palette
+
+    pal = default_palette()
+    assert hashlib.sha256(pal.astype("<u4").tobytes()).hexdigest() == golden["default_palette_sha256"]
+    from oracle.oracle import PIXEL_DTYPE
+
+    cases = golden["colorize_default_palette"]
+    pix = np.zeros((1, len(cases)), dtype=PIXEL_DTYPE)
+    pix["value"][0] = [c["value"] for c in cases]
+    pix["weight"][0] = 1
+    got = oracle.compose(pix, pal, 1.0)[0]
+    assert got.tolist() == [c["rgba"] for c in cases]
+
+
+def test_oracle_matches_reference_live(oracle, reference):
+    """Where the reference builds on this host: extra random points, bit for bit."""
+    rng = np.random.default_rng(7)
+    xs = rng.uniform(-2.2, 0.8, 4000)
+    ys = rng.uniform(-1.3, 1.3, 4000)
+    for x, y in zip(xs, ys):
+        for dbl in (0, 1):
+            xv, yv = (x, y) if dbl else (np.float32(x), np.float32(y))
+            assert oracle.compute_fractal(MANDELBROT, dbl, ARITH_PARITY, 500, xv, yv) == reference.mandelbrot(dbl, 500,
+                                                                                                             xv, yv)
+    c = (-0.8, 0.156)
+    for x, y in zip(xs[:1000] * 0.6, ys[:1000]):
+        for dbl in (0, 1):
+            xv, yv = (x, y) if dbl else (np.float32(x), np.float32(y))
+            assert oracle.compute_fractal(JULIA, dbl, ARITH_PARITY, 300, xv, yv, c) == reference.julia(dbl, 300, xv,
+                                                                                                      yv, c)
