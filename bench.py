@@ -79,6 +79,24 @@ def boundary_point(seed, max_iter=MAX_ITER, steps=200):
     return c_in.real, c_in.imag
 
 
+def deep_center(seed, bits=1024):
+    """A deep-zoom centre as "[-]I.hex" fixed-point strings with `bits` fraction
+    bits: the boundary point of `seed` (binary64) extended below its last bit
+    with seeded random bits."""
+    import numpy as np
+    from fractions import Fraction
+
+    from chaos_gb300 import to_hex_fixed
+    cx, cy = boundary_point(seed)
+    rng = np.random.default_rng(seed + 12345)
+    out = []
+    for v in (cx, cy):
+        low = Fraction(int.from_bytes(rng.bytes(bits // 8), "little"), 1 << bits) * Fraction(2) ** -60
+        f = Fraction(v) + (low if v >= 0 else -low)
+        out.append(to_hex_fixed(f, bits))
+    return out[0], out[1]
+
+
 def workload(seed=WORKLOAD_SEED):
     from chaos_gb300.palette import seeded_palette
     cx, cy = boundary_point(seed)
@@ -384,7 +402,7 @@ def run_ours(args):
         "data": "synthetic: seeded boundary centre, seeded jitter offsets, seeded palette",
         "config": {"workload": f"Mandelbrot {W}x{H} span {SPAN} maxIter {MAX_ITER} {SPP} jittered spp, "
                                f"256-entry palette with linear interpolation",
-                   "center": list(wl["center"]), "tier": "f64", "arith": "fma",
+                   "center": list(wl["center"]), "tier": "f64", "arith": "rounded (no contraction)",
                    "l2": "flushed between steps (256 MiB write, outside the events)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "pixel_iterations_per_step": iters_per_frame,

@@ -41,6 +41,8 @@ SAMPLES_CENTER = 0
 SAMPLES_JITTER = 1
 TIER_F32 = 0
 TIER_F64 = 1
+TIER_PERTURB_F32 = 3
+TIER_PERTURB_F64 = 4
 
 MANDELBROT = 0
 JULIA = 1
@@ -81,7 +83,7 @@ class FrameOut(C.Structure):
     _fields_ = [
         ("counts", C.c_void_p), ("smooth", C.c_void_p), ("pixels", C.c_void_p), ("pixels_pitch", C.c_long),
         ("rgba", C.c_void_p), ("palette", C.c_void_p), ("palette_len", C.c_uint32),
-        ("interior_rgba", C.c_uint32), ("total_iterations", C.c_void_p),
+        ("interior_rgba", C.c_uint32), ("total_iterations", C.c_void_p), ("rebases", C.c_void_p),
     ]
 
 
@@ -126,6 +128,11 @@ SIGNATURES = {
     "chaos_render_frame": (_int, [C.POINTER(FrameDesc), C.POINTER(FrameOut), _vp]),
     "chaos_render_frame_host": (_int, [C.POINTER(FrameDesc), _vp, _u32, _u32, _vp, C.POINTER(C.c_ulonglong), _vp]),
     "chaos_measure_fma_peak": (_int, [_u32, C.POINTER(C.c_double)]),
+    "chaos_orbit_create": (_int, [C.c_char_p, C.c_char_p, _u32, _u32, C.POINTER(_vp)]),
+    "chaos_orbit_info": (_int, [_vp, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
+    "chaos_orbit_destroy": (_int, [_vp]),
+    "chaos_render_frame_perturb_async": (_int, [C.POINTER(FrameDesc), _vp, C.POINTER(FrameOut), _vp]),
+    "chaos_render_frame_perturb": (_int, [C.POINTER(FrameDesc), _vp, C.POINTER(FrameOut), _vp]),
 }
 
 _lib = None

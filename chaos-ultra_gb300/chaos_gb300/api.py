@@ -172,3 +172,48 @@ def measure_fma_peak(tier):
     v = C.c_double()
     check(lib().chaos_measure_fma_peak(tier, C.byref(v)))
     return v.value
+
+
+class Orbit:
+    """Reference orbit of a deep-zoom centre (chaos_orbit_create).  Centres are
+    "[-]I.hex" fixed-point strings (see to_hex_fixed)."""
+
+    def __init__(self, center_x, center_y, bits, max_iterations):
+        h = C.c_void_p()
+        check(lib().chaos_orbit_create(center_x.encode(), center_y.encode(), bits, max_iterations, C.byref(h)))
+        self.handle = h
+
+    def info(self):
+        n, e, b = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        check(lib().chaos_orbit_info(self.handle, C.byref(n), C.byref(e), C.byref(b)))
+        return {"stored": n.value, "escaped_at": e.value, "bits": b.value}
+
+    def close(self):
+        if self.handle:
+            lib().chaos_orbit_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def render_frame_perturb(desc: FrameDesc, orbit: Orbit, out: FrameOut, stream=None, sync=True):
+    fn = lib().chaos_render_frame_perturb if sync else lib().chaos_render_frame_perturb_async
+    check(fn(C.byref(desc), orbit.handle, C.byref(out), _stream(stream)))
+
+
+def to_hex_fixed(value, bits):
+    """A real number (int/float/fractions.Fraction/decimal string handled by
+    fractions.Fraction) as "[-]I.hex" with `bits` fraction bits, truncated."""
+    from fractions import Fraction
+    v = Fraction(value)
+    neg = v < 0
+    v = abs(v)
+    ip = int(v)
+    frac = v - ip
+    digits = (bits + 3) // 4
+    f = int(frac * (1 << (4 * digits)))
+    return ("-" if neg else "") + f"{ip}." + format(f, f"0{digits}x")

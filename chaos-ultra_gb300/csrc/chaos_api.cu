@@ -161,6 +161,29 @@ double double_ulp(double d)  // java.lang.Math.ulp(double)
 
 }  // namespace
 
+namespace chaos {
+// shared with the other translation units of the library (chaos_perturb.cu)
+int api_fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int api_device_counter(cudaStream_t s, uint32_t **counter, int *sms)
+{
+    DeviceState *d;
+    int rc = device_state(&d);
+    if (rc) return rc;
+    *sms = d->sms;
+    return take_counter(d, s, counter);
+}
+}  // namespace chaos
+
 struct chaos_module {
     int fractal = FRACTAL_MANDELBROT;
     std::string name;

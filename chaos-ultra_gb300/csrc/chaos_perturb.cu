@@ -1,0 +1,431 @@
+// chaos_perturb.cu -- deep-zoom tier: perturbation against a reference orbit.
+//
+// The reference orbit Z_n of the frame centre C is computed on the host in
+// multi-word fixed point (bigfix.h) and kept on the device.  Each sample at
+// c = C + dc iterates only its difference d_n = z_n - Z_m in binary32 or
+// binary64:
+//     d_{n+1} = (2 Z_m + d_n) d_n + dc,   m <- m + 1,   z_{n+1} = Z_m + d_{n+1}
+// Escape is tested on z (continue while |z|^2 < 4, as the reference loop).
+// Glitch test and repair (rebasing): when |z| < |d| the difference has lost
+// its precision relative to z, so the sample restarts from the start of the
+// orbit with d = z (Z_0 = 0); the same happens when m reaches the end of a
+// reference orbit that escaped early.  Rebases are counted.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/chaos_gb300.h"
+#include "bigfix.h"
+#include "chaos_kernels.cuh"
+
+namespace chaos {
+
+int api_fail(int code, const char *fmt, ...);  // chaos_api.cu
+int api_device_counter(cudaStream_t s, uint32_t **counter, int *sms);
+
+template <class D> struct Vec2T;
+template <> struct Vec2T<float> {
+    using type = float2;
+};
+template <> struct Vec2T<double> {
+    using type = double2;
+};
+
+template <class D> struct PerturbArgs {
+    uint32_t w, h, spp, mode, max_iter, n_pix;
+    uint64_t seed;
+    double ps, half_w, half_h;
+    const typename Vec2T<D>::type *orbit;  // Z_0 .. Z_{orbit_last}
+    uint32_t orbit_last;
+    uint32_t *counts;
+    float *smooth;
+    PixelInfo *pixels;
+    long pixels_pitch;
+    uint32_t *rgba;
+    const uint32_t *palette;
+    uint32_t palette_len;
+    uint32_t interior_rgba;
+    unsigned long long *total;
+    unsigned long long *rebases;
+    uint32_t *counter;
+};
+
+__device__ __forceinline__ double unit53(uint64_t h) { return (double)(h >> 11) * 0x1p-53; }
+
+// n + 1 - log2(log2|z_n|), as the plain frame path.
+__device__ __forceinline__ float perturb_smooth(uint32_t i, float r2, uint32_t max_iter)
+{
+    if (i >= max_iter) return (float)max_iter;
+    if (!(r2 < 3.0e38f)) return (float)i;
+    float l = __fmul_rn(0.5f, log2f(r2));
+    return __fsub_rn((float)(i + 1u), log2f(l));
+}
+
+__device__ __forceinline__ void perturb_palette(const uint32_t *pal, uint32_t len, float nu, float ch[4])
+{
+    float fl = (float)len;
+    float t = fmodf(nu, fl);
+    if (t < 0.f) t = __fadd_rn(t, fl);
+    uint32_t i0 = (uint32_t)t;
+    if (i0 >= len) i0 = len - 1u;
+    float f = __fsub_rn(t, (float)i0);
+    uint32_t i1 = i0 + 1u == len ? 0u : i0 + 1u;
+    uint32_t c0 = pal[i0], c1 = pal[i1];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        float a0 = (float)((c0 >> (8 * k)) & 255u), a1 = (float)((c1 >> (8 * k)) & 255u);
+        ch[k] = __fmaf_rn(__fsub_rn(a1, a0), f, a0);
+    }
+}
+
+template <class D, int K> __global__ void __launch_bounds__(256) k_perturb(PerturbArgs<D> a)
+{
+    using O = Op<D>;
+    constexpr uint32_t FULLM = 0xffffffffu;
+    __shared__ uint32_t s_pal[4096];
+    const uint32_t *pal = a.palette;
+    if (a.rgba && a.palette_len <= 4096u) {
+        for (uint32_t k = threadIdx.x; k < a.palette_len; k += blockDim.x) s_pal[k] = a.palette[k];
+        pal = s_pal;
+    }
+    __syncthreads();
+
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    uint32_t pix = 0xffffffffu, s = 0, i = 0, m = 0;
+    D dx = D(0), dy = D(0), dcx = D(0), dcy = D(0), Zx = D(0), Zy = D(0);
+    bool need = true, begin = false;
+    float acc_v = 0.f, acc[4] = {0.f, 0.f, 0.f, 0.f};
+    unsigned long long iters = 0, rebases = 0;
+
+    for (;;) {
+        uint32_t need_mask = __ballot_sync(FULLM, need);
+        if (need_mask) {
+            uint32_t leader = __ffs(need_mask) - 1u;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(a.counter, (uint32_t)__popc(need_mask));
+            base = __shfl_sync(FULLM, base, leader);
+            if (need) {
+                pix = base + (uint32_t)__popc(need_mask & lt_mask);
+                need = false;
+                begin = true;
+                s = 0;
+                acc_v = 0.f;
+                acc[0] = acc[1] = acc[2] = acc[3] = 0.f;
+            }
+        }
+        const bool active = pix < a.n_pix;
+        if (!__any_sync(FULLM, active)) break;
+
+        bool done = false;
+        D r2 = D(0);
+        if (active) {
+            if (begin) {
+                begin = false;
+                uint32_t px = pix % a.w, py = pix / a.w;
+                double ox = 0.5, oy = 0.5;
+                if (a.mode == SAMPLES_JITTER) {
+                    ox = unit53(sample_hash(a.seed, pix, s, 0));
+                    oy = unit53(sample_hash(a.seed, pix, s, 1));
+                }
+                double ddx = __dmul_rn(__dsub_rn(__dadd_rn((double)px, ox), a.half_w), a.ps);
+                double ddy = __dmul_rn(-__dsub_rn(__dadd_rn((double)py, oy), a.half_h), a.ps);
+                dcx = (D)ddx;
+                dcy = (D)ddy;
+                dx = D(0);
+                dy = D(0);
+                Zx = D(0);
+                Zy = D(0);
+                m = 0;
+                i = 0;
+                if (a.max_iter == 0) done = true;
+            }
+#pragma unroll 4
+            for (int k = 0; k < K && !done; k++) {
+                // d' = (2Z + d) d + dc
+                D wx = O::fma(D(2), Zx, dx), wy = O::fma(D(2), Zy, dy);
+                D ndx = O::fma(wx, dx, O::fma(-wy, dy, dcx));
+                D ndy = O::fma(wx, dy, O::fma(wy, dx, dcy));
+                ++m;
+                ++i;
+                typename Vec2T<D>::type Z = a.orbit[m];
+                D zx = O::add(Z.x, ndx), zy = O::add(Z.y, ndy);
+                r2 = O::fma(zx, zx, O::mul(zy, zy));
+                if (!(r2 < D(4)) || i == a.max_iter) {
+                    done = true;
+                    break;
+                }
+                D d2 = O::fma(ndx, ndx, O::mul(ndy, ndy));
+                if (r2 < d2 || m == a.orbit_last) {
+                    dx = zx;
+                    dy = zy;
+                    Zx = D(0);
+                    Zy = D(0);
+                    m = 0;
+                    ++rebases;
+                } else {
+                    dx = ndx;
+                    dy = ndy;
+                    Zx = Z.x;
+                    Zy = Z.y;
+                }
+            }
+        }
+        if (done) {
+            const bool escaped = i < a.max_iter || !(r2 < D(4));
+            const uint32_t cnt = i;
+            const float nu = escaped && i < a.max_iter ? perturb_smooth(i, (float)r2, a.max_iter)
+                                                       : (float)a.max_iter;
+            const size_t sidx = (size_t)pix * a.spp + s;
+            if (a.counts) a.counts[sidx] = cnt;
+            if (a.smooth) a.smooth[sidx] = nu;
+            iters += cnt;
+            const bool esc = cnt < a.max_iter;
+            acc_v = __fadd_rn(acc_v, esc ? nu : 0.f);
+            if (a.rgba) {
+                float ch[4];
+                if (esc) {
+                    perturb_palette(pal, a.palette_len, nu, ch);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) ch[k] = (float)((a.interior_rgba >> (8 * k)) & 255u);
+                }
+#pragma unroll
+                for (int k = 0; k < 4; k++) acc[k] = __fadd_rn(acc[k], ch[k]);
+            }
+            ++s;
+            if (s == a.spp) {
+                uint32_t px = pix % a.w, py = pix / a.w;
+                if (a.pixels)
+                    store_pixel(pixel_ptr(a.pixels, a.pixels_pitch, px, py),
+                                make_pixel(__fdiv_rn(acc_v, (float)a.spp), (float)a.spp));
+                if (a.rgba) {
+                    uint32_t out = 0;
+                    float n = (float)a.spp;
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        float v = __fadd_rn(__fdiv_rn(acc[k], n), 0.5f);
+                        v = v < 255.f ? v : 255.f;
+                        out |= ((uint32_t)v & 255u) << (8 * k);
+                    }
+                    a.rgba[pix] = out;
+                }
+                need = true;
+            } else {
+                begin = true;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        iters += __shfl_down_sync(FULLM, iters, o);
+        rebases += __shfl_down_sync(FULLM, rebases, o);
+    }
+    if (lane == 0) {
+        if (a.total && iters) atomicAdd(a.total, iters);
+        if (a.rebases && rebases) atomicAdd(a.rebases, rebases);
+    }
+}
+
+template <class D> static cudaError_t launch_perturb(const PerturbArgs<D> &a, int sms, cudaStream_t s)
+{
+    static const int occ = [] {
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_perturb<D, 16>, 256, 0) != cudaSuccess || n < 1) n = 1;
+        return n;
+    }();
+    unsigned long long warps = ((unsigned long long)a.n_pix + 31ull) / 32ull;
+    unsigned long long blocks = (warps + 7ull) / 8ull;
+    unsigned long long cap = (unsigned long long)occ * (unsigned long long)sms;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    k_perturb<D, 16><<<(unsigned)blocks, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace chaos
+
+using namespace chaos;
+
+// ---- reference orbit ---------------------------------------------------------
+
+struct chaos_orbit {
+    int device = -1;
+    uint32_t max_iter = 0;
+    uint32_t last = 0;        // index of the last stored Z
+    uint32_t escaped_at = 0;  // iteration at which the reference escaped, or max_iter
+    uint32_t bits = 0;
+    double center_x = 0, center_y = 0;  // rounded centre, for reporting
+    float2 *z32 = nullptr;
+    double2 *z64 = nullptr;
+};
+
+int chaos_orbit_create(const char *center_x, const char *center_y, uint32_t bits, uint32_t max_iterations,
+                       chaos_orbit **out)
+{
+    if (!center_x || !center_y || !out) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (max_iterations < 1) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "maxIterations must be a positive number");
+    if (bits < 64 || bits > 64u * BIGFIX_MAX_LIMBS)
+        return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "precision must be 64..%d bits", 64 * BIGFIX_MAX_LIMBS);
+    const int limbs = (int)((bits + 63) / 64);
+    BigFix cx, cy;
+    if (!bigfix_parse_hex(center_x, limbs, cx) || !bigfix_parse_hex(center_y, limbs, cy))
+        return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "centre must be \"[-]I.hex\" fixed point");
+    if (cx.w[limbs] > 4 || cy.w[limbs] > 4) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "centre outside |c| < 4");
+
+    std::vector<double2> z64;
+    z64.reserve(std::min<uint32_t>(max_iterations, 1u << 20) + 1);
+    z64.push_back(make_double2(0.0, 0.0));
+    BigFix zx = bigfix_zero(limbs), zy = bigfix_zero(limbs);
+    uint32_t n = 0;
+    uint32_t escaped = max_iterations;
+    while (n < max_iterations) {
+        BigFix xx = bigfix_mul(zx, zx), yy = bigfix_mul(zy, zy), xy = bigfix_mul(zx, zy);
+        BigFix nx = bigfix_add(bigfix_sub(xx, yy), cx);
+        BigFix ny = bigfix_add(bigfix_mul2(xy), cy);
+        zx = nx;
+        zy = ny;
+        ++n;
+        double dx = bigfix_to_double(zx), dy = bigfix_to_double(zy);
+        z64.push_back(make_double2(dx, dy));
+        if (!(dx * dx + dy * dy < 4.0)) {
+            escaped = n;
+            break;
+        }
+    }
+    std::vector<float2> z32(z64.size());
+    for (size_t k = 0; k < z64.size(); k++) z32[k] = make_float2((float)z64[k].x, (float)z64[k].y);
+
+    chaos_orbit *o = new (std::nothrow) chaos_orbit();
+    if (!o) return api_fail(CHAOS_ERR_OUT_OF_MEMORY, "out of host memory");
+    cudaGetDevice(&o->device);
+    o->max_iter = max_iterations;
+    o->last = (uint32_t)(z64.size() - 1);
+    o->escaped_at = escaped;
+    o->bits = (uint32_t)(64 * limbs);
+    o->center_x = bigfix_to_double(cx);
+    o->center_y = bigfix_to_double(cy);
+    cudaError_t e = cudaMalloc(&o->z64, z64.size() * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&o->z32, z32.size() * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMemcpy(o->z64, z64.data(), z64.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(o->z32, z32.data(), z32.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        if (o->z64) cudaFree(o->z64);
+        if (o->z32) cudaFree(o->z32);
+        delete o;
+        return api_fail(CHAOS_ERR_CUDA, "reference orbit upload: %s", cudaGetErrorString(e));
+    }
+    *out = o;
+    return CHAOS_OK;
+}
+
+int chaos_orbit_info(const chaos_orbit *o, uint32_t *stored, uint32_t *escaped_at, uint32_t *bits)
+{
+    if (!o) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL orbit");
+    if (stored) *stored = o->last + 1;
+    if (escaped_at) *escaped_at = o->escaped_at;
+    if (bits) *bits = o->bits;
+    return CHAOS_OK;
+}
+
+int chaos_orbit_destroy(chaos_orbit *o)
+{
+    if (!o) return CHAOS_OK;
+    if (o->z64) cudaFree(o->z64);
+    if (o->z32) cudaFree(o->z32);
+    delete o;
+    return CHAOS_OK;
+}
+
+template <class D>
+static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const chaos_frame_out *o, cudaStream_t s,
+                        bool sync)
+{
+    PerturbArgs<D> a{};
+    a.w = d->width;
+    a.h = d->height;
+    a.spp = d->samples_per_pixel;
+    a.mode = d->sample_mode;
+    a.max_iter = d->max_iterations;
+    a.n_pix = d->width * d->height;
+    a.seed = d->seed;
+    a.ps = d->pixel_size;
+    a.half_w = 0.5 * d->width;
+    a.half_h = 0.5 * d->height;
+    if (std::is_same<D, float>::value)
+        a.orbit = reinterpret_cast<const typename Vec2T<D>::type *>(orb->z32);
+    else
+        a.orbit = reinterpret_cast<const typename Vec2T<D>::type *>(orb->z64);
+    a.orbit_last = orb->last;
+    a.counts = o->counts;
+    a.smooth = o->smooth;
+    a.pixels = reinterpret_cast<PixelInfo *>(o->pixels);
+    a.pixels_pitch = o->pixels_pitch;
+    a.rgba = o->rgba;
+    a.palette = o->palette;
+    a.palette_len = o->palette_len;
+    a.interior_rgba = o->interior_rgba;
+    a.total = o->total_iterations;
+    a.rebases = o->rebases;
+    int sms = 0;
+    int rc = api_device_counter(s, &a.counter, &sms);
+    if (rc) return rc;
+    cudaError_t e = launch_perturb<D>(a, sms, s);
+    if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e));
+    if (sync) {
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "cudaStreamSynchronize: %s", cudaGetErrorString(e));
+    }
+    return CHAOS_OK;
+}
+
+static int perturb_entry(const chaos_frame_desc *d, const chaos_orbit *orb, const chaos_frame_out *o, cudaStream_t s,
+                         bool sync)
+{
+    if (!d || !orb || !o) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (d->width == 0 || d->height == 0 || (uint64_t)d->width * d->height > (1ull << 31))
+        return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "bad frame size %u x %u", d->width, d->height);
+    if (d->samples_per_pixel < 1 || d->samples_per_pixel > 64)
+        return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "samples_per_pixel must be 1..64");
+    if (d->sample_mode == CHAOS_SAMPLES_CENTER && d->samples_per_pixel != 1)
+        return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "pixel-centre sampling takes one sample per pixel");
+    if (d->fractal != 0) return api_fail(CHAOS_ERR_UNSUPPORTED, "perturbation is implemented for mandelbrot");
+    if (!(d->pixel_size > 0) || !std::isfinite(d->pixel_size))
+        return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "pixel size must be finite and > 0");
+    if (d->max_iterations > orb->max_iter)
+        return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "orbit computed for maxIterations %u < %u", orb->max_iter,
+                        d->max_iterations);
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (dev != orb->device) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "orbit lives on device %d", orb->device);
+    if (o->rgba && (!o->palette || o->palette_len == 0))
+        return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "rgba output needs a palette");
+    if (d->tier == CHAOS_TIER_PERTURB_F32) {
+        // the differences must stay normal binary32 numbers
+        if (d->pixel_size < 1e-30)
+            return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "binary32 differences need pixel size >= 1e-30 (got %g)",
+                            d->pixel_size);
+        return perturb_impl<float>(d, orb, o, s, sync);
+    }
+    if (d->tier == CHAOS_TIER_PERTURB_F64) {
+        if (d->pixel_size < 1e-290)
+            return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "binary64 differences need pixel size >= 1e-290");
+        return perturb_impl<double>(d, orb, o, s, sync);
+    }
+    return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "tier %u is not a perturbation tier", d->tier);
+}
+
+int chaos_render_frame_perturb_async(const chaos_frame_desc *desc, const chaos_orbit *orbit,
+                                     const chaos_frame_out *out, void *stream)
+{
+    return perturb_entry(desc, orbit, out, (cudaStream_t)stream, false);
+}
+
+int chaos_render_frame_perturb(const chaos_frame_desc *desc, const chaos_orbit *orbit, const chaos_frame_out *out,
+                               void *stream)
+{
+    return perturb_entry(desc, orbit, out, (cudaStream_t)stream, true);
+}

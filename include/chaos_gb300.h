@@ -204,8 +204,10 @@ int chaos_renderer_destroy(chaos_renderer *r);
 #define CHAOS_SAMPLES_CENTER 0 /* one sample at each pixel centre */
 #define CHAOS_SAMPLES_JITTER 1 /* samples_per_pixel seeded uniform offsets */
 
-#define CHAOS_TIER_F32 0  /* escape loop in binary32 */
-#define CHAOS_TIER_F64 1  /* escape loop in binary64 */
+#define CHAOS_TIER_F32 0         /* escape loop in binary32 */
+#define CHAOS_TIER_F64 1         /* escape loop in binary64 */
+#define CHAOS_TIER_PERTURB_F32 3 /* perturbation, binary32 differences (pixel size >= 1e-30) */
+#define CHAOS_TIER_PERTURB_F64 4 /* perturbation, binary64 differences (pixel size >= 1e-290) */
 
 /* One frame of the plain escape-time renderer.  Sample s of pixel (px, py)
  * sits at plane point
@@ -244,6 +246,7 @@ typedef struct chaos_frame_out {
     uint32_t palette_len;
     uint32_t interior_rgba;
     unsigned long long *total_iterations;
+    unsigned long long *rebases; /* perturbation tiers: glitch repairs (rebasing events) */
 } chaos_frame_out;
 
 /* Enqueue one frame (does not synchronise). */
@@ -259,6 +262,31 @@ int chaos_render_frame(const chaos_frame_desc *desc, const chaos_frame_out *out,
 int chaos_render_frame_host(const chaos_frame_desc *desc, const uint32_t *palette, uint32_t palette_len,
                             uint32_t interior_rgba, uint32_t *rgba_host, unsigned long long *total_host,
                             void *stream);
+
+/* ---- deep zoom: perturbation against a multi-word reference orbit ------- */
+
+/* The reference orbit Z_n of the frame centre, computed on the host in
+ * multi-word fixed point (`bits` of fraction, 64..1536) and kept on the current
+ * device.  The centre is given as "[-]I.hex": a decimal integer part and
+ * hexadecimal fraction digits (4 bits each), e.g. "-0.8a3f...".  The orbit is
+ * stored until the reference escapes or reaches max_iterations. */
+typedef struct chaos_orbit chaos_orbit;
+int chaos_orbit_create(const char *center_x, const char *center_y, uint32_t bits, uint32_t max_iterations,
+                       chaos_orbit **out);
+/* Stored entries (Z_0..Z_{stored-1}), the iteration the reference escaped at
+ * (max_iterations if it did not) and the precision actually used. */
+int chaos_orbit_info(const chaos_orbit *orbit, uint32_t *stored, uint32_t *escaped_at, uint32_t *bits);
+int chaos_orbit_destroy(chaos_orbit *orbit);
+
+/* A frame by perturbation (tier CHAOS_TIER_PERTURB_F32 or _F64, Mandelbrot).
+ * Sample positions as in chaos_render_frame with the orbit's centre as centre
+ * (desc->center_x/y are not used): each sample iterates its difference from the
+ * reference orbit and restarts from the orbit's start (rebasing) when
+ * |z| < |difference| or when the orbit ends.  Outputs as chaos_render_frame. */
+int chaos_render_frame_perturb_async(const chaos_frame_desc *desc, const chaos_orbit *orbit,
+                                     const chaos_frame_out *out, void *stream);
+int chaos_render_frame_perturb(const chaos_frame_desc *desc, const chaos_orbit *orbit, const chaos_frame_out *out,
+                               void *stream);
 
 /* ---- diagnostics -------------------------------------------------------- */
 

@@ -830,3 +830,219 @@ int orc_max_threads(void)
     return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------------ */
+/* High-precision direct iteration (the deep-zoom oracle)                     */
+/* ------------------------------------------------------------------------ */
+/* Signed fixed point with 32-bit limbs: value = sign * sum_{k=0..L} w[k] *
+ * 2^(32(k-L)), w[L] the integer part.  Independent of the library's own
+ * multi-word code (64-bit limbs); pinned against mpmath by the tests. */
+#define HP_MAX 64 /* up to 2048 fraction bits */
+typedef struct {
+    int L;
+    int neg;
+    uint32_t w[HP_MAX + 1];
+} hpnum;
+
+static int hp_iszero(const hpnum *a)
+{
+    for (int k = 0; k <= a->L; k++)
+        if (a->w[k]) return 0;
+    return 1;
+}
+
+static int hp_cmpmag(const hpnum *a, const hpnum *b)
+{
+    for (int k = a->L; k >= 0; k--)
+        if (a->w[k] != b->w[k]) return a->w[k] < b->w[k] ? -1 : 1;
+    return 0;
+}
+
+static void hp_addsub(const hpnum *a, const hpnum *b, int negate_b, hpnum *r)
+{
+    int bneg = b->neg ^ negate_b;
+    r->L = a->L;
+    if (a->neg == bneg) {
+        uint64_t c = 0;
+        for (int k = 0; k <= a->L; k++) {
+            c += (uint64_t)a->w[k] + b->w[k];
+            r->w[k] = (uint32_t)c;
+            c >>= 32;
+        }
+        r->neg = a->neg;
+    } else {
+        const hpnum *x = a, *y = b;
+        int sign = a->neg;
+        if (hp_cmpmag(a, b) < 0) {
+            x = b;
+            y = a;
+            sign = bneg;
+        }
+        int64_t br = 0;
+        for (int k = 0; k <= a->L; k++) {
+            int64_t d = (int64_t)x->w[k] - y->w[k] - br;
+            br = d < 0;
+            r->w[k] = (uint32_t)(d + (br ? ((int64_t)1 << 32) : 0));
+        }
+        r->neg = sign;
+    }
+    if (hp_iszero(r)) r->neg = 0;
+}
+
+static void hp_mul(const hpnum *a, const hpnum *b, hpnum *r)
+{
+    int L = a->L;
+    uint64_t col[2 * HP_MAX + 4];
+    memset(col, 0, sizeof(uint64_t) * (size_t)(2 * L + 4));
+    uint32_t p[2 * HP_MAX + 4];
+    /* column sums of 32x32 products, carried as we go */
+    for (int i = 0; i <= L; i++) {
+        uint64_t carry = 0;
+        for (int j = 0; j <= L; j++) {
+            uint64_t t = (uint64_t)a->w[i] * b->w[j] + col[i + j] + carry;
+            col[i + j] = t & 0xffffffffu;
+            carry = t >> 32;
+        }
+        int k = i + L + 1;
+        while (carry) {
+            uint64_t t = col[k] + carry;
+            col[k] = t & 0xffffffffu;
+            carry = t >> 32;
+            k++;
+        }
+    }
+    for (int k = 0; k < 2 * L + 4; k++) p[k] = (uint32_t)col[k];
+    r->L = L;
+    for (int k = 0; k <= L; k++) r->w[k] = p[k + L];
+    r->neg = (a->neg != b->neg) && !hp_iszero(r);
+}
+
+static void hp_from_double(double d, int L, hpnum *r)
+{
+    memset(r, 0, sizeof *r);
+    r->L = L;
+    if (d == 0.0) return;
+    r->neg = d < 0;
+    d = fabs(d);
+    int e;
+    double m = frexp(d, &e);
+    uint64_t mant = (uint64_t)ldexp(m, 53);
+    int shift = e - 53 + 32 * L; /* bit position of the mantissa's lsb */
+    for (int b = 0; b < 53; b++) {
+        if (!((mant >> b) & 1)) continue;
+        int pos = shift + b;
+        if (pos < 0 || pos >= 32 * (L + 1)) continue;
+        r->w[pos / 32] |= 1u << (pos % 32);
+    }
+    if (hp_iszero(r)) r->neg = 0;
+}
+
+static double hp_to_double(const hpnum *a)
+{
+    double v = 0;
+    for (int k = a->L; k >= 0 && k >= a->L - 3; k--) v += ldexp((double)a->w[k], 32 * (k - a->L));
+    return a->neg ? -v : v;
+}
+
+static int hp_parse_hex(const char *s, int L, hpnum *r)
+{
+    memset(r, 0, sizeof *r);
+    r->L = L;
+    int neg = 0;
+    if (*s == '-') {
+        neg = 1;
+        s++;
+    }
+    uint32_t ip = 0;
+    while (*s >= '0' && *s <= '9') ip = ip * 10 + (uint32_t)(*s++ - '0');
+    r->w[L] = ip;
+    if (*s == '.') {
+        s++;
+        int bit = 32 * L;
+        while (*s) {
+            int v;
+            char c = *s++;
+            if (c >= '0' && c <= '9')
+                v = c - '0';
+            else if (c >= 'a' && c <= 'f')
+                v = c - 'a' + 10;
+            else if (c >= 'A' && c <= 'F')
+                v = c - 'A' + 10;
+            else
+                return 0;
+            bit -= 4;
+            if (bit >= 0) r->w[bit / 32] |= (uint32_t)v << (bit % 32);
+        }
+    }
+    r->neg = neg && !hp_iszero(r);
+    return 1;
+}
+
+/* Mandelbrot at c = C + (dcx, dcy) in `bits` of fixed-point fraction:
+ * continue while |z|^2 < 4 and i < max_iter (the reference loop's test).
+ * Returns i; *r2 = |z_i|^2 as a double. */
+uint32_t orc_hp_escape(const char *cx_hex, const char *cy_hex, double dcx, double dcy, uint32_t bits,
+                       uint32_t max_iter, double *r2)
+{
+    int L = (int)((bits + 31) / 32);
+    if (L > HP_MAX) L = HP_MAX;
+    hpnum cx, cy, dx, dy, zx, zy, xx, yy, xy, t;
+    hp_parse_hex(cx_hex, L, &cx);
+    hp_parse_hex(cy_hex, L, &cy);
+    hp_from_double(dcx, L, &dx);
+    hp_from_double(dcy, L, &dy);
+    hp_addsub(&cx, &dx, 0, &t);
+    cx = t;
+    hp_addsub(&cy, &dy, 0, &t);
+    cy = t;
+    memset(&zx, 0, sizeof zx);
+    memset(&zy, 0, sizeof zy);
+    zx.L = zy.L = L;
+    uint32_t i = 0;
+    double rr = 0;
+    for (;;) {
+        hp_mul(&zx, &zx, &xx);
+        hp_mul(&zy, &zy, &yy);
+        double x2 = hp_to_double(&xx), y2 = hp_to_double(&yy);
+        rr = x2 + y2;
+        if (!(i < max_iter && rr < 4.0)) break;
+        hp_mul(&zx, &zy, &xy);
+        hp_addsub(&xx, &yy, 1, &t);
+        hp_addsub(&t, &cx, 0, &zx);
+        hp_addsub(&xy, &xy, 0, &t);
+        hp_addsub(&t, &cy, 0, &zy);
+        ++i;
+    }
+    if (r2) *r2 = rr;
+    return i;
+}
+
+void orc_hp_escape_batch(const char *cx_hex, const char *cy_hex, long n, const double *dcx, const double *dcy,
+                         uint32_t bits, uint32_t max_iter, uint32_t *counts, double *r2)
+{
+#pragma omp parallel for schedule(dynamic, 1)
+    for (long k = 0; k < n; k++) {
+        double rr;
+        counts[k] = orc_hp_escape(cx_hex, cy_hex, dcx[k], dcy[k], bits, max_iter, &rr);
+        if (r2) r2[k] = rr;
+    }
+}
+
+/* The plane offsets dc of frame samples relative to the centre, in the order
+ * of orc_frame's outputs (perturbation frames): dc = ((p + o) - n/2) * ps. */
+void orc_frame_offsets(const orc_frame_desc *d, long pix_start, long pix_count, double *dcx, double *dcy)
+{
+    for (long q = 0; q < pix_count; q++) {
+        uint32_t pix = (uint32_t)(pix_start + q);
+        uint32_t px = pix % d->w, py = pix / d->w;
+        for (uint32_t s = 0; s < d->spp; s++) {
+            double ox = 0.5, oy = 0.5;
+            if (d->mode == 1) {
+                ox = (double)(orc_sample_hash(d->seed, pix, s, 0) >> 11) * 0x1p-53;
+                oy = (double)(orc_sample_hash(d->seed, pix, s, 1) >> 11) * 0x1p-53;
+            }
+            dcx[(size_t)q * d->spp + s] = (((double)px + ox) - 0.5 * d->w) * d->pixel_size;
+            dcy[(size_t)q * d->spp + s] = -(((double)py + oy) - 0.5 * d->h) * d->pixel_size;
+        }
+    }
+}

@@ -73,6 +73,14 @@ class Oracle:
         L.orc_mandelbrot_points_d.restype = C.c_uint64
         L.orc_mandelbrot_points_d.argtypes = [C.c_long, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p]
         L.orc_max_threads.restype = C.c_int
+        L.orc_hp_escape.restype = C.c_uint32
+        L.orc_hp_escape.argtypes = [C.c_char_p, C.c_char_p, C.c_double, C.c_double, C.c_uint32, C.c_uint32,
+                                    C.POINTER(C.c_double)]
+        L.orc_hp_escape_batch.restype = None
+        L.orc_hp_escape_batch.argtypes = [C.c_char_p, C.c_char_p, C.c_long, C.c_void_p, C.c_void_p, C.c_uint32,
+                                          C.c_uint32, C.c_void_p, C.c_void_p]
+        L.orc_frame_offsets.restype = None
+        L.orc_frame_offsets.argtypes = [C.POINTER(FrameDesc), C.c_long, C.c_long, C.c_void_p, C.c_void_p]
         L.orc_sample_hash.restype = C.c_uint64
         L.orc_sample_hash.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32]
 
@@ -155,6 +163,28 @@ class Oracle:
         total = self.lib.orc_mandelbrot_points_d(len(xs), _ptr(xs), _ptr(ys), max_iter, arith, _ptr(out))
         return int(total), out
 
+    def hp_escape(self, cx_hex, cy_hex, dcx, dcy, bits, max_iter):
+        r2 = C.c_double()
+        i = self.lib.orc_hp_escape(cx_hex.encode(), cy_hex.encode(), dcx, dcy, bits, max_iter, C.byref(r2))
+        return i, r2.value
+
+    def hp_escape_batch(self, cx_hex, cy_hex, dcx, dcy, bits, max_iter):
+        dcx = np.ascontiguousarray(dcx, dtype=np.float64)
+        dcy = np.ascontiguousarray(dcy, dtype=np.float64)
+        counts = np.zeros(len(dcx), dtype=np.uint32)
+        r2 = np.zeros(len(dcx), dtype=np.float64)
+        self.lib.orc_hp_escape_batch(cx_hex.encode(), cy_hex.encode(), len(dcx), _ptr(dcx), _ptr(dcy), bits,
+                                     max_iter, _ptr(counts), _ptr(r2))
+        return counts, r2
+
+    def frame_offsets(self, w, h, spp, mode, seed, pixel_size, pix_start, pix_count):
+        """Plane offsets (dcx, dcy) from the centre of frame samples of pixels [pix_start, +pix_count)."""
+        d = FrameDesc(w, h, 0, spp, mode, 1, 0, 0, seed, 0.0, 0.0, pixel_size, 0.0, 0.0)
+        xs = np.zeros(pix_count * spp, dtype=np.float64)
+        ys = np.zeros(pix_count * spp, dtype=np.float64)
+        self.lib.orc_frame_offsets(C.byref(d), pix_start, pix_count, _ptr(xs), _ptr(ys))
+        return xs, ys
+
     def max_threads(self):
         return self.lib.orc_max_threads()
 
@@ -207,6 +237,28 @@ class Reference:
         out = np.zeros(len(xs), dtype=np.uint32)
         total = self.lib.ref_mandelbrot_points_d(len(xs), _ptr(xs), _ptr(ys), max_iter, threads, _ptr(out))
         return total, out
+
+    def hp_escape(self, cx_hex, cy_hex, dcx, dcy, bits, max_iter):
+        r2 = C.c_double()
+        i = self.lib.orc_hp_escape(cx_hex.encode(), cy_hex.encode(), dcx, dcy, bits, max_iter, C.byref(r2))
+        return i, r2.value
+
+    def hp_escape_batch(self, cx_hex, cy_hex, dcx, dcy, bits, max_iter):
+        dcx = np.ascontiguousarray(dcx, dtype=np.float64)
+        dcy = np.ascontiguousarray(dcy, dtype=np.float64)
+        counts = np.zeros(len(dcx), dtype=np.uint32)
+        r2 = np.zeros(len(dcx), dtype=np.float64)
+        self.lib.orc_hp_escape_batch(cx_hex.encode(), cy_hex.encode(), len(dcx), _ptr(dcx), _ptr(dcy), bits,
+                                     max_iter, _ptr(counts), _ptr(r2))
+        return counts, r2
+
+    def frame_offsets(self, w, h, spp, mode, seed, pixel_size, pix_start, pix_count):
+        """Plane offsets (dcx, dcy) from the centre of frame samples of pixels [pix_start, +pix_count)."""
+        d = FrameDesc(w, h, 0, spp, mode, 1, 0, 0, seed, 0.0, 0.0, pixel_size, 0.0, 0.0)
+        xs = np.zeros(pix_count * spp, dtype=np.float64)
+        ys = np.zeros(pix_count * spp, dtype=np.float64)
+        self.lib.orc_frame_offsets(C.byref(d), pix_start, pix_count, _ptr(xs), _ptr(ys))
+        return xs, ys
 
     def max_threads(self):
         return self.lib.ref_max_threads()
