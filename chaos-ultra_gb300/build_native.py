@@ -55,7 +55,7 @@ def build(verbose=False, ptxas_info=False, force=False):
 
     jobs = []
     objs = []
-    for name in ("chaos_kernels", "chaos_api", "chaos_perturb"):
+    for name in ("chaos_kernels", "chaos_api", "chaos_perturb", "chaos_noalloc"):
         src = os.path.join(CSRC, name + ".cu")
         obj = os.path.join(BUILD, name + ".o")
         objs.append(obj)

@@ -128,6 +128,8 @@ SIGNATURES = {
     "chaos_render_frame": (_int, [C.POINTER(FrameDesc), C.POINTER(FrameOut), _vp]),
     "chaos_render_frame_host": (_int, [C.POINTER(FrameDesc), _vp, _u32, _u32, _vp, C.POINTER(C.c_ulonglong), _vp]),
     "chaos_measure_fma_peak": (_int, [_u32, C.POINTER(C.c_double)]),
+    "chaos_render_frame_host_noalloc": (_int, [C.POINTER(FrameDesc), _vp, _u32, _u32, _vp,
+                                               C.POINTER(C.c_ulonglong), _vp]),
     "chaos_orbit_create": (_int, [C.c_char_p, C.c_char_p, _u32, _u32, C.POINTER(_vp)]),
     "chaos_orbit_info": (_int, [_vp, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
     "chaos_orbit_destroy": (_int, [_vp]),

@@ -288,6 +288,21 @@ int chaos_render_frame_perturb_async(const chaos_frame_desc *desc, const chaos_o
 int chaos_render_frame_perturb(const chaos_frame_desc *desc, const chaos_orbit *orbit, const chaos_frame_out *out,
                                void *stream);
 
+/* chaos_render_frame_host for callers that must not allocate GPU memory (a
+ * host whose GPU memory is fixed before it starts serving frames, code between
+ * a stream-capture begin and end, a JNI/Panama binding without a CUDA
+ * allocator).  No counterpart in the reference.  The device-side image,
+ * palette, work counter and total live in one 64 MiB array that is part of the
+ * library (every GPU that loads it holds the array until exit): frames of at
+ * most 16,773,056 pixels (3840x2160 fits), palettes of at most 4096 entries,
+ * tiers CHAOS_TIER_F32/F64; larger requests fail with
+ * CHAOS_ERR_INVALID_ARGUMENT.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) and should come before any stream
+ * capture.  All calls share the array: calls whose GPU work overlaps race. */
+int chaos_render_frame_host_noalloc(const chaos_frame_desc *desc, const uint32_t *palette, uint32_t palette_len,
+                                    uint32_t interior_rgba, uint32_t *rgba_host, unsigned long long *total_host,
+                                    void *stream);
+
 /* ---- diagnostics -------------------------------------------------------- */
 
 /* Measured fused-multiply-add throughput of the current device in FLOP/s
