@@ -40,6 +40,7 @@ for _p in (PKG_DIR, ROOT):
 
 WORKLOAD_SEED = 2
 W, H, SPAN, MAX_ITER, SPP = 3840, 2160, 1e-10, 20000, 4
+FULL_W = W  # the plane span is defined on the full 3840-pixel width
 METRIC = "Gpixel-iter/s at <=0.1% escape-count mismatch vs FP64 oracle"
 MISMATCH_SAMPLE_PIXELS = 4096
 
@@ -48,59 +49,20 @@ MISMATCH_SAMPLE_PIXELS = 4096
 # workload
 # ---------------------------------------------------------------------------
 
-def _escapes(cx, cy, max_iter):
-    x = y = 0.0
-    for _ in range(max_iter):
-        xx, yy = x * x, y * y
-        if xx + yy >= 4.0:
-            return True
-        y = 2.0 * x * y + cy
-        x = xx - yy + cx
-    return False
-
-
-def boundary_point(seed, max_iter=MAX_ITER, steps=200):
-    """Bisection between a seeded interior point of the main cardioid
-    (c = mu/2 - mu^2/4, |mu| < 1) and a seeded point on |c| = 2.5."""
-    import numpy as np
-    rng = np.random.default_rng(seed)
-    r, t, s = rng.uniform(0.3, 0.95), rng.uniform(0, 2 * math.pi), rng.uniform(0, 2 * math.pi)
-    mu = complex(r * math.cos(t), r * math.sin(t))
-    c_in = mu / 2 - mu * mu / 4
-    c_out = complex(2.5 * math.cos(s), 2.5 * math.sin(s))
-    for _ in range(steps):
-        mid = (c_in + c_out) / 2
-        if mid == c_in or mid == c_out:
-            break
-        if _escapes(mid.real, mid.imag, max_iter):
-            c_out = mid
-        else:
-            c_in = mid
-    return c_in.real, c_in.imag
+def boundary_point(seed, max_iter=MAX_ITER):
+    from chaos_gb300.workloads import boundary_point as bp
+    return bp(seed, max_iter)
 
 
 def deep_center(seed, bits=1024):
-    """A deep-zoom centre as "[-]I.hex" fixed-point strings with `bits` fraction
-    bits: the boundary point of `seed` (binary64) extended below its last bit
-    with seeded random bits."""
-    import numpy as np
-    from fractions import Fraction
-
-    from chaos_gb300 import to_hex_fixed
-    cx, cy = boundary_point(seed)
-    rng = np.random.default_rng(seed + 12345)
-    out = []
-    for v in (cx, cy):
-        low = Fraction(int.from_bytes(rng.bytes(bits // 8), "little"), 1 << bits) * Fraction(2) ** -60
-        f = Fraction(v) + (low if v >= 0 else -low)
-        out.append(to_hex_fixed(f, bits))
-    return out[0], out[1]
+    from chaos_gb300.workloads import deep_center as dc
+    return dc(seed, bits)
 
 
 def workload(seed=WORKLOAD_SEED):
     from chaos_gb300.palette import seeded_palette
     cx, cy = boundary_point(seed)
-    return {"center": (cx, cy), "pixel_size": SPAN / W, "palette": seeded_palette(256, seed=seed),
+    return {"center": (cx, cy), "pixel_size": SPAN / FULL_W, "palette": seeded_palette(256, seed=seed),
             "jitter_seed": 1000 + seed, "interior_rgba": 0xFF000000}
 
 
@@ -216,9 +178,9 @@ def cpu_baseline(wl, budget_s=12.0):
         t0 = time.perf_counter()
         total, _ = run(xs, ys)
         dt = time.perf_counter() - t0
-        if dt >= budget_s / 4 or n >= (1 << 17):
+        if dt >= budget_s / 4 or n >= min(1 << 17, W * H):
             break
-        n = min(1 << 17, int(n * max(2.0, (budget_s / 4) / max(dt, 1e-3))))
+        n = min(1 << 17, W * H, int(n * max(2.0, (budget_s / 4) / max(dt, 1e-3))))
     return {"value": total / dt / 1e9, "unit": "Gpixel-iter/s", "cores": threads, "kind": kind,
             "sample": f"{n} seeded pixels x {SPP} jittered samples of the frame, maxIter {MAX_ITER}, FP64, "
                       f"{total} pixel-iterations in {dt:.2f} s"}
@@ -244,7 +206,7 @@ def run_reference(args):
     t0 = time.perf_counter()
     run(xs, ys)
     dt = max(time.perf_counter() - t0, 1e-3)
-    n = max(256, min(1 << 18, int(n * 8.0 / dt)))
+    n = max(256, min(1 << 18, W * H, int(n * 8.0 / dt)))
     pts = [cpu_sample_points(wl, n, seed=200 + k) for k in range(args.warmup + args.steps)]
     for k in range(args.warmup):
         run(pts[k][1], pts[k][2])
@@ -430,7 +392,12 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["c2", "c2-crop"], default="c2",
+                    help="c2-crop: the central 480x270 pixels of the same frame (for profiler captures)")
     args = ap.parse_args()
+    if args.workload == "c2-crop":
+        global W, H
+        W, H = 480, 270
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -97,11 +97,13 @@ template <class R, int A> __device__ __forceinline__ void step(R &x, R &y, R cx,
 //     i = 0; while (i < max_iter && r2(z) < 4) { z = z^2 + c; ++i; }  return i
 // run as blocks of ESCAPE_BLOCK untested steps.  A block is kept when its last
 // state still tests below 4; otherwise the state rolls back to the block start
-// and the steps are redone one test at a time.  This is exact when |c| <= 1.9:
-// once a computed |z|^2 reaches 4, |z'| >= 4 - 1.9 = 2.1 and |z| keeps growing
-// until it overflows to inf/NaN, and neither tests below 4, so a block whose
-// last state tests below 4 contains no escape.  For |c| > 1.9 `blockable` is
-// false and every step is tested.  r2_exit is r2 of the final state.
+// and the steps are redone one test at a time.  This is exact when
+// |c|^2 <= 3.99 (|c| <= 1.9975): once a computed |z|^2 reaches 4,
+// |z'| >= 4 - 1.9975 > 2.002 (rounding moves these by ~1e-6 at most in
+// binary32), and |z| keeps growing until it overflows to inf/NaN; neither
+// tests below 4, so a block whose last state tests below 4 contains no
+// escape.  Otherwise `blockable` is false and every step is tested.
+// r2_exit is r2 of the final state.
 template <class R, int A>
 __device__ __forceinline__ uint32_t escape(uint32_t max_iter, R x, R y, R cx, R cy, bool blockable, R &r2_exit)
 {
@@ -136,7 +138,7 @@ __device__ __forceinline__ uint32_t escape(uint32_t max_iter, R x, R y, R cx, R 
 
 template <class R> __device__ __forceinline__ bool blockable_c(R cx, R cy)
 {
-    return radius2<R, ARITH_PARITY>(cx, cy) <= R(3.61);
+    return radius2<R, ARITH_PARITY>(cx, cy) <= R(3.99);
 }
 
 // computeFractal (mandelbrot.cu:11-25, julia.cu:5-17) as an unsigned escape

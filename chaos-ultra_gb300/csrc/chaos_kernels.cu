@@ -140,6 +140,7 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
     uint32_t pix = 0xffffffffu, s = 0, i = 0;
     R x = R(0), y = R(0), cx = R(0), cy = R(0);
     bool blk = false, need = true, begin = false;
+    uint32_t window = 0;  // > 0: the escape lies within the next `window` steps
     float acc_v = 0.f, acc[4] = {0.f, 0.f, 0.f, 0.f};
     unsigned long long iters = 0;
 
@@ -164,6 +165,7 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
 
         bool done = false;
         R r2 = R(0);
+        uint32_t lim = 0;  // steps this lane takes this round: a power of two <= K
         if (active) {
             if (begin) {
                 begin = false;
@@ -182,50 +184,66 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
                 }
                 blk = blockable_c(cx, cy);
                 i = 0;
+                window = 0;
                 r2 = radius2<R, A>(x, y);
                 if (a.max_iter == 0 || !(r2 < R(4))) done = true;
             }
             if (!done) {
-                if (blk && a.max_iter - i >= (uint32_t)K) {
-                    R sx = x, sy = y;
-#pragma unroll
-                    for (int k = 0; k < K; k++) step<R, A>(x, y, cx, cy);
-                    r2 = radius2<R, A>(x, y);
-                    if (r2 < R(4)) {
-                        i += (uint32_t)K;
-                        if (i == a.max_iter) done = true;
-                    } else {
-                        // An escape happened inside the block: redo it with a
-                        // test after every step (it ends within K steps).
-                        x = sx;
-                        y = sy;
-                        for (int k = 0; k < K; k++) {
-                            step<R, A>(x, y, cx, cy);
-                            ++i;
-                            r2 = radius2<R, A>(x, y);
-                            if (!(r2 < R(4))) break;
-                        }
-                        done = true;
-                    }
+                if (!blk) {
+                    lim = 1;
+                } else if (window) {
+                    lim = window > 1u ? window >> 1 : 1u;
                 } else {
                     uint32_t rest = a.max_iter - i;
-                    uint32_t lim = rest < (uint32_t)K ? rest : (uint32_t)K;
-                    for (uint32_t k = 0; k < lim; k++) {
-                        step<R, A>(x, y, cx, cy);
-                        ++i;
-                        r2 = radius2<R, A>(x, y);
-                        if (!(r2 < R(4))) {
-                            done = true;
-                            break;
-                        }
-                    }
-                    if (i == a.max_iter) done = true;
+                    lim = rest >= (uint32_t)K ? (uint32_t)K : 1u << (31 - __clz(rest));
                 }
+            }
+        }
+        // Every stepping lane runs the same K unrolled steps.  A lane with
+        // lim < K keeps the state it had after lim steps (captured after steps
+        // 1, 2, 4, ...): that is how a lane whose block overshot an escape
+        // halves its search window each round without holding up the others.
+        const bool stepping = active && !done;
+        const bool partial = stepping && lim < (uint32_t)K;
+        const bool any_partial = __any_sync(FULL, partial);
+        if (stepping) {
+            const R sx = x, sy = y;
+            if (any_partial) {
+                R kx = x, ky = y;
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    step<R, A>(x, y, cx, cy);
+                    if (((k + 1) & k) == 0 && k + 1 < K && (uint32_t)(k + 1) == lim) {
+                        kx = x;
+                        ky = y;
+                    }
+                }
+                if (partial) {
+                    x = kx;
+                    y = ky;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < K; k++) step<R, A>(x, y, cx, cy);
+            }
+            r2 = radius2<R, A>(x, y);
+            if (r2 < R(4)) {
+                i += lim;
+                window = window > 1u ? window - lim : 0u;
+                if (i == a.max_iter) done = true;
+            } else if (lim == 1u) {
+                i += 1u;  // the escape step
+                done = true;
+            } else {
+                // the escape lies within these lim steps: search them
+                x = sx;
+                y = sy;
+                window = lim;
             }
         }
         if (done) {
             const bool escaped = i < a.max_iter;
-            const float nu = smooth_value(i, (float)r2, a.max_iter);
+            const float nu = (a.smooth || a.pixels || a.rgba) ? smooth_value(i, (float)r2, a.max_iter) : 0.f;
             const size_t sidx = (size_t)pix * a.spp + s;
             if (a.counts) a.counts[sidx] = i;
             if (a.smooth) a.smooth[sidx] = nu;
