@@ -190,6 +190,19 @@ def cpu_baseline(wl, budget_s=12.0):
 # arms
 # ---------------------------------------------------------------------------
 
+def aggregate_over_ranks(kernel_ms, pixel_iterations_per_step, steps, world, device=None):
+    """Replicas: every rank ran `steps` steps of the same work.  The job's time
+    is the slowest rank's; the job's throughput counts every rank's work.
+    Returns (max_ms, Gpixel-iter/s of the whole job)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(kernel_ms)], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    max_ms = float(t.item())
+    return max_ms, pixel_iterations_per_step * steps * world / (max_ms / 1e3) / 1e9
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -289,11 +302,7 @@ def run_ours(args):
         dist.barrier()
     lat = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     kernel_ms = sum(lat)
-    t = torch.tensor([kernel_ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    max_ms = float(t.item())
-    value = iters_per_frame * args.steps * world / (max_ms / 1e3) / 1e9
+    max_ms, value = aggregate_over_ranks(kernel_ms, iters_per_frame, args.steps, world, dev)
 
     # end to end: the host-buffer call a caller without device memory makes
     host_rgba = np.zeros(W * H, dtype=np.uint32)
@@ -386,13 +395,166 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def _l2_flush(torch, dev):
+    buf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    return lambda k: buf.fill_(k & 255)
+
+
+def run_batch(args):
+    """C4: 64 viewports (side 256..2048, span 1e-12..1e-3, maxIter 500..50000,
+    seeded boundary centres) in one CUDA-graph launch, tier per viewport."""
+    import numpy as np
+    import torch
+
+    import chaos_gb300 as cg
+    from chaos_gb300.workloads import c4_palette, c4_viewports
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    specs = c4_viewports()
+    pal = c4_palette()
+    dpal = torch.from_numpy(pal.view(np.int32)).to(dev)
+
+    def make(force_tier):
+        bufs, vps = [], []
+        for k, sp in enumerate(specs):
+            n = sp["width"] * sp["height"]
+            counts = torch.zeros(n, dtype=torch.int32, device=dev)
+            rgba = torch.zeros(n, dtype=torch.int32, device=dev)
+            bufs.append((counts, rgba))
+            vps.append(cg.Viewport(width=sp["width"], height=sp["height"], max_iterations=sp["max_iter"],
+                                   samples_per_pixel=1, sample_mode=cg.SAMPLES_CENTER,
+                                   tier=force_tier, seed=sp["seed"], center_x=sp["center"][0],
+                                   center_y=sp["center"][1], pixel_size=sp["span"] / sp["width"],
+                                   counts=counts.data_ptr(), rgba=rgba.data_ptr()))
+        return cg.Batch(vps, dpal.data_ptr(), len(pal), 0xFF000000), bufs
+
+    batch, bufs = make(cg.TIER_AUTO)
+    stream = torch.cuda.current_stream()
+    flush = _l2_flush(torch, dev)
+    for _ in range(args.warmup):
+        batch.launch(stream)
+    torch.cuda.synchronize()
+    per_launch = batch.read_total()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(0)
+    clocks.start()
+    for k in range(args.steps):
+        flush(k)
+        ev[k][0].record(stream)
+        batch.launch(stream)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    value = per_launch * args.steps / (sum(ms) / 1e3) / 1e9
+    tiers = batch.tiers()
+    tiered_counts = [c.cpu().numpy() for c, _ in bufs]
+
+    plain, pbufs = make(cg.TIER_F64)
+    plain.launch(stream)
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    plain.launch(stream)
+    s1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = s0.elapsed_time(s1)
+    plain_value = plain.read_total() / (plain_ms / 1e3) / 1e9
+    diff = sum(int((a != c.cpu().numpy()).sum()) for a, (c, _) in zip(tiered_counts, pbufs))
+    total = sum(len(a) for a in tiered_counts)
+    line = {"metric": "Gpixel-iter/s (batched uneven launch)", "value": value, "unit": "Gpixel-iter/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(ms) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/ff/f64 per viewport",
+            "data": "synthetic: seeded viewports and boundary centres",
+            "config": {"workload": "C4: 64 Mandelbrot viewports, side log-uniform 256..2048, span log-uniform "
+                                   "1e-12..1e-3, maxIter log-uniform 500..50000, one CUDA-graph launch",
+                       "pixels": total, "l2": "flushed between launches"},
+            "tiers": {"f32": tiers.count(0), "floatfloat": tiers.count(2), "f64": tiers.count(1)},
+            "pixel_iterations_per_step": per_launch,
+            "plain_f64": {"value": plain_value, "ms": plain_ms, "speedup_of_tiered": value / plain_value},
+            "escape_count_mismatch_vs_f64_batch": diff / total,
+            "gpu_launches": args.steps, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args):
+    """C5: 16 zoom sessions (720p..2160p), 1.02x zoom per frame toward seeded
+    boundary points, Poisson arrivals at 60 Hz per session, HBM-budget admission,
+    sample reuse from the previous frame; p50/p99 frame latency."""
+    import numpy as np
+    import torch
+
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import default_palette
+    from chaos_gb300.workloads import boundary_points
+
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(5)
+    res = [(1280, 720), (1920, 1080), (2560, 1440), (3840, 2160)]
+    n_sessions, seconds, hz = 16, 2.0, 60.0
+    targets = boundary_points(list(range(500, 500 + n_sessions)), max_iter=2000)
+    srv = cg.Server(48 << 30, default_palette())
+    sids, shapes = [], []
+    for k in range(n_sessions):
+        w, h = res[int(rng.integers(0, 4))]
+        d = cg.SessionDesc(width=w, height=h, max_iterations=2000, max_super_sampling=2.0, flags=1 | 4 | 8,
+                           fractal=cg.MANDELBROT, arith=cg.ARITH_FMA, center_x=-0.5, center_y=0.0, span=3.0,
+                           target_x=targets[k][0], target_y=targets[k][1], zoom_per_frame=1.02)
+        sids.append(srv.open(d))
+        shapes.append((w, h))
+    # warm-up: one frame per session (renderQuality) before the timed trace
+    for sid in sids:
+        srv.submit(sid)
+    srv.drain()
+    warm = len(srv.records())
+    it0 = sum(srv.read(sid)[1] for sid in sids)
+    sess, arr = [], []
+    for sid in sids:
+        t = 0.0
+        while True:
+            t += rng.exponential(1.0 / hz)
+            if t > seconds:
+                break
+            sess.append(sid)
+            arr.append(t)
+    order = np.argsort(arr)
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = srv.clock()
+    srv.run_trace(np.array(sess)[order], np.array(arr)[order])
+    t1 = srv.clock()
+    clk = clocks.stop()
+    recs = srv.records()[warm:]
+    lat = np.array([(r[4] - r[2]) * 1e3 for r in recs])
+    lat1080 = np.array([(r[4] - r[2]) * 1e3 for r in recs if shapes[r[0]] == (1920, 1080)])
+    iters = sum(srv.read(sid)[1] for sid in sids) - it0
+    value = iters / (t1 - t0) / 1e9
+    line = {"metric": "Gpixel-iter/s; p99 frame latency (serving)", "value": value, "unit": "Gpixel-iter/s",
+            "n_gpus": 1, "steps": len(recs), "warmup": warm, "ms_per_step": float(lat.mean()),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 per frame",
+            "data": "synthetic: seeded resolutions, boundary targets and Poisson arrivals",
+            "config": {"workload": f"C5: {n_sessions} sessions, 1280x720..3840x2160, zoom 1.02x/frame, "
+                                   f"Poisson {hz:g} Hz per session for {seconds:g} s, maxIter 2000, maxSS 2, "
+                                   "sample reuse + foveation", "resolutions": [f"{w}x{h}" for w, h in shapes],
+                       "hbm_budget_gib": 48, "hbm_used_gib": srv.usage()[0] / 2 ** 30},
+            "frames": len(recs), "trace_s": t1 - t0,
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                           "max": float(lat.max()),
+                           "p50_1080p": float(np.percentile(lat1080, 50)) if len(lat1080) else None,
+                           "p99_1080p": float(np.percentile(lat1080, 99)) if len(lat1080) else None},
+            "pixel_iterations": iters, "clocks": clk}
+    print(json.dumps(line), flush=True)
+    srv.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["c2", "c2-crop"], default="c2",
+    ap.add_argument("--workload", choices=["c2", "c2-crop", "c4", "c5"], default="c2",
                     help="c2-crop: the central 480x270 pixels of the same frame (for profiler captures)")
     args = ap.parse_args()
     if args.workload == "c2-crop":
@@ -400,6 +562,10 @@ def main():
         W, H = 480, 270
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c4":
+        run_batch(args)
+    elif args.workload == "c5":
+        run_serve(args)
     else:
         run_ours(args)
 

@@ -19,7 +19,7 @@ ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]
-FRACTALS = {"mandelbrot": 0, "julia": 1}
+FRACTALS = {"mandelbrot": 0, "julia": 1, "newton_wired": 2, "newton_generic": 3, "newton_iterations": 4}
 
 
 def nvcc():
@@ -55,18 +55,22 @@ def build(verbose=False, ptxas_info=False, force=False):
 
     jobs = []
     objs = []
-    for name in ("chaos_kernels", "chaos_api", "chaos_perturb", "chaos_noalloc"):
+    for name in ("chaos_kernels", "chaos_api", "chaos_perturb", "chaos_noalloc", "chaos_batch", "chaos_serve",
+                 "chaos_newton"):
         src = os.path.join(CSRC, name + ".cu")
         obj = os.path.join(BUILD, name + ".o")
         objs.append(obj)
+        # the Newton modules' thrust::complex code is rounded operation by operation
+        fmad = ["--fmad=false"] if name == "chaos_newton" else []
         if force or not _newer(obj, [src] + headers):
-            jobs.append([exe, *ARCH, *COMMON, *extra, "-Xcompiler", "-fPIC", "-c", src, "-o", obj])
+            jobs.append([exe, *ARCH, *COMMON, *extra, *fmad, "-Xcompiler", "-fPIC", "-c", src, "-o", obj])
     dropin = os.path.join(CSRC, "dropin_module.cu")
     for fractal, fid in FRACTALS.items():
         for sub, arith in (("cudaKernels", "chaos::ARITH_FMA"), ("cudaKernels_parity", "chaos::ARITH_PARITY")):
             out = os.path.join(HERE, sub, fractal + ".ptx")
             if force or not _newer(out, [dropin] + headers):
-                jobs.append([exe, *ARCH, *COMMON, *extra, "-cubin", f"-DCHAOS_DROPIN_FRACTAL={fid}",
+                fmad = ["--fmad=false"] if sub == "cudaKernels_parity" else []
+                jobs.append([exe, *ARCH, *COMMON, *extra, *fmad, "-cubin", f"-DCHAOS_DROPIN_FRACTAL={fid}",
                              f"-DCHAOS_DROPIN_ARITH={arith}", dropin, "-o", out])
     with ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
         outs = list(ex.map(_run, jobs))

@@ -41,6 +41,7 @@ SAMPLES_CENTER = 0
 SAMPLES_JITTER = 1
 TIER_F32 = 0
 TIER_F64 = 1
+TIER_FLOATFLOAT = 2
 TIER_PERTURB_F32 = 3
 TIER_PERTURB_F64 = 4
 
@@ -87,6 +88,36 @@ class FrameOut(C.Structure):
     ]
 
 
+class Viewport(C.Structure):
+    _fields_ = [
+        ("width", C.c_uint32), ("height", C.c_uint32), ("max_iterations", C.c_uint32),
+        ("samples_per_pixel", C.c_uint32), ("sample_mode", C.c_uint32), ("tier", C.c_uint32),
+        ("seed", C.c_uint64), ("center_x", C.c_double), ("center_y", C.c_double), ("pixel_size", C.c_double),
+        ("counts", C.c_void_p), ("smooth", C.c_void_p), ("rgba", C.c_void_p),
+    ]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("block_threads", C.c_uint32 * 3), ("escape_block", C.c_uint32 * 3)]
+
+
+TIER_AUTO = 255
+
+
+class SessionDesc(C.Structure):
+    _fields_ = [
+        ("width", C.c_uint32), ("height", C.c_uint32), ("max_iterations", C.c_uint32),
+        ("max_super_sampling", C.c_float), ("flags", C.c_uint32), ("fractal", C.c_uint32), ("arith", C.c_int32),
+        ("pad_", C.c_uint32), ("center_x", C.c_double), ("center_y", C.c_double), ("span", C.c_double),
+        ("target_x", C.c_double), ("target_y", C.c_double), ("zoom_per_frame", C.c_double),
+        ("julia_cx", C.c_double), ("julia_cy", C.c_double),
+    ]
+
+
+class FrameRecord(C.Structure):
+    _fields_ = [("session", C.c_uint32), ("frame", C.c_uint32), ("arrival_s", C.c_double), ("start_s", C.c_double),
+                ("done_s", C.c_double), ("precision", C.c_int32), ("pad_", C.c_int32)]
+
 _F4 = C.c_float * 4
 _D4 = C.c_double * 4
 _vp = C.c_void_p
@@ -128,6 +159,26 @@ SIGNATURES = {
     "chaos_render_frame": (_int, [C.POINTER(FrameDesc), C.POINTER(FrameOut), _vp]),
     "chaos_render_frame_host": (_int, [C.POINTER(FrameDesc), _vp, _u32, _u32, _vp, C.POINTER(C.c_ulonglong), _vp]),
     "chaos_measure_fma_peak": (_int, [_u32, C.POINTER(C.c_double)]),
+    "chaos_batch_auto_tier": (_u32, [C.c_double, C.c_double, C.c_double]),
+    "chaos_batch_create": (_int, [C.POINTER(Viewport), _u32, _vp, _u32, _u32, C.POINTER(BatchConfig),
+                                  C.POINTER(_vp)]),
+    "chaos_batch_launch": (_int, [_vp, _vp]),
+    "chaos_batch_tiers": (_int, [_vp, C.POINTER(_u32), _u32]),
+    "chaos_batch_total": (_int, [_vp, C.POINTER(_vp)]),
+    "chaos_batch_read_total": (_int, [_vp, C.POINTER(C.c_ulonglong)]),
+    "chaos_batch_destroy": (_int, [_vp]),
+    "chaos_server_create": (_int, [C.c_size_t, _vp, _u32, C.POINTER(_vp)]),
+    "chaos_server_session_bytes": (_int, [C.POINTER(SessionDesc), C.POINTER(C.c_size_t)]),
+    "chaos_server_open": (_int, [_vp, C.POINTER(SessionDesc), C.POINTER(_u32)]),
+    "chaos_server_close": (_int, [_vp, _u32]),
+    "chaos_server_submit": (_int, [_vp, _u32, C.c_double]),
+    "chaos_server_drain": (_int, [_vp]),
+    "chaos_server_run_trace": (_int, [_vp, _vp, _vp, _u32]),
+    "chaos_server_records": (_int, [_vp, _vp, _u32, C.POINTER(_u32)]),
+    "chaos_server_read": (_int, [_vp, _u32, _vp, C.POINTER(C.c_ulonglong)]),
+    "chaos_server_usage": (_int, [_vp, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "chaos_server_clock": (C.c_double, [_vp]),
+    "chaos_server_destroy": (_int, [_vp]),
     "chaos_render_frame_host_noalloc": (_int, [C.POINTER(FrameDesc), _vp, _u32, _u32, _vp,
                                                C.POINTER(C.c_ulonglong), _vp]),
     "chaos_orbit_create": (_int, [C.c_char_p, C.c_char_p, _u32, _u32, C.POINTER(_vp)]),

@@ -1,7 +1,8 @@
 """Thin object layer over the C ABI (names follow the reference's Java classes)."""
 import ctypes as C
 
-from ._native import (ARITH_FMA, FrameDesc, FrameOut, RenderingModel, _D4, _F4, check, lib)
+from ._native import (ARITH_FMA, BatchConfig, FrameDesc, FrameOut, FrameRecord, RenderingModel, SessionDesc, Viewport,
+                      _D4, _F4, check, lib)
 
 
 def version():
@@ -217,3 +218,126 @@ def to_hex_fixed(value, bits):
     digits = (bits + 3) // 4
     f = int(frac * (1 << (4 * digits)))
     return ("-" if neg else "") + f"{ip}." + format(f, f"0{digits}x")
+
+
+class Batch:
+    """Many viewports in one CUDA-graph launch (chaos_batch_*)."""
+
+    def __init__(self, viewports, palette_ptr=None, palette_len=0, interior_rgba=0xFF000000, config=None):
+        arr = (Viewport * len(viewports))(*viewports)
+        h = C.c_void_p()
+        cfg = C.byref(config) if config is not None else None
+        check(lib().chaos_batch_create(arr, len(viewports), palette_ptr, palette_len, interior_rgba, cfg,
+                                       C.byref(h)))
+        self.handle = h
+        self.n = len(viewports)
+
+    def launch(self, stream=None):
+        check(lib().chaos_batch_launch(self.handle, _stream(stream)))
+
+    def tiers(self):
+        t = (C.c_uint32 * self.n)()
+        check(lib().chaos_batch_tiers(self.handle, t, self.n))
+        return list(t)
+
+    def total_ptr(self):
+        p = C.c_void_p()
+        check(lib().chaos_batch_total(self.handle, C.byref(p)))
+        return p.value
+
+    def read_total(self):
+        t = C.c_ulonglong()
+        check(lib().chaos_batch_read_total(self.handle, C.byref(t)))
+        return t.value
+
+    def close(self):
+        if self.handle:
+            lib().chaos_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def auto_tier(center_x, center_y, pixel_size):
+    return lib().chaos_batch_auto_tier(center_x, center_y, pixel_size)
+
+
+class Server:
+    """Concurrent zoom sessions admitted by an HBM budget (chaos_server_*)."""
+
+    def __init__(self, hbm_budget_bytes, palette):
+        import numpy as np
+        pal = np.ascontiguousarray(palette, dtype=np.uint32)
+        h = C.c_void_p()
+        check(lib().chaos_server_create(hbm_budget_bytes, pal.ctypes.data_as(C.c_void_p), len(pal), C.byref(h)))
+        self.handle = h
+        self.shapes = {}
+
+    def open(self, desc: SessionDesc):
+        sid = C.c_uint32()
+        check(lib().chaos_server_open(self.handle, C.byref(desc), C.byref(sid)))
+        self.shapes[sid.value] = (desc.height, desc.width)
+        return sid.value
+
+    @staticmethod
+    def session_bytes(desc: SessionDesc):
+        b = C.c_size_t()
+        check(lib().chaos_server_session_bytes(C.byref(desc), C.byref(b)))
+        return b.value
+
+    def close_session(self, sid):
+        check(lib().chaos_server_close(self.handle, sid))
+        self.shapes.pop(sid, None)
+
+    def submit(self, sid, arrival_s=None):
+        if arrival_s is None:
+            arrival_s = self.clock()
+        check(lib().chaos_server_submit(self.handle, sid, arrival_s))
+
+    def drain(self):
+        check(lib().chaos_server_drain(self.handle))
+
+    def run_trace(self, sessions, arrivals):
+        import numpy as np
+        s = np.ascontiguousarray(sessions, dtype=np.uint32)
+        a = np.ascontiguousarray(arrivals, dtype=np.float64)
+        check(lib().chaos_server_run_trace(self.handle, s.ctypes.data_as(C.c_void_p), a.ctypes.data_as(C.c_void_p),
+                                           len(s)))
+
+    def records(self):
+        n = C.c_uint32()
+        check(lib().chaos_server_records(self.handle, None, 0, C.byref(n)))
+        buf = (FrameRecord * max(1, n.value))()
+        check(lib().chaos_server_records(self.handle, buf, n.value, C.byref(n)))
+        return [(r.session, r.frame, r.arrival_s, r.start_s, r.done_s, r.precision) for r in buf[:n.value]]
+
+    def read(self, sid):
+        import numpy as np
+        h, w = self.shapes[sid]
+        out = np.zeros((h, w), dtype=np.uint32)
+        it = C.c_ulonglong()
+        check(lib().chaos_server_read(self.handle, sid, out.ctypes.data_as(C.c_void_p), C.byref(it)))
+        return out, it.value
+
+    def usage(self):
+        u, b = C.c_size_t(), C.c_size_t()
+        check(lib().chaos_server_usage(self.handle, C.byref(u), C.byref(b)))
+        return u.value, b.value
+
+    def clock(self):
+        return lib().chaos_server_clock(self.handle)
+
+    def close(self):
+        if self.handle:
+            lib().chaos_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

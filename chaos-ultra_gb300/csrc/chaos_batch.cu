@@ -1,0 +1,481 @@
+// chaos_batch.cu -- many viewports of uneven size and iteration limit in one
+// CUDA-graph launch.
+//
+// Each viewport is rendered at a precision tier chosen from its pixel size
+// (binary32, float-float or binary64).  Per tier one persistent kernel serves
+// all of that tier's viewports from a single job space (job = one pixel with
+// its samples; a lane maps its job to a viewport by binary search over the
+// viewports' job offsets held in shared memory).  The three kernels sit in one
+// fork-join CUDA graph, so the tail of one tier's kernel overlaps the next.
+// The escape loop is the frame path's: blocks of K untested steps, and a lane
+// whose block overshot an escape halves its search window inside the warp's
+// regular blocks.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/chaos_gb300.h"
+#include "chaos_frame.cuh"
+
+namespace chaos {
+
+int api_fail(int code, const char *fmt, ...);  // chaos_api.cu
+
+struct BatchViewport {
+    uint32_t w, h, spp, mode, max_iter;
+    uint32_t job_base;  // first job of this viewport in its tier's job space
+    uint64_t seed;
+    double center_x, center_y, ps;
+    uint32_t *counts;
+    float *smooth;
+    uint32_t *rgba;
+};
+
+struct BatchArgs {
+    const BatchViewport *vps;
+    uint32_t n_vp, n_jobs;
+    uint32_t *counter;
+    unsigned long long *total;
+    const uint32_t *palette;
+    uint32_t palette_len;
+    uint32_t interior_rgba;
+};
+
+// Number policies: binary32, binary64 (fused multiply-adds) and float-float.
+template <class N> struct Num;
+template <> struct Num<float> {
+    using T = float;
+    static __device__ __forceinline__ T from(double d) { return (float)d; }
+    static __device__ __forceinline__ T zero() { return 0.f; }
+    static __device__ __forceinline__ void step(T &x, T &y, T cx, T cy) { chaos::step<float, ARITH_FMA>(x, y, cx, cy); }
+    static __device__ __forceinline__ float r2(T x, T y) { return radius2<float, ARITH_FMA>(x, y); }
+    static __device__ __forceinline__ bool blockable(T cx, T cy) { return blockable_c(cx, cy); }
+};
+template <> struct Num<double> {
+    using T = double;
+    static __device__ __forceinline__ T from(double d) { return d; }
+    static __device__ __forceinline__ T zero() { return 0.0; }
+    static __device__ __forceinline__ void step(T &x, T &y, T cx, T cy) { chaos::step<double, ARITH_FMA>(x, y, cx, cy); }
+    static __device__ __forceinline__ double r2(T x, T y) { return radius2<double, ARITH_FMA>(x, y); }
+    static __device__ __forceinline__ bool blockable(T cx, T cy) { return blockable_c(cx, cy); }
+};
+template <> struct Num<FF> {
+    using T = FF;
+    static __device__ __forceinline__ T from(double d) { return ff_from_double(d); }
+    static __device__ __forceinline__ T zero() { return FF{0.f, 0.f}; }
+    static __device__ __forceinline__ void step(T &x, T &y, T cx, T cy) { ff_step(x, y, cx, cy); }
+    static __device__ __forceinline__ float r2(T x, T y) { return ff_radius2(x, y); }
+    static __device__ __forceinline__ bool blockable(T cx, T cy) { return blockable_c(cx.hi, cy.hi); }
+};
+
+constexpr uint32_t BATCH_MAX_VIEWPORTS = 1024;
+
+template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchArgs a)
+{
+    using P = Num<N>;
+    using T = typename P::T;
+    constexpr uint32_t FULLM = 0xffffffffu;
+    __shared__ uint32_t s_pal[4096];
+    __shared__ uint32_t s_base[BATCH_MAX_VIEWPORTS + 1];
+    const uint32_t *pal = a.palette;
+    if (a.palette && a.palette_len <= 4096u) {
+        for (uint32_t k = threadIdx.x; k < a.palette_len; k += blockDim.x) s_pal[k] = a.palette[k];
+        pal = s_pal;
+    }
+    for (uint32_t k = threadIdx.x; k < a.n_vp; k += blockDim.x) s_base[k] = a.vps[k].job_base;
+    if (threadIdx.x == 0) s_base[a.n_vp] = a.n_jobs;
+    __syncthreads();
+
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    uint32_t job = 0xffffffffu, vp = 0, pix = 0, s = 0, i = 0, window = 0, max_iter = 0, spp = 1;
+    T x = P::zero(), y = P::zero(), cx = P::zero(), cy = P::zero();
+    bool blk = false, need = true, begin = false;
+    float acc_v = 0.f, acc[4] = {0.f, 0.f, 0.f, 0.f};
+    unsigned long long iters = 0;
+
+    for (;;) {
+        uint32_t need_mask = __ballot_sync(FULLM, need);
+        if (need_mask) {
+            uint32_t leader = __ffs(need_mask) - 1u;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(a.counter, (uint32_t)__popc(need_mask));
+            base = __shfl_sync(FULLM, base, leader);
+            if (need) {
+                job = base + (uint32_t)__popc(need_mask & lt_mask);
+                need = false;
+                if (job < a.n_jobs) {
+                    uint32_t lo = 0, hi = a.n_vp;  // last viewport with job_base <= job
+                    while (hi - lo > 1) {
+                        uint32_t mid = (lo + hi) >> 1;
+                        if (s_base[mid] <= job)
+                            lo = mid;
+                        else
+                            hi = mid;
+                    }
+                    vp = lo;
+                    pix = job - s_base[lo];
+                    max_iter = a.vps[lo].max_iter;
+                    spp = a.vps[lo].spp;
+                    begin = true;
+                    s = 0;
+                    acc_v = 0.f;
+                    acc[0] = acc[1] = acc[2] = acc[3] = 0.f;
+                }
+            }
+        }
+        const bool active = job < a.n_jobs;
+        if (!__any_sync(FULLM, active)) break;
+
+        bool done = false;
+        float r2 = 0.f;
+        uint32_t lim = 0;
+        if (active) {
+            if (begin) {
+                begin = false;
+                const BatchViewport &v = a.vps[vp];
+                uint32_t px = pix % v.w, py = pix / v.w;
+                double ox = 0.5, oy = 0.5;
+                if (v.mode == SAMPLES_JITTER) {
+                    ox = unit_interval_t<double>(sample_hash(v.seed, pix, s, 0));
+                    oy = unit_interval_t<double>(sample_hash(v.seed, pix, s, 1));
+                }
+                double dxp = __dsub_rn(__dadd_rn((double)px, ox), 0.5 * v.w);
+                double dyp = __dsub_rn(__dadd_rn((double)py, oy), 0.5 * v.h);
+                cx = P::from(__fma_rn(dxp, v.ps, v.center_x));
+                cy = P::from(__fma_rn(-dyp, v.ps, v.center_y));
+                x = P::zero();
+                y = P::zero();
+                blk = P::blockable(cx, cy);
+                i = 0;
+                window = 0;
+                if (max_iter == 0) done = true;
+            }
+            if (!done) {
+                if (!blk) {
+                    lim = 1;
+                } else if (window) {
+                    lim = window > 1u ? window >> 1 : 1u;
+                } else {
+                    uint32_t rest = max_iter - i;
+                    lim = rest >= (uint32_t)K ? (uint32_t)K : 1u << (31 - __clz(rest));
+                }
+            }
+        }
+        const bool stepping = active && !done;
+        const bool partial = stepping && lim < (uint32_t)K;
+        const bool any_partial = __any_sync(FULLM, partial);
+        if (stepping) {
+            const T sx = x, sy = y;
+            if (any_partial) {
+                T kx = x, ky = y;
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    P::step(x, y, cx, cy);
+                    if (((k + 1) & k) == 0 && k + 1 < K && (uint32_t)(k + 1) == lim) {
+                        kx = x;
+                        ky = y;
+                    }
+                }
+                if (partial) {
+                    x = kx;
+                    y = ky;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < K; k++) P::step(x, y, cx, cy);
+            }
+            auto rr = P::r2(x, y);
+            r2 = (float)rr;
+            if (rr < 4) {
+                i += lim;
+                window = window > 1u ? window - lim : 0u;
+                if (i == max_iter) done = true;
+            } else if (lim == 1u) {
+                i += 1u;
+                done = true;
+            } else {
+                x = sx;
+                y = sy;
+                window = lim;
+            }
+        }
+        if (done) {
+            const BatchViewport &v = a.vps[vp];
+            const bool escaped = i < max_iter;
+            const float nu = frame_smooth(i, r2, max_iter);
+            const size_t sidx = (size_t)pix * spp + s;
+            if (v.counts) v.counts[sidx] = i;
+            if (v.smooth) v.smooth[sidx] = nu;
+            iters += i;
+            acc_v = __fadd_rn(acc_v, escaped ? nu : 0.f);
+            if (v.rgba) {
+                float ch[4];
+                if (escaped) {
+                    frame_palette_lerp(pal, a.palette_len, nu, ch);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) ch[k] = (float)((a.interior_rgba >> (8 * k)) & 255u);
+                }
+#pragma unroll
+                for (int k = 0; k < 4; k++) acc[k] = __fadd_rn(acc[k], ch[k]);
+            }
+            ++s;
+            if (s == spp) {
+                if (v.rgba) v.rgba[pix] = frame_pack_rgba(acc, spp);
+                need = true;
+            } else {
+                begin = true;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) iters += __shfl_down_sync(FULLM, iters, o);
+    if (lane == 0 && iters && a.total) atomicAdd(a.total, iters);
+}
+
+template <class N, int K> static cudaError_t launch_batch_k(const BatchArgs &a, int threads, int sms, cudaStream_t s)
+{
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch<N, K>, threads, 0) != cudaSuccess || occ < 1)
+        occ = 1;
+    unsigned long long warps = ((unsigned long long)a.n_jobs + 31ull) / 32ull;
+    unsigned long long per_block = (unsigned long long)threads / 32ull;
+    unsigned long long blocks = (warps + per_block - 1) / per_block;
+    unsigned long long cap = (unsigned long long)occ * (unsigned long long)sms;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    k_batch<N, K><<<(unsigned)blocks, threads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <class N> static cudaError_t launch_batch(const BatchArgs &a, int threads, int k, int sms, cudaStream_t s)
+{
+    if (k == 8) return launch_batch_k<N, 8>(a, threads, sms, s);
+    if (k == 32) return launch_batch_k<N, 32>(a, threads, sms, s);
+    return launch_batch_k<N, 16>(a, threads, sms, s);
+}
+
+}  // namespace chaos
+
+using namespace chaos;
+
+namespace {
+constexpr int kTiers = 3;  // 0 binary32, 1 float-float, 2 binary64
+int tier_slot(uint32_t tier) { return tier == CHAOS_TIER_F32 ? 0 : tier == CHAOS_TIER_FLOATFLOAT ? 1 : 2; }
+}  // namespace
+
+struct chaos_batch {
+    int device = -1;
+    std::vector<uint32_t> tiers;  // chosen tier per viewport
+    BatchViewport *d_vps[kTiers] = {nullptr, nullptr, nullptr};
+    uint32_t n_vp[kTiers] = {0, 0, 0}, n_jobs[kTiers] = {0, 0, 0};
+    uint32_t *d_counters = nullptr;
+    unsigned long long *d_total = nullptr;
+    const uint32_t *palette = nullptr;
+    uint32_t palette_len = 0, interior = 0;
+    int threads[kTiers] = {256, 256, 256}, k[kTiers] = {16, 16, 16};
+    int sms = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long pixel_iterations_hint = 0;
+};
+
+uint32_t chaos_batch_auto_tier(double center_x, double center_y, double pixel_size)
+{
+    double m = std::max(std::max(std::fabs(center_x), std::fabs(center_y)), 1.0 / 256);
+    if (pixel_size >= m * 0x1p-18) return CHAOS_TIER_F32;
+    if (pixel_size >= m * 0x1p-42) return CHAOS_TIER_FLOATFLOAT;
+    return CHAOS_TIER_F64;
+}
+
+static void batch_free(chaos_batch *b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (int t = 0; t < kTiers; t++)
+        if (b->d_vps[t]) cudaFree(b->d_vps[t]);
+    if (b->d_counters) cudaFree(b->d_counters);
+    if (b->d_total) cudaFree(b->d_total);
+    delete b;
+}
+
+static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s1, cudaStream_t s2, cudaEvent_t fork,
+                                 cudaEvent_t j1, cudaEvent_t j2)
+{
+    cudaError_t e = cudaMemsetAsync(b->d_counters, 0, kTiers * sizeof(uint32_t), s0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_total, 0, sizeof(unsigned long long), s0);
+    if (e == cudaSuccess) e = cudaEventRecord(fork, s0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s1, fork, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, fork, 0);
+    cudaStream_t st[kTiers] = {s0, s1, s2};
+    // binary64 first: its kernels are the longest, the cheaper tiers fill in behind
+    const int order[kTiers] = {2, 1, 0};
+    for (int oi = 0; oi < kTiers && e == cudaSuccess; oi++) {
+        int t = order[oi];
+        if (!b->n_jobs[t]) continue;
+        BatchArgs a{};
+        a.vps = b->d_vps[t];
+        a.n_vp = b->n_vp[t];
+        a.n_jobs = b->n_jobs[t];
+        a.counter = b->d_counters + t;
+        a.total = b->d_total;
+        a.palette = b->palette;
+        a.palette_len = b->palette_len;
+        a.interior_rgba = b->interior;
+        cudaStream_t s = st[oi];
+        if (t == 0) e = launch_batch<float>(a, b->threads[t], b->k[t], b->sms, s);
+        if (t == 1) e = launch_batch<FF>(a, b->threads[t], b->k[t], b->sms, s);
+        if (t == 2) e = launch_batch<double>(a, b->threads[t], b->k[t], b->sms, s);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(j1, s1);
+    if (e == cudaSuccess) e = cudaEventRecord(j2, s2);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s0, j1, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s0, j2, 0);
+    return e;
+}
+
+int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *palette, uint32_t palette_len,
+                       uint32_t interior_rgba, const chaos_batch_config *cfg, chaos_batch **out)
+{
+    if (!vps || !out || n == 0) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "viewports required");
+    if (n > BATCH_MAX_VIEWPORTS) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "at most %u viewports", BATCH_MAX_VIEWPORTS);
+    std::vector<BatchViewport> per[kTiers];
+    std::vector<uint32_t> tiers(n);
+    uint64_t jobs[kTiers] = {0, 0, 0};
+    bool any_rgba = false;
+    for (uint32_t k = 0; k < n; k++) {
+        const chaos_viewport &v = vps[k];
+        if (v.width == 0 || v.height == 0 || (uint64_t)v.width * v.height > (1ull << 31))
+            return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "viewport %u: bad size", k);
+        if (v.samples_per_pixel < 1 || v.samples_per_pixel > 64)
+            return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "viewport %u: samples_per_pixel must be 1..64", k);
+        if (v.sample_mode > CHAOS_SAMPLES_JITTER ||
+            (v.sample_mode == CHAOS_SAMPLES_CENTER && v.samples_per_pixel != 1))
+            return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "viewport %u: bad sample mode", k);
+        if (!std::isfinite(v.center_x) || !std::isfinite(v.center_y) || !(v.pixel_size > 0) ||
+            !std::isfinite(v.pixel_size))
+            return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "viewport %u: centre/pixel size", k);
+        uint32_t tier = v.tier == CHAOS_TIER_AUTO ? chaos_batch_auto_tier(v.center_x, v.center_y, v.pixel_size) : v.tier;
+        if (tier != CHAOS_TIER_F32 && tier != CHAOS_TIER_FLOATFLOAT && tier != CHAOS_TIER_F64)
+            return api_fail(CHAOS_ERR_UNSUPPORTED, "viewport %u: tier %u not batchable", k, tier);
+        tiers[k] = tier;
+        int t = tier_slot(tier);
+        BatchViewport bv{};
+        bv.w = v.width;
+        bv.h = v.height;
+        bv.spp = v.samples_per_pixel;
+        bv.mode = v.sample_mode;
+        bv.max_iter = v.max_iterations;
+        bv.job_base = (uint32_t)jobs[t];
+        bv.seed = v.seed;
+        bv.center_x = v.center_x;
+        bv.center_y = v.center_y;
+        bv.ps = v.pixel_size;
+        bv.counts = v.counts;
+        bv.smooth = v.smooth;
+        bv.rgba = v.rgba;
+        any_rgba |= v.rgba != nullptr;
+        jobs[t] += (uint64_t)v.width * v.height;
+        if (jobs[t] > (1ull << 31)) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "batch too large");
+        per[t].push_back(bv);
+    }
+    if (any_rgba && (!palette || palette_len == 0 || palette_len > 4096))
+        return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "rgba outputs need a device palette of 1..4096 entries");
+
+    chaos_batch *b = new (std::nothrow) chaos_batch();
+    if (!b) return api_fail(CHAOS_ERR_OUT_OF_MEMORY, "out of host memory");
+    cudaGetDevice(&b->device);
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
+    b->tiers = tiers;
+    b->palette = palette;
+    b->palette_len = palette_len;
+    b->interior = interior_rgba;
+    if (cfg) {
+        for (int t = 0; t < kTiers; t++) {
+            if (cfg->block_threads[t]) b->threads[t] = (int)cfg->block_threads[t];
+            if (cfg->escape_block[t]) b->k[t] = (int)cfg->escape_block[t];
+            if (b->threads[t] % 32 || b->threads[t] < 32 || b->threads[t] > 512 ||
+                (b->k[t] != 8 && b->k[t] != 16 && b->k[t] != 32)) {
+                batch_free(b);
+                return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "tier %d: threads 32..512 (multiple of 32), block 8/16/32",
+                                t);
+            }
+        }
+    }
+    cudaError_t e = cudaMalloc(&b->d_counters, kTiers * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_total, sizeof(unsigned long long));
+    for (int t = 0; t < kTiers && e == cudaSuccess; t++) {
+        b->n_vp[t] = (uint32_t)per[t].size();
+        b->n_jobs[t] = (uint32_t)jobs[t];
+        if (per[t].empty()) continue;
+        e = cudaMalloc(&b->d_vps[t], per[t].size() * sizeof(BatchViewport));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(b->d_vps[t], per[t].data(), per[t].size() * sizeof(BatchViewport), cudaMemcpyHostToDevice);
+    }
+    // capture the fork-join launch into a graph
+    cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr;
+    cudaEvent_t fork = nullptr, j1 = nullptr, j2 = nullptr;
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j1, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j2, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t ee = batch_enqueue(b, s0, s1, s2, fork, j1, j2);
+        e = cudaStreamEndCapture(s0, &b->graph);
+        if (ee != cudaSuccess) e = ee;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    if (fork) cudaEventDestroy(fork);
+    if (j1) cudaEventDestroy(j1);
+    if (j2) cudaEventDestroy(j2);
+    if (s0) cudaStreamDestroy(s0);
+    if (s1) cudaStreamDestroy(s1);
+    if (s2) cudaStreamDestroy(s2);
+    if (e != cudaSuccess) {
+        batch_free(b);
+        return api_fail(CHAOS_ERR_CUDA, "batch set-up: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return CHAOS_OK;
+}
+
+int chaos_batch_launch(chaos_batch *b, void *stream)
+{
+    if (!b) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL batch");
+    cudaError_t e = cudaGraphLaunch(b->exec, (cudaStream_t)stream);
+    if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "cudaGraphLaunch: %s", cudaGetErrorString(e));
+    return CHAOS_OK;
+}
+
+int chaos_batch_tiers(const chaos_batch *b, uint32_t *tiers, uint32_t n)
+{
+    if (!b || !tiers || n < b->tiers.size()) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "bad argument");
+    std::copy(b->tiers.begin(), b->tiers.end(), tiers);
+    return CHAOS_OK;
+}
+
+int chaos_batch_total(const chaos_batch *b, unsigned long long **device_total)
+{
+    if (!b || !device_total) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "bad argument");
+    *device_total = b->d_total;
+    return CHAOS_OK;
+}
+
+int chaos_batch_read_total(const chaos_batch *b, unsigned long long *total)
+{
+    if (!b || !total) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "bad argument");
+    cudaError_t e = cudaMemcpy(total, b->d_total, sizeof *total, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "read total: %s", cudaGetErrorString(e));
+    return CHAOS_OK;
+}
+
+int chaos_batch_destroy(chaos_batch *b)
+{
+    if (b) batch_free(b);
+    return CHAOS_OK;
+}

@@ -30,7 +30,28 @@ struct PixelInfo {
 static_assert(sizeof(PixelInfo) == 16, "pixel_info_t is 16 bytes");
 
 enum Arith { ARITH_PARITY = 0, ARITH_FMA = 1 };
-enum FractalKind { FRACTAL_MANDELBROT = 0, FRACTAL_JULIA = 1 };
+enum FractalKind {
+    FRACTAL_MANDELBROT = 0,
+    FRACTAL_JULIA = 1,
+    FRACTAL_NEWTON_WIRED = 2,      // src/main/cuda/fractals/newton_wired.cu
+    FRACTAL_NEWTON_GENERIC = 3,    // newton_generic.cu
+    FRACTAL_NEWTON_ITERATIONS = 4  // newton_iterations.cu
+};
+
+// The Newton modules' __constant__ symbols (newton_generic.cu:7-8,
+// newton_iterations.cu:7-9): roots as (re, im) pairs, polynomial coefficients
+// c0..c3 (f = c0 + c1 z + c2 z^2 + c3 z^3), and the palette stride of the
+// iteration colouring.
+struct NewtonParams {
+    double roots[6];
+    double coefficients[4];
+    int color_magnifier;
+    int pad;
+};
+
+// Newton-method value of a start point (chaos_newton.cuh; only the
+// translation units that render Newton fractals include its definition).
+template <class R, int F> __device__ uint32_t newton_compute(uint32_t max_iterations, R zx, R zy, const NewtonParams &p);
 
 // kernel flag bits, gen.cu:157-161 (bit 1 is the Java-side "visualise" flag)
 constexpr uint32_t FLAG_ADAPTIVE_SS = 1u << 0;
@@ -174,7 +195,17 @@ template <class R> struct SampleGeometry {
     R psx, psy;  // pixel size, image.size() / gridSize (gen.cu:97)
     uint32_t max_iter;
     R jcx, jcy;
+    NewtonParams newton;  // Newton modules only
 };
+
+// computeFractal of the module F at plane point (cx, cy).
+template <class R, int A, int F> __device__ __forceinline__ uint32_t compute_fractal_g(const SampleGeometry<R> &g, R cx, R cy)
+{
+    if constexpr (F >= FRACTAL_NEWTON_WIRED)
+        return newton_compute<R, F>(g.max_iter, cx, cy, g.newton);
+    else
+        return compute_fractal<R, A, F>(g.max_iter, cx, cy, g.jcx, g.jcy);
+}
 
 template <class R>
 __device__ __forceinline__ SampleGeometry<R> make_geometry(const Rect<R> &r, UInt2 size, uint32_t max_iter, double jcx,
@@ -229,10 +260,11 @@ __device__ __forceinline__ float dispersion(const float *data, uint32_t data_len
 // sampleTheFractal for the lanes of `mask`, which call it together with the
 // same sample_count_f.  Lanes with valid == false (pixels outside the image)
 // take part in the votes as "yes" and compute nothing, which is how the
-// reference's exited lanes drop out of __activemask().
+// reference's exited lanes drop out of __activemask().  `iters` accumulates the
+// pixel-iterations of the samples taken (an interior sample counts max_iter).
 template <class R, int A, int F>
 __device__ uint32_t sample_the_fractal(const SampleGeometry<R> &g, uint32_t px, uint32_t py, float &sample_count_f,
-                                       bool adaptive, bool valid, uint32_t mask)
+                                       bool adaptive, bool valid, uint32_t mask, unsigned long long &iters)
 {
     if (sample_count_f < 1.f) {  // gen.cu:87-90
         sample_count_f = 0.f;
@@ -247,7 +279,9 @@ __device__ uint32_t sample_the_fractal(const SampleGeometry<R> &g, uint32_t px, 
         if (valid) {
             R cx, cy;
             sample_point(g, px, py, i, sample_count_f, cx, cy);
-            e = compute_fractal<R, A, F>(g.max_iter, cx, cy, g.jcx, g.jcy);
+            e = compute_fractal_g<R, A, F>(g, cx, cy);
+            // pixel-iterations (escape-time modules; the Newton modules return a root index)
+            if (F < FRACTAL_NEWTON_WIRED) iters += (F == FRACTAL_MANDELBROT && e == 0u) ? g.max_iter : e;
         }
         sum += e;
         if (i < ADAPTIVE_THRESHOLD) samples[i] = (float)e;
@@ -335,12 +369,14 @@ __device__ __forceinline__ PixelInfo make_pixel(float value, float weight)
 // fractalRenderMain for one lane of an 8x4 warp tile (gen.cu:168-181).
 template <class R, int A, int F>
 __device__ __forceinline__ void render_main_tile(const SampleGeometry<R> &g, void *out, long pitch, UInt2 size,
-                                                 uint32_t x0, uint32_t y0, uint32_t lane, float max_ss, uint32_t flags)
+                                                 uint32_t x0, uint32_t y0, uint32_t lane, float max_ss, uint32_t flags,
+                                                 unsigned long long &iters)
 {
     UInt2 p = tile_pixel(x0, y0, lane);
     bool valid = p.x < size.x && p.y < size.y;
     float sc = max_ss;
-    uint32_t result = sample_the_fractal<R, A, F>(g, p.x, p.y, sc, (flags & FLAG_ADAPTIVE_SS) != 0, valid, 0xffffffffu);
+    uint32_t result =
+        sample_the_fractal<R, A, F>(g, p.x, p.y, sc, (flags & FLAG_ADAPTIVE_SS) != 0, valid, 0xffffffffu, iters);
     if (valid) store_pixel(pixel_ptr(out, pitch, p.x, p.y), make_pixel((float)result, sc));
 }
 
@@ -416,7 +452,8 @@ template <class R, int A, int F>
 __device__ __forceinline__ void render_advanced_tile(const SampleGeometry<R> &g, const Rect<R> &image,
                                                      const Rect<R> &image_reused, void *out, long pitch, UInt2 size,
                                                      const void *in, long in_pitch, UInt2 focus, uint32_t x0,
-                                                     uint32_t y0, uint32_t lane, float max_ss, uint32_t flags)
+                                                     uint32_t y0, uint32_t lane, float max_ss, uint32_t flags,
+                                                     unsigned long long &iters)
 {
     UInt2 p = tile_pixel(x0, y0, lane);
     bool valid = p.x < size.x && p.y < size.y;
@@ -450,7 +487,7 @@ __device__ __forceinline__ void render_advanced_tile(const SampleGeometry<R> &g,
     }
     if (group_a) {
         float sc = advised;
-        float samples = (float)sample_the_fractal<R, A, F>(g, p.x, p.y, sc, adaptive, true, mask_a);
+        float samples = (float)sample_the_fractal<R, A, F>(g, p.x, p.y, sc, adaptive, true, mask_a, iters);
         float rw = __fmul_rn(reused_w, 0.75f);
         res.weight_of_new_samples = sc;
         res.weight = __fadd_rn(rw, sc);
@@ -458,7 +495,7 @@ __device__ __forceinline__ void render_advanced_tile(const SampleGeometry<R> &g,
     }
     if (group_b) {
         float sc = advised < 1.f ? 1.f : advised;
-        res.value = (float)sample_the_fractal<R, A, F>(g, p.x, p.y, sc, adaptive, true, mask_b);
+        res.value = (float)sample_the_fractal<R, A, F>(g, p.x, p.y, sc, adaptive, true, mask_b, iters);
         res.weight = sc;
     }
     if (valid) store_pixel(pixel_ptr(out, pitch, p.x, p.y), res);
@@ -489,8 +526,30 @@ __device__ __forceinline__ uint32_t palette_index(float value, uint32_t palette_
     return palette_len - (vi % palette_len) - 1u;
 }
 
+// Colouring modes of the modules' colorize().
+enum ColorMode {
+    COLOR_PALETTE = 0,     // mandelbrot.cu:27-35, julia.cu:19-27
+    COLOR_ROOTS = 1,       // newton_wired.cu:67-80, newton_generic.cu:75-88: red/green/blue per root, black
+    COLOR_MAGNIFIED = 2    // newton_iterations.cu:70-78: palette stride colorMagnifier
+};
+
+__device__ __forceinline__ uint32_t colorize_value(float value, const uint32_t *palette, uint32_t palette_len,
+                                                   int mode, int magnifier)
+{
+    if (mode == COLOR_ROOTS) {
+        uint32_t r = (uint32_t)roundf(value);
+        return r == 1u ? 0xff0000ffu : r == 2u ? 0xff00ff00u : r == 3u ? 0xffff0000u : 0xff000000u;
+    }
+    if (mode == COLOR_MAGNIFIED) {
+        uint32_t vi = (uint32_t)roundf(value);
+        return palette[palette_len - (vi * (uint32_t)magnifier % palette_len) - 1u];
+    }
+    return palette[palette_index(value, palette_len)];
+}
+
 __device__ __forceinline__ uint32_t compose_pixel(const PixelInfo &p, const uint32_t *palette, uint32_t palette_len,
-                                                  float max_ss, bool visualize)
+                                                  float max_ss, bool visualize, int mode = COLOR_PALETTE,
+                                                  int magnifier = 1)
 {
     if (visualize) {
         uint32_t full = (uint32_t)fmax(1.0, (double)max_ss);
@@ -498,7 +557,7 @@ __device__ __forceinline__ uint32_t compose_pixel(const PixelInfo &p, const uint
         if (p.is_reused) c = colorize_sample_count((uint32_t)p.weight_of_new_samples, full);
         return c;
     }
-    return palette[palette_index(p.value, palette_len)];
+    return colorize_value(p.value, palette, palette_len, mode, magnifier);
 }
 
 }  // namespace chaos

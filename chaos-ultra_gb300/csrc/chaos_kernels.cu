@@ -12,48 +12,11 @@
 #include <cstdio>
 
 #include "chaos_kernels.cuh"
+#include "chaos_refmode.cuh"
 
 namespace chaos {
 
-constexpr uint32_t FULL = 0xffffffffu;
-constexpr int PERSIST_THREADS = 256;
 constexpr uint32_t PALETTE_SMEM = 4096;
-
-// ---------------------------------------------------------------------------
-// Reference-mode persistent kernels
-// ---------------------------------------------------------------------------
-
-__device__ __forceinline__ uint32_t next_tile(uint32_t *counter, uint32_t lane)
-{
-    uint32_t t = 0;
-    if (lane == 0) t = atomicAdd(counter, 1u);
-    return __shfl_sync(FULL, t, 0);
-}
-
-template <class R, int A, int F> __global__ void __launch_bounds__(PERSIST_THREADS) k_main(MainArgs<R> a)
-{
-    const uint32_t lane = threadIdx.x & 31u;
-    const SampleGeometry<R> g = make_geometry(a.image, a.size, a.max_iter, a.jcx, a.jcy);
-    for (;;) {
-        uint32_t t = next_tile(a.counter, lane);
-        if (t >= a.n_tiles) break;
-        uint32_t x0 = 8u * (t % a.tiles_x), y0 = 4u * (t / a.tiles_x);
-        render_main_tile<R, A, F>(g, a.out, a.pitch, a.size, x0, y0, lane, a.max_ss, a.flags);
-    }
-}
-
-template <class R, int A, int F> __global__ void __launch_bounds__(PERSIST_THREADS) k_advanced(AdvancedArgs<R> a)
-{
-    const uint32_t lane = threadIdx.x & 31u;
-    const SampleGeometry<R> g = make_geometry(a.m.image, a.m.size, a.m.max_iter, a.m.jcx, a.m.jcy);
-    for (;;) {
-        uint32_t t = next_tile(a.m.counter, lane);
-        if (t >= a.m.n_tiles) break;
-        uint32_t x0 = 8u * (t % a.m.tiles_x), y0 = 4u * (t / a.m.tiles_x);
-        render_advanced_tile<R, A, F>(g, a.m.image, a.image_reused, a.m.out, a.m.pitch, a.m.size, a.in, a.in_pitch,
-                                      a.focus, x0, y0, lane, a.m.max_ss, a.m.flags);
-    }
-}
 
 // ---------------------------------------------------------------------------
 // Independent-sample frames with per-lane refill
@@ -289,7 +252,7 @@ __global__ void __launch_bounds__(256) k_compose(ComposeArgs a)
 {
     __shared__ uint32_t s_pal[PALETTE_SMEM];
     const uint32_t *pal = a.palette;
-    if (!a.visualize && a.palette_len <= PALETTE_SMEM) {
+    if (!a.visualize && a.palette && a.palette_len <= PALETTE_SMEM) {
         for (uint32_t k = threadIdx.x; k < a.palette_len; k += blockDim.x) s_pal[k] = a.palette[k];
         pal = s_pal;
     }
@@ -301,8 +264,9 @@ __global__ void __launch_bounds__(256) k_compose(ComposeArgs a)
         uint32_t c[4] = {0, 0, 0, 0};
 #pragma unroll
         for (int k = 0; k < 4; k++)
-            if (x + k < a.w) c[k] = compose_pixel(load_pixel(pixel_ptr(a.in, a.pitch, x + k, y)), pal, a.palette_len,
-                                                  a.max_ss, a.visualize);
+            if (x + k < a.w)
+                c[k] = compose_pixel(load_pixel(pixel_ptr(a.in, a.pitch, x + k, y)), pal, a.palette_len, a.max_ss,
+                                     a.visualize, a.color_mode, a.magnifier);
         uint32_t *row = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(a.out) + (size_t)y * (size_t)a.out_pitch);
         if (x + 3u < a.w && (reinterpret_cast<uintptr_t>(row + x) & 15u) == 0) {
             *reinterpret_cast<uint4 *>(row + x) = make_uint4(c[0], c[1], c[2], c[3]);
@@ -337,32 +301,11 @@ template <int F> __global__ void k_debug()
 // Launchers
 // ---------------------------------------------------------------------------
 
-template <class KernelPtr> static int occupancy(KernelPtr k, int threads)
-{
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads, 0) != cudaSuccess || n < 1) n = 1;
-    return n;
-}
-
-static unsigned grid_for(unsigned long long work_warps, int occ, int sms)
-{
-    unsigned long long blocks = (work_warps + (PERSIST_THREADS / 32) - 1) / (PERSIST_THREADS / 32);
-    unsigned long long cap = (unsigned long long)occ * (unsigned long long)sms;
-    if (blocks > cap) blocks = cap;
-    if (blocks < 1) blocks = 1;
-    return (unsigned)blocks;
-}
-
-template <class R, int A, int F> static cudaError_t launch_main_t(const MainArgs<R> &a, int sms, cudaStream_t s)
-{
-    static const int occ = occupancy(k_main<R, A, F>, PERSIST_THREADS);
-    k_main<R, A, F><<<grid_for(a.n_tiles, occ, sms), PERSIST_THREADS, 0, s>>>(a);
-    return cudaGetLastError();
-}
 
 template <class R>
 cudaError_t launch_main(const MainArgs<R> &a, int arith, int fractal, int sms, cudaStream_t s)
 {
+    if (fractal >= FRACTAL_NEWTON_WIRED) return launch_main_newton<R>(a, fractal, sms, s);
     if (arith == ARITH_PARITY)
         return fractal == FRACTAL_JULIA ? launch_main_t<R, ARITH_PARITY, FRACTAL_JULIA>(a, sms, s)
                                         : launch_main_t<R, ARITH_PARITY, FRACTAL_MANDELBROT>(a, sms, s);
@@ -370,16 +313,11 @@ cudaError_t launch_main(const MainArgs<R> &a, int arith, int fractal, int sms, c
                                     : launch_main_t<R, ARITH_FMA, FRACTAL_MANDELBROT>(a, sms, s);
 }
 
-template <class R, int A, int F> static cudaError_t launch_advanced_t(const AdvancedArgs<R> &a, int sms, cudaStream_t s)
-{
-    static const int occ = occupancy(k_advanced<R, A, F>, PERSIST_THREADS);
-    k_advanced<R, A, F><<<grid_for(a.m.n_tiles, occ, sms), PERSIST_THREADS, 0, s>>>(a);
-    return cudaGetLastError();
-}
 
 template <class R>
 cudaError_t launch_advanced(const AdvancedArgs<R> &a, int arith, int fractal, int sms, cudaStream_t s)
 {
+    if (fractal >= FRACTAL_NEWTON_WIRED) return launch_advanced_newton<R>(a, fractal, sms, s);
     if (arith == ARITH_PARITY)
         return fractal == FRACTAL_JULIA ? launch_advanced_t<R, ARITH_PARITY, FRACTAL_JULIA>(a, sms, s)
                                         : launch_advanced_t<R, ARITH_PARITY, FRACTAL_MANDELBROT>(a, sms, s);

@@ -37,6 +37,8 @@ template <class R> struct MainArgs {
     double jcx, jcy;
     uint32_t tiles_x, n_tiles;
     uint32_t *counter;
+    unsigned long long *total;  // optional: pixel-iterations of the samples taken
+    NewtonParams newton;        // Newton modules only
 };
 
 template <class R> struct AdvancedArgs {
@@ -74,6 +76,8 @@ struct ComposeArgs {
     uint32_t palette_len;
     float max_ss;
     bool visualize;
+    int color_mode;  // ColorMode of the module
+    int magnifier;   // colorMagnifier (COLOR_MAGNIFIED)
 };
 
 // Launchers (chaos_kernels.cu).  Return the cudaError_t of the launch.
@@ -87,6 +91,13 @@ cudaError_t launch_compose(const ComposeArgs &a, cudaStream_t s);
 cudaError_t launch_under_sampled(void *out, long pitch, uint32_t w, uint32_t h, Rect<float> rect, uint32_t max_iter,
                                  uint32_t level, int fractal, double jcx, double jcy, cudaStream_t s);
 cudaError_t launch_debug(int fractal, cudaStream_t s);
+// Newton modules (chaos_newton.cu, rounded arithmetic).
+template <class R> cudaError_t launch_main_newton(const MainArgs<R> &a, int fractal, int device_sms, cudaStream_t s);
+template <class R>
+cudaError_t launch_advanced_newton(const AdvancedArgs<R> &a, int fractal, int device_sms, cudaStream_t s);
+cudaError_t launch_under_sampled_newton(void *out, long pitch, uint32_t w, uint32_t h, Rect<float> rect,
+                                        uint32_t max_iter, uint32_t level, int fractal, const NewtonParams &p,
+                                        cudaStream_t s);
 // FMA-pipe probe: grid x 256 threads, `iters` rounds of 8 independent FMA chains.
 cudaError_t launch_fma_peak(bool dbl, int blocks, uint32_t iters, double *sink, cudaStream_t s);
 

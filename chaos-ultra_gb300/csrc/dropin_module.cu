@@ -9,8 +9,13 @@
 // RenderingKernel.java:20-25, KernelMain.java:19-20, KernelAdvanced.java:26-29,
 // KernelCompose.java:24-33, KernelUnderSampled.java), and the __constant__
 // symbols the host writes by name (cuModuleGetGlobal):
-//     VISUALIZE_SAMPLE_COUNT  bool, 1 byte        gen.cu:14
-//     julia_c                 double[2] (julia)   julia.cu:3
+//     VISUALIZE_SAMPLE_COUNT  bool, 1 byte                     gen.cu:14
+//     julia_c                 double[2] (julia)                julia.cu:3
+//     roots                   Point<double>[3] = double[6]     newton_generic.cu:7, newton_iterations.cu:7
+//     coefficients            double[4]                        newton_generic.cu:8, newton_iterations.cu:8
+//     colorMagnifier          int (newton iterations)          newton_iterations.cu:9
+// Fractal ids: 0 mandelbrot, 1 julia, 2 newton_wired, 3 newton_generic,
+// 4 newton_iterations.
 //
 // Launch shape is the host's: blocks of 32x32 threads, grid ceil(W/32) x
 // ceil(H/32) (CudaFractalRenderer.java:36-37, 242-243, 371-378).  Each warp
@@ -29,7 +34,10 @@
 #include "chaos_device.cuh"
 
 #ifndef CHAOS_DROPIN_FRACTAL
-#error "define CHAOS_DROPIN_FRACTAL (0 = mandelbrot, 1 = julia)"
+#error "define CHAOS_DROPIN_FRACTAL (0 mandelbrot, 1 julia, 2-4 newton wired/generic/iterations)"
+#endif
+#if CHAOS_DROPIN_FRACTAL >= 2
+#include "chaos_newton.cuh"
 #endif
 #ifndef CHAOS_DROPIN_ARITH
 #define CHAOS_DROPIN_ARITH chaos::ARITH_FMA
@@ -42,6 +50,13 @@ using chaos::UInt2;
 __constant__ bool VISUALIZE_SAMPLE_COUNT = false;
 #if CHAOS_DROPIN_FRACTAL == 1
 __constant__ double julia_c[2];
+#endif
+#if CHAOS_DROPIN_FRACTAL == 3 || CHAOS_DROPIN_FRACTAL == 4
+__constant__ double roots[6];
+__constant__ double coefficients[4];
+#endif
+#if CHAOS_DROPIN_FRACTAL == 4
+__constant__ int colorMagnifier;
 #endif
 
 namespace {
@@ -57,6 +72,33 @@ __device__ __forceinline__ void julia_constant(double &jx, double &jy)
 #else
     jx = 0.0;
     jy = 0.0;
+#endif
+}
+
+__device__ __forceinline__ void newton_constants(chaos::NewtonParams &p)
+{
+#if CHAOS_DROPIN_FRACTAL == 3 || CHAOS_DROPIN_FRACTAL == 4
+    for (int k = 0; k < 6; k++) p.roots[k] = roots[k];
+    for (int k = 0; k < 4; k++) p.coefficients[k] = coefficients[k];
+#endif
+#if CHAOS_DROPIN_FRACTAL == 4
+    p.color_magnifier = colorMagnifier;
+#endif
+    (void)p;
+}
+
+__device__ __forceinline__ int color_mode()
+{
+    return kFractal == 2 || kFractal == 3 ? chaos::COLOR_ROOTS : kFractal == 4 ? chaos::COLOR_MAGNIFIED
+                                                                               : chaos::COLOR_PALETTE;
+}
+
+__device__ __forceinline__ int color_magnifier()
+{
+#if CHAOS_DROPIN_FRACTAL == 4
+    return colorMagnifier;
+#else
+    return 1;
 #endif
 }
 
@@ -80,8 +122,10 @@ __device__ __forceinline__ void main_entry(PixelInfo *out, long pitch, UInt2 siz
     if (x0 >= size.x || y0 >= size.y) return;  // whole warp outside the image
     double jx, jy;
     julia_constant(jx, jy);
-    const chaos::SampleGeometry<R> g = chaos::make_geometry(image, size, max_iter, jx, jy);
-    chaos::render_main_tile<R, kArith, kFractal>(g, out, pitch, size, x0, y0, lane, max_ss, flags);
+    chaos::SampleGeometry<R> g = chaos::make_geometry(image, size, max_iter, jx, jy);
+    newton_constants(g.newton);
+    unsigned long long iters = 0;  // the Java host reads no iteration counts
+    chaos::render_main_tile<R, kArith, kFractal>(g, out, pitch, size, x0, y0, lane, max_ss, flags, iters);
 }
 
 template <class R>
@@ -94,9 +138,11 @@ __device__ __forceinline__ void advanced_entry(PixelInfo *out, long pitch, UInt2
     if (x0 >= size.x || y0 >= size.y) return;
     double jx, jy;
     julia_constant(jx, jy);
-    const chaos::SampleGeometry<R> g = chaos::make_geometry(image, size, max_iter, jx, jy);
+    chaos::SampleGeometry<R> g = chaos::make_geometry(image, size, max_iter, jx, jy);
+    newton_constants(g.newton);
+    unsigned long long iters = 0;
     chaos::render_advanced_tile<R, kArith, kFractal>(g, image, image_reused, out, pitch, size, in, in_pitch, focus, x0,
-                                                     y0, lane, max_ss, flags);
+                                                     y0, lane, max_ss, flags, iters);
 }
 
 }  // namespace
@@ -155,8 +201,13 @@ extern "C" __global__ void __launch_bounds__(1024, 1)
         uint32_t full = (uint32_t)fmax(1.0, (double)maxSuperSampling);
         color = chaos::colorize_sample_count((uint32_t)p.weight, full);
         if (p.is_reused) color = chaos::colorize_sample_count((uint32_t)p.weight_of_new_samples, full);
+    } else if (color_mode() == chaos::COLOR_ROOTS) {
+        color = chaos::colorize_value(p.value, nullptr, 0, chaos::COLOR_ROOTS, 1);
     } else {
-        uint32_t idx = chaos::palette_index(p.value, paletteLength);
+        uint32_t vi = (uint32_t)roundf(p.value);
+        uint32_t idx = color_mode() == chaos::COLOR_MAGNIFIED
+                           ? paletteLength - (vi * (uint32_t)color_magnifier() % paletteLength) - 1u
+                           : chaos::palette_index(p.value, paletteLength);
         surf2Dread(&color, colorPalette, (int)(idx * sizeof(uint32_t)), 0);
     }
     surf2Dwrite(color, surfaceOutput, (int)(x * sizeof(uint32_t)), (int)y);
@@ -177,7 +228,12 @@ extern "C" __global__ void __launch_bounds__(1024, 1)
     float cy = __fsub_rn(right_top_y, __fmul_rn((float)iy, ph));
     double jx, jy;
     julia_constant(jx, jy);
-    uint32_t e = chaos::compute_fractal<float, kArith, kFractal>(maxIterations, cx, cy, (float)jx, (float)jy);
+    chaos::SampleGeometry<float> g{};
+    g.max_iter = maxIterations;
+    g.jcx = (float)jx;
+    g.jcy = (float)jy;
+    newton_constants(g.newton);
+    uint32_t e = chaos::compute_fractal_g<float, kArith, kFractal>(g, cx, cy);
     chaos::store_pixel(chaos::pixel_ptr(output, outputPitch, ix, iy),
                        chaos::make_pixel((float)e, __fdiv_rn(1.f, (float)underSamplingLevel)));
 }
@@ -187,5 +243,6 @@ extern "C" __global__ void debug()
 {
     const uint32_t x = blockDim.x * blockIdx.x + threadIdx.x;
     const uint32_t y = blockDim.y * blockIdx.y + threadIdx.y;
-    if (x == 0 && y == 0) printf("hello from %s\n", kFractal == 1 ? "julia" : "mandelbrot");
+    // debugFractal: the escape-time modules greet, the Newton modules' is empty
+    if (x == 0 && y == 0 && kFractal <= 1) printf("hello from %s\n", kFractal == 1 ? "julia" : "mandelbrot");
 }

@@ -206,6 +206,7 @@ int chaos_renderer_destroy(chaos_renderer *r);
 
 #define CHAOS_TIER_F32 0         /* escape loop in binary32 */
 #define CHAOS_TIER_F64 1         /* escape loop in binary64 */
+#define CHAOS_TIER_FLOATFLOAT 2  /* float-float (two binary32 words, ~48 bits), batched viewports */
 #define CHAOS_TIER_PERTURB_F32 3 /* perturbation, binary32 differences (pixel size >= 1e-30) */
 #define CHAOS_TIER_PERTURB_F64 4 /* perturbation, binary64 differences (pixel size >= 1e-290) */
 
@@ -262,6 +263,117 @@ int chaos_render_frame(const chaos_frame_desc *desc, const chaos_frame_out *out,
 int chaos_render_frame_host(const chaos_frame_desc *desc, const uint32_t *palette, uint32_t palette_len,
                             uint32_t interior_rgba, uint32_t *rgba_host, unsigned long long *total_host,
                             void *stream);
+
+/* ---- batches: many viewports in one CUDA-graph launch -------------------- */
+
+#define CHAOS_TIER_AUTO 255
+
+/* One viewport of a batch.  Samples as in chaos_frame_desc (the plane point is
+ * computed in binary64, then rounded to the viewport's tier).  Outputs are
+ * device pointers, each optional: counts/smooth [height][width][spp], rgba
+ * [height][width] (needs the batch palette). */
+typedef struct chaos_viewport {
+    uint32_t width, height;
+    uint32_t max_iterations;
+    uint32_t samples_per_pixel;
+    uint32_t sample_mode;
+    uint32_t tier; /* CHAOS_TIER_F32, _FLOATFLOAT, _F64 or CHAOS_TIER_AUTO */
+    uint64_t seed;
+    double center_x, center_y, pixel_size;
+    uint32_t *counts;
+    float *smooth;
+    uint32_t *rgba;
+} chaos_viewport;
+
+/* Launch shape per tier (index 0 binary32, 1 float-float, 2 binary64); zero
+ * keeps the default (256 threads, 16-step escape blocks). */
+typedef struct chaos_batch_config {
+    uint32_t block_threads[3]; /* 32..512, multiple of 32 */
+    uint32_t escape_block[3];  /* 8, 16 or 32 */
+} chaos_batch_config;
+
+typedef struct chaos_batch chaos_batch;
+
+/* The tier CHAOS_TIER_AUTO picks: binary32 while the pixel is at least
+ * 2^-18 m, float-float down to 2^-42 m, binary64 below (m = max(|cx|, |cy|, 1/256)). */
+uint32_t chaos_batch_auto_tier(double center_x, double center_y, double pixel_size);
+/* Upload the viewport table and build one CUDA graph: a memset of the work
+ * counters, then one persistent kernel per tier present, forked and joined. */
+int chaos_batch_create(const chaos_viewport *viewports, uint32_t n, const uint32_t *palette, uint32_t palette_len,
+                       uint32_t interior_rgba, const chaos_batch_config *config, chaos_batch **out);
+/* One cudaGraphLaunch on `stream` (does not synchronise). */
+int chaos_batch_launch(chaos_batch *batch, void *stream);
+/* The tier each viewport got (n >= number of viewports). */
+int chaos_batch_tiers(const chaos_batch *batch, uint32_t *tiers, uint32_t n);
+/* Device address of the batch's pixel-iteration total (reset by every launch). */
+int chaos_batch_total(const chaos_batch *batch, unsigned long long **device_total);
+/* The same total copied to host memory (synchronises the device). */
+int chaos_batch_read_total(const chaos_batch *batch, unsigned long long *total);
+int chaos_batch_destroy(chaos_batch *batch);
+
+/* ---- serving: concurrent zoom sessions ----------------------------------- */
+
+/* A viewer zooming toward (target_x, target_y): frame 0 shows the plane of
+ * width `span` centred on (center_x, center_y); every later frame shrinks the
+ * plane by zoom_per_frame about the target, which keeps its place on screen
+ * (RenderingController.zoomAt, J/rendering/RenderingController.java:130-150).
+ * Frames follow CudaFractalRenderer: renderQuality first, then renderFast
+ * (sample reuse from the previous frame, foveation around the target's pixel
+ * when CHAOS_FLAG_FOVEATION is set). */
+typedef struct chaos_session_desc {
+    uint32_t width, height;
+    uint32_t max_iterations;
+    float max_super_sampling;
+    uint32_t flags; /* CHAOS_FLAG_ADAPTIVE_SS | CHAOS_FLAG_SAMPLE_REUSE | CHAOS_FLAG_FOVEATION */
+    uint32_t fractal;
+    int32_t arith;
+    uint32_t pad_;
+    double center_x, center_y, span;
+    double target_x, target_y;
+    double zoom_per_frame;
+    double julia_cx, julia_cy;
+} chaos_session_desc;
+
+/* One served frame; times in seconds on the server's clock. */
+typedef struct chaos_frame_record {
+    uint32_t session, frame;
+    double arrival_s, start_s, done_s; /* done_s < 0: not finished */
+    int32_t precision;                 /* CHAOS_PRECISION_* the frame used */
+    int32_t pad_;
+} chaos_frame_record;
+
+typedef struct chaos_server chaos_server;
+
+/* A server with an HBM budget (bytes) for its sessions and one palette (host
+ * array, copied).  Sessions are admitted against the budget. */
+int chaos_server_create(size_t hbm_budget_bytes, const uint32_t *palette, uint32_t palette_len,
+                        chaos_server **out);
+/* Bytes a session of this shape is charged (two reuse buffers + RGBA8 output). */
+int chaos_server_session_bytes(const chaos_session_desc *desc, size_t *bytes);
+/* Open a session: refused with CHAOS_ERR_OUT_OF_MEMORY (nothing allocated)
+ * when it does not fit the remaining budget.  The session keeps its buffers
+ * and its own CUDA stream until closed. */
+int chaos_server_open(chaos_server *server, const chaos_session_desc *desc, uint32_t *session);
+int chaos_server_close(chaos_server *server, uint32_t session);
+/* Enqueue the session's next frame and return at once (arrival_s is recorded
+ * as the request's arrival time). */
+int chaos_server_submit(chaos_server *server, uint32_t session, double arrival_s);
+/* Wait until every submitted frame has finished. */
+int chaos_server_drain(chaos_server *server);
+/* Replay a request trace in real time: request k is submitted when the
+ * server clock reaches (clock at the call) + arrival_s[k]; then drain. */
+int chaos_server_run_trace(chaos_server *server, const uint32_t *sessions, const double *arrival_s, uint32_t n);
+/* Records of all frames submitted so far (*n = their number; at most max are copied). */
+int chaos_server_records(chaos_server *server, chaos_frame_record *out, uint32_t max, uint32_t *n);
+/* The session's latest RGBA8 image (width*height words) and the pixel-iterations
+ * its frames have run so far; waits for the session's queued frames. */
+int chaos_server_read(chaos_server *server, uint32_t session, uint32_t *host_rgba,
+                      unsigned long long *pixel_iterations);
+/* Bytes held by open sessions and the budget. */
+int chaos_server_usage(const chaos_server *server, size_t *used, size_t *budget);
+/* Seconds since the server was created. */
+double chaos_server_clock(const chaos_server *server);
+int chaos_server_destroy(chaos_server *server);
 
 /* ---- deep zoom: perturbation against a multi-word reference orbit ------- */
 

@@ -1046,3 +1046,125 @@ void orc_frame_offsets(const orc_frame_desc *d, long pix_start, long pix_count, 
         }
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* Batched viewports (the library's k_batch) and float-float arithmetic      */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    float hi, lo;
+} ff_t;
+
+static ff_t ff_fast_two_sum(float a, float b)
+{
+    float s = a + b;
+    ff_t r = {s, b - (s - a)};
+    return r;
+}
+static ff_t ff_add(ff_t a, ff_t b)
+{
+    float s = a.hi + b.hi;
+    float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e = e + (a.lo + b.lo);
+    return ff_fast_two_sum(s, e);
+}
+static ff_t ff_mul(ff_t a, ff_t b)
+{
+    float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return ff_fast_two_sum(p, e);
+}
+static ff_t ff_sqr(ff_t a)
+{
+    float p = a.hi * a.hi;
+    float e = fmaf(a.hi, a.hi, -p);
+    e = fmaf(a.hi + a.hi, a.lo, e);
+    return ff_fast_two_sum(p, e);
+}
+static ff_t ff_from_double(double d)
+{
+    float hi = (float)d;
+    ff_t r = {hi, (float)(d - (double)hi)};
+    return r;
+}
+
+static uint32_t esc_ff(uint32_t max_iter, ff_t cx, ff_t cy, float *r2_exit)
+{
+    ff_t x = {0.f, 0.f}, y = {0.f, 0.f};
+    uint32_t i = 0;
+    float r2;
+    for (;;) {
+        r2 = fmaf(x.hi, x.hi, y.hi * y.hi);
+        if (!(i < max_iter && r2 < 4.0f)) break;
+        ff_t xx = ff_sqr(x), yy = ff_sqr(y), xy = ff_mul(x, y);
+        ff_t nyy = {-yy.hi, -yy.lo};
+        ff_t xn = ff_add(ff_add(xx, nyy), cx);
+        ff_t xy2 = {xy.hi + xy.hi, xy.lo + xy.lo};
+        y = ff_add(xy2, cy);
+        x = xn;
+        ++i;
+    }
+    *r2_exit = r2;
+    return i;
+}
+
+typedef struct {
+    uint32_t w, h, spp, mode, max_iter, tier; /* tier: 0 binary32, 1 binary64, 2 float-float */
+    uint64_t seed;
+    double cx, cy, ps;
+} orc_viewport;
+
+/* One viewport of a batch: sample point in binary64 (fma), rounded to the
+ * tier, Mandelbrot with fused multiply-adds (binary32/64) or float-float;
+ * outputs as orc_frame.  Returns the pixel-iterations. */
+uint64_t orc_batch_viewport(const orc_viewport *v, uint32_t *counts, float *smooth, uint32_t *rgba,
+                            const uint32_t *palette, uint32_t palette_len, uint32_t interior_rgba)
+{
+    uint64_t total = 0;
+    long n = (long)v->w * v->h;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : total)
+    for (long q = 0; q < n; q++) {
+        uint32_t pix = (uint32_t)q, px = pix % v->w, py = pix / v->w;
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        for (uint32_t s = 0; s < v->spp; s++) {
+            double ox = 0.5, oy = 0.5;
+            if (v->mode == 1) {
+                ox = (double)(orc_sample_hash(v->seed, pix, s, 0) >> 11) * 0x1p-53;
+                oy = (double)(orc_sample_hash(v->seed, pix, s, 1) >> 11) * 0x1p-53;
+            }
+            double dxp = ((double)px + ox) - 0.5 * v->w, dyp = ((double)py + oy) - 0.5 * v->h;
+            double cxd = fma(dxp, v->ps, v->cx), cyd = fma(-dyp, v->ps, v->cy);
+            uint32_t i;
+            float r2f;
+            if (v->tier == 0) {
+                i = esc_fma_f(v->max_iter, 0.f, 0.f, (float)cxd, (float)cyd, &r2f);
+            } else if (v->tier == 1) {
+                double r2;
+                i = esc_fma_d(v->max_iter, 0.0, 0.0, cxd, cyd, &r2);
+                r2f = (float)r2;
+            } else {
+                i = esc_ff(v->max_iter, ff_from_double(cxd), ff_from_double(cyd), &r2f);
+            }
+            int escaped = i < v->max_iter;
+            float nu = smooth_value(i, r2f, v->max_iter);
+            size_t sidx = (size_t)q * v->spp + s;
+            if (counts) counts[sidx] = i;
+            if (smooth) smooth[sidx] = nu;
+            total += i;
+            if (rgba) {
+                float ch[4];
+                if (escaped) {
+                    palette_lerp(palette, palette_len, nu, ch);
+                } else {
+                    for (int k = 0; k < 4; k++) ch[k] = (float)((interior_rgba >> (8 * k)) & 255u);
+                }
+                for (int k = 0; k < 4; k++) acc[k] = acc[k] + ch[k];
+            }
+        }
+        if (rgba) rgba[q] = pack_mean_rgba(acc, v->spp);
+    }
+    return total;
+}

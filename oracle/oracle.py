@@ -30,6 +30,13 @@ class FrameDesc(C.Structure):
                 ("pixel_size", C.c_double), ("jcx", C.c_double), ("jcy", C.c_double)]
 
 
+class Viewport(C.Structure):
+    """orc_viewport (oracle/chaos_oracle.c); tier 0 binary32, 1 binary64, 2 float-float."""
+    _fields_ = [("w", C.c_uint32), ("h", C.c_uint32), ("spp", C.c_uint32), ("mode", C.c_uint32),
+                ("max_iter", C.c_uint32), ("tier", C.c_uint32), ("seed", C.c_uint64), ("cx", C.c_double),
+                ("cy", C.c_double), ("ps", C.c_double)]
+
+
 _d4 = C.c_double * 4
 _d2 = C.c_double * 2
 
@@ -79,6 +86,9 @@ class Oracle:
         L.orc_hp_escape_batch.restype = None
         L.orc_hp_escape_batch.argtypes = [C.c_char_p, C.c_char_p, C.c_long, C.c_void_p, C.c_void_p, C.c_uint32,
                                           C.c_uint32, C.c_void_p, C.c_void_p]
+        L.orc_batch_viewport.restype = C.c_uint64
+        L.orc_batch_viewport.argtypes = [C.POINTER(Viewport), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_uint32, C.c_uint32]
         L.orc_frame_offsets.restype = None
         L.orc_frame_offsets.argtypes = [C.POINTER(FrameDesc), C.c_long, C.c_long, C.c_void_p, C.c_void_p]
         L.orc_sample_hash.restype = C.c_uint64
@@ -185,6 +195,17 @@ class Oracle:
         self.lib.orc_frame_offsets(C.byref(d), pix_start, pix_count, _ptr(xs), _ptr(ys))
         return xs, ys
 
+    def batch_viewport(self, w, h, spp, mode, max_iter, tier, seed, center, ps, palette=None,
+                       interior_rgba=0xFF000000):
+        v = Viewport(w, h, spp, mode, max_iter, tier, seed, center[0], center[1], ps)
+        counts = np.zeros(w * h * spp, dtype=np.uint32)
+        sm = np.zeros(w * h * spp, dtype=np.float32)
+        pal = np.ascontiguousarray(palette, dtype=np.uint32) if palette is not None else None
+        rgba = np.zeros(w * h, dtype=np.uint32) if pal is not None else None
+        total = self.lib.orc_batch_viewport(C.byref(v), _ptr(counts), _ptr(sm), _ptr(rgba), _ptr(pal),
+                                            len(pal) if pal is not None else 0, interior_rgba)
+        return {"total": int(total), "counts": counts, "smooth": sm, "rgba": rgba}
+
     def max_threads(self):
         return self.lib.orc_max_threads()
 
@@ -259,6 +280,17 @@ class Reference:
         ys = np.zeros(pix_count * spp, dtype=np.float64)
         self.lib.orc_frame_offsets(C.byref(d), pix_start, pix_count, _ptr(xs), _ptr(ys))
         return xs, ys
+
+    def batch_viewport(self, w, h, spp, mode, max_iter, tier, seed, center, ps, palette=None,
+                       interior_rgba=0xFF000000):
+        v = Viewport(w, h, spp, mode, max_iter, tier, seed, center[0], center[1], ps)
+        counts = np.zeros(w * h * spp, dtype=np.uint32)
+        sm = np.zeros(w * h * spp, dtype=np.float32)
+        pal = np.ascontiguousarray(palette, dtype=np.uint32) if palette is not None else None
+        rgba = np.zeros(w * h, dtype=np.uint32) if pal is not None else None
+        total = self.lib.orc_batch_viewport(C.byref(v), _ptr(counts), _ptr(sm), _ptr(rgba), _ptr(pal),
+                                            len(pal) if pal is not None else 0, interior_rgba)
+        return {"total": int(total), "counts": counts, "smooth": sm, "rgba": rgba}
 
     def max_threads(self):
         return self.lib.ref_max_threads()

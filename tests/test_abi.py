@@ -179,7 +179,8 @@ def test_struct_layouts_match_header(native, tmp_path):
     if not cc:
         pytest.skip("no C compiler")
     structs = {"chaos_rendering_model": cg.RenderingModel, "chaos_frame_desc": cg.FrameDesc,
-               "chaos_frame_out": cg.FrameOut}
+               "chaos_frame_out": cg.FrameOut, "chaos_viewport": cg.Viewport, "chaos_batch_config": cg.BatchConfig,
+               "chaos_session_desc": cg.SessionDesc, "chaos_frame_record": cg.FrameRecord}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
