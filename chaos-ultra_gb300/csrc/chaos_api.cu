@@ -132,7 +132,108 @@ struct FractalInfo {
     const char *name;
     int kind;
 };
-const FractalInfo kFractals[] = {{"mandelbrot", FRACTAL_MANDELBROT}, {"julia", FRACTAL_JULIA}};
+// Registered modules: the module file name and the name the Java GUI shows
+// (CudaFractalRendererProvider.java:19-31, modules/Module*.java constructors).
+const FractalInfo kFractals[] = {
+    {"mandelbrot", FRACTAL_MANDELBROT},          {"julia", FRACTAL_JULIA},
+    {"newton_wired", FRACTAL_NEWTON_WIRED},      {"newton wired", FRACTAL_NEWTON_WIRED},
+    {"newton_generic", FRACTAL_NEWTON_GENERIC},  {"newton generic", FRACTAL_NEWTON_GENERIC},
+    {"newton_iterations", FRACTAL_NEWTON_ITERATIONS}, {"newton colored by iterations", FRACTAL_NEWTON_ITERATIONS}};
+const char *kDisplayNames[] = {"mandelbrot", "julia", "newton wired", "newton generic",
+                               "newton colored by iterations"};
+
+// ---- the JSON subset of the Newton modules' custom parameters -------------
+// {"coefficients": [a3, a2, a1, a0], "roots": [[re, im], x3], "colorMagnifier": n}
+// (ModuleNewtonGeneric.parseJsonToParams, ModuleNewtonIterations.java:15-24)
+struct JsonValue {
+    enum Kind { NUMBER, ARRAY, OBJECT, OTHER } kind = OTHER;
+    double number = 0;
+    std::vector<JsonValue> items;
+    std::vector<std::pair<std::string, JsonValue>> members;
+};
+
+void json_ws(const char *&p)
+{
+    while (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r') p++;
+}
+
+bool json_parse(const char *&p, JsonValue &v, int depth = 0)
+{
+    if (depth > 16) return false;
+    json_ws(p);
+    if (*p == '[') {
+        p++;
+        v.kind = JsonValue::ARRAY;
+        json_ws(p);
+        if (*p == ']') {
+            p++;
+            return true;
+        }
+        for (;;) {
+            JsonValue item;
+            if (!json_parse(p, item, depth + 1)) return false;
+            v.items.push_back(item);
+            json_ws(p);
+            if (*p == ',') {
+                p++;
+                continue;
+            }
+            if (*p == ']') {
+                p++;
+                return true;
+            }
+            return false;
+        }
+    }
+    if (*p == '{') {
+        p++;
+        v.kind = JsonValue::OBJECT;
+        json_ws(p);
+        if (*p == '}') {
+            p++;
+            return true;
+        }
+        for (;;) {
+            json_ws(p);
+            if (*p != '"') return false;
+            const char *q = ++p;
+            while (*p && *p != '"') p++;
+            if (*p != '"') return false;
+            std::string key(q, p - q);
+            p++;
+            json_ws(p);
+            if (*p != ':') return false;
+            p++;
+            JsonValue item;
+            if (!json_parse(p, item, depth + 1)) return false;
+            v.members.emplace_back(key, item);
+            json_ws(p);
+            if (*p == ',') {
+                p++;
+                continue;
+            }
+            if (*p == '}') {
+                p++;
+                return true;
+            }
+            return false;
+        }
+    }
+    char *end = nullptr;
+    double d = std::strtod(p, &end);
+    if (end == p) return false;
+    v.kind = JsonValue::NUMBER;
+    v.number = d;
+    p = end;
+    return true;
+}
+
+const JsonValue *json_member(const JsonValue &o, const char *key)
+{
+    for (const auto &m : o.members)
+        if (m.first == key) return &m.second;
+    return nullptr;
+}
 
 int arith_of(int arith)
 {
@@ -189,6 +290,7 @@ struct chaos_module {
     std::string name;
     bool visualize = false;
     double julia_c[2] = {0.0, 0.0};
+    NewtonParams newton{};
 };
 
 
@@ -196,7 +298,10 @@ const char *chaos_last_error(void) { return g_last_error.c_str(); }
 
 const char *chaos_version(void) { return "chaos_gb300 0.1 (sm_103a)"; }
 
-const char *chaos_available_fractals(void) { return "mandelbrot,julia"; }
+const char *chaos_available_fractals(void)
+{
+    return "mandelbrot,julia,newton wired,newton generic,newton colored by iterations";
+}
 
 int chaos_module_open(const char *fractal_name, chaos_module **out)
 {
@@ -206,7 +311,14 @@ int chaos_module_open(const char *fractal_name, chaos_module **out)
             chaos_module *m = new (std::nothrow) chaos_module();
             if (!m) return fail(CHAOS_ERR_OUT_OF_MEMORY, "out of host memory");
             m->fractal = f.kind;
-            m->name = f.name;
+            m->name = kDisplayNames[f.kind];
+            // The Newton modules start from their supplyDefaultValues parameters
+            // (ModuleNewtonGeneric.java:67-74, ModuleNewtonIterations.java:26-33).
+            const double roots[6] = {1, 0, -0.5, 0.86602540378, -0.5, -0.86602540378};
+            const double coefficients[4] = {-1, 0, 0, 1};  // z^3 - 1, stored c0..c3
+            std::memcpy(m->newton.roots, roots, sizeof roots);
+            std::memcpy(m->newton.coefficients, coefficients, sizeof coefficients);
+            m->newton.color_magnifier = 11;
             *out = m;
             return CHAOS_OK;
         }
@@ -235,13 +347,63 @@ int chaos_module_write_constant(chaos_module *m, const char *name, const void *s
         std::memcpy(m->julia_c, src, sizeof m->julia_c);
         return CHAOS_OK;
     }
+    const bool generic = m->fractal == FRACTAL_NEWTON_GENERIC || m->fractal == FRACTAL_NEWTON_ITERATIONS;
+    if (generic && std::strcmp(name, "roots") == 0) {
+        if (size != sizeof m->newton.roots) return fail(CHAOS_ERR_INVALID_ARGUMENT, "roots is 48 bytes, got %zu", size);
+        std::memcpy(m->newton.roots, src, sizeof m->newton.roots);
+        return CHAOS_OK;
+    }
+    if (generic && std::strcmp(name, "coefficients") == 0) {
+        if (size != sizeof m->newton.coefficients)
+            return fail(CHAOS_ERR_INVALID_ARGUMENT, "coefficients is 32 bytes, got %zu", size);
+        std::memcpy(m->newton.coefficients, src, sizeof m->newton.coefficients);
+        return CHAOS_OK;
+    }
+    if (m->fractal == FRACTAL_NEWTON_ITERATIONS && std::strcmp(name, "colorMagnifier") == 0) {
+        if (size != sizeof(int)) return fail(CHAOS_ERR_INVALID_ARGUMENT, "colorMagnifier is 4 bytes, got %zu", size);
+        std::memcpy(&m->newton.color_magnifier, src, sizeof(int));
+        return CHAOS_OK;
+    }
     return fail(CHAOS_ERR_NOT_FOUND, "no constant named %s in module %s", name, m->name.c_str());
 }
 
 int chaos_module_set_custom_params(chaos_module *m, const char *text)
 {
     if (!m || !text) return fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (m->fractal != FRACTAL_JULIA) return CHAOS_OK;  // ModuleMandelbrot ignores its parameters
+    if (m->fractal == FRACTAL_NEWTON_GENERIC || m->fractal == FRACTAL_NEWTON_ITERATIONS) {
+        const char *p = text;
+        JsonValue v;
+        if (!json_parse(p, v) || v.kind != JsonValue::OBJECT)
+            return fail(CHAOS_ERR_INVALID_ARGUMENT, "custom parameters must be a JSON object");
+        const JsonValue *c = json_member(v, "coefficients"), *r = json_member(v, "roots");
+        if (!c || !r || c->kind != JsonValue::ARRAY || r->kind != JsonValue::ARRAY)
+            return fail(CHAOS_ERR_INVALID_ARGUMENT, "\"coefficients\" and \"roots\" arrays are required");
+        if (c->items.size() != 4) return fail(CHAOS_ERR_INVALID_ARGUMENT, "expecting 4 coefficients");
+        if (r->items.size() != 3) return fail(CHAOS_ERR_INVALID_ARGUMENT, "expecting 3 roots");
+        NewtonParams np = m->newton;
+        for (int k = 0; k < 4; k++) {
+            if (c->items[k].kind != JsonValue::NUMBER) return fail(CHAOS_ERR_INVALID_ARGUMENT, "bad coefficient");
+            np.coefficients[3 - k] = c->items[k].number;  // the user writes the highest power first
+        }
+        for (int k = 0; k < 3; k++) {
+            const JsonValue &root = r->items[k];
+            if (root.kind != JsonValue::ARRAY || root.items.size() != 2 || root.items[0].kind != JsonValue::NUMBER ||
+                root.items[1].kind != JsonValue::NUMBER)
+                return fail(CHAOS_ERR_INVALID_ARGUMENT, "Found a root that is not represented as [real, imag].");
+            np.roots[2 * k] = root.items[0].number;
+            np.roots[2 * k + 1] = root.items[1].number;
+        }
+        if (m->fractal == FRACTAL_NEWTON_ITERATIONS) {
+            const JsonValue *mag = json_member(v, "colorMagnifier");
+            if (mag) {
+                if (mag->kind != JsonValue::NUMBER) return fail(CHAOS_ERR_INVALID_ARGUMENT, "bad colorMagnifier");
+                np.color_magnifier = (int)mag->number;
+            }
+        }
+        m->newton = np;
+        return CHAOS_OK;
+    }
+    if (m->fractal != FRACTAL_JULIA) return CHAOS_OK;  // ModuleMandelbrot / ModuleNewtonWired ignore theirs
     // ModuleJulia: numbers separated by ',' or ';' (parseParamsAsDoubles,
     // FractalRenderingModule.java:233-241); the first two are julia_c.
     std::vector<double> vals;
@@ -279,11 +441,11 @@ int chaos_module_default_view(const chaos_module *m, double *cx, double *cy, dou
         *zoom = 2.0;
         *max_iter = 1600;
         *max_ss = 5.f;
-    } else {  // Model.resetRenderingValuesToDefault (Model.java:284-294) + ModuleJulia.java:40-49
+    } else {  // Model.resetRenderingValuesToDefault (Model.java:284-294) + the module's supplyDefaultValues
         *cx = 0.0;
         *cy = 0.0;
         *zoom = 4.0;
-        *max_iter = 900;
+        *max_iter = m->fractal == FRACTAL_JULIA ? 900 : 200;  // ModuleJulia.java:40-49, ModuleNewton*.java
         *max_ss = 2.f;
     }
     return CHAOS_OK;
@@ -315,6 +477,7 @@ static int render_main(chaos_module *m, chaos_pixel_info *out, long pitch, uint3
     a.flags = flags;
     a.jcx = m->julia_c[0];
     a.jcy = m->julia_c[1];
+    a.newton = m->newton;
     a.tiles_x = (w + 7u) / 8u;
     a.n_tiles = a.tiles_x * ((h + 3u) / 4u);
     if ((rc = take_counter(d, s, &a.counter))) return rc;
@@ -351,6 +514,7 @@ static int render_advanced(chaos_module *m, chaos_pixel_info *out, long pitch, u
     a.m.flags = flags;
     a.m.jcx = m->julia_c[0];
     a.m.jcy = m->julia_c[1];
+    a.m.newton = m->newton;
     a.m.tiles_x = (w + 7u) / 8u;
     a.m.n_tiles = a.m.tiles_x * ((h + 3u) / 4u);
     a.image_reused = Rect<R>{rect_reused[0], rect_reused[1], rect_reused[2], rect_reused[3]};
@@ -405,7 +569,8 @@ static int compose_impl(chaos_module *m, const chaos_pixel_info *in, long pitch,
     if ((rc = check_pitched(in, pitch, w, "input"))) return rc;
     if (!out || out_pitch < (long)(4u * w) || ((uintptr_t)out & 3u) || (out_pitch & 3))
         return fail(CHAOS_ERR_INVALID_ARGUMENT, "bad output buffer");
-    if (!m->visualize && (!palette || palette_len == 0))
+    const bool roots_only = m->fractal == FRACTAL_NEWTON_WIRED || m->fractal == FRACTAL_NEWTON_GENERIC;
+    if (!m->visualize && !roots_only && (!palette || palette_len == 0))
         return fail(CHAOS_ERR_INVALID_ARGUMENT, "palette required (length > 0)");
     ComposeArgs a{};
     a.in = in;
@@ -418,6 +583,10 @@ static int compose_impl(chaos_module *m, const chaos_pixel_info *in, long pitch,
     a.palette_len = palette_len;
     a.max_ss = max_ss;
     a.visualize = m->visualize;
+    a.color_mode = m->fractal == FRACTAL_NEWTON_WIRED || m->fractal == FRACTAL_NEWTON_GENERIC ? COLOR_ROOTS
+                   : m->fractal == FRACTAL_NEWTON_ITERATIONS                                 ? COLOR_MAGNIFIED
+                                                                                              : COLOR_PALETTE;
+    a.magnifier = m->newton.color_magnifier;
     return finish(launch_compose(a, s), s, sync);
 }
 
@@ -439,8 +608,13 @@ int chaos_render_under_sampled(chaos_module *m, chaos_pixel_info *out, long pitc
     if (level < 1) return fail(CHAOS_ERR_INVALID_ARGUMENT, "underSamplingLevel must be at least 1, current value: %u", level);
     if (!finite4(rect)) return fail(CHAOS_ERR_INVALID_ARGUMENT, "plane segment must be finite");
     cudaStream_t s = (cudaStream_t)stream;
-    return finish(launch_under_sampled(out, pitch, width, height, Rect<float>{rect[0], rect[1], rect[2], rect[3]},
-                                       max_iterations, level, m->fractal, m->julia_c[0], m->julia_c[1], s),
+    const Rect<float> r{rect[0], rect[1], rect[2], rect[3]};
+    if (m->fractal >= FRACTAL_NEWTON_WIRED)
+        return finish(
+            launch_under_sampled_newton(out, pitch, width, height, r, max_iterations, level, m->fractal, m->newton, s),
+            s, true);
+    return finish(launch_under_sampled(out, pitch, width, height, r, max_iterations, level, m->fractal,
+                                       m->julia_c[0], m->julia_c[1], s),
                   s, true);
 }
 

@@ -368,6 +368,7 @@ cudaError_t launch_under_sampled(void *out, long pitch, uint32_t w, uint32_t h, 
 
 cudaError_t launch_debug(int fractal, cudaStream_t s)
 {
+    if (fractal >= FRACTAL_NEWTON_WIRED) return cudaSuccess;  // the Newton modules' debugFractal is empty
     if (fractal == FRACTAL_JULIA)
         k_debug<FRACTAL_JULIA><<<1, 1, 0, s>>>();
     else

@@ -263,6 +263,8 @@ struct chaos_orbit {
     double2 *z64 = nullptr;
 };
 
+static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t max_iterations, chaos_orbit **out);
+
 int chaos_orbit_create(const char *center_x, const char *center_y, uint32_t bits, uint32_t max_iterations,
                        chaos_orbit **out)
 {
@@ -275,6 +277,23 @@ int chaos_orbit_create(const char *center_x, const char *center_y, uint32_t bits
     if (!bigfix_parse_hex(center_x, limbs, cx) || !bigfix_parse_hex(center_y, limbs, cy))
         return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "centre must be \"[-]I.hex\" fixed point");
     if (cx.w[limbs] > 4 || cy.w[limbs] > 4) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "centre outside |c| < 4");
+    return orbit_compute(cx, cy, limbs, max_iterations, out);
+}
+
+namespace chaos {
+// The orbit of a binary64 centre (the batch's perturbation viewports).
+int api_orbit_create_d(double center_x, double center_y, uint32_t bits, uint32_t max_iterations, chaos_orbit **out)
+{
+    if (!std::isfinite(center_x) || !std::isfinite(center_y) || std::fabs(center_x) >= 4 || std::fabs(center_y) >= 4)
+        return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "centre outside |c| < 4");
+    const int limbs = (int)((std::min(std::max(bits, 64u), 64u * BIGFIX_MAX_LIMBS) + 63) / 64);
+    return orbit_compute(bigfix_from_double(center_x, limbs), bigfix_from_double(center_y, limbs), limbs,
+                         max_iterations, out);
+}
+}  // namespace chaos
+
+static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t max_iterations, chaos_orbit **out)
+{
 
     std::vector<double2> z64;
     z64.reserve(std::min<uint32_t>(max_iterations, 1u << 20) + 1);

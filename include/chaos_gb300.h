@@ -81,7 +81,11 @@ typedef struct chaos_pixel_info {
 
 typedef struct chaos_module chaos_module;
 
-/* Open the module of a registered fractal ("mandelbrot", "julia").
+/* Open the module of a registered fractal: "mandelbrot", "julia",
+ * "newton_wired" / "newton wired", "newton_generic" / "newton generic",
+ * "newton_iterations" / "newton colored by iterations" (module file name or
+ * the name the Java GUI shows).  The Newton modules' kernels always use
+ * rounded arithmetic (the `arith` argument does not apply to them).
  * Replaces FractalRenderingModule.initialize (J/cudarenderer/
  * FractalRenderingModule.java:73-100) + CudaFractalRendererProvider.getRenderer
  * (J/cudarenderer/CudaFractalRendererProvider.java:47-66). */
@@ -94,10 +98,15 @@ const char *chaos_module_fractal_name(const chaos_module *m);
 
 /* Write a module constant by name, size must equal the symbol's size
  * ("VISUALIZE_SAMPLE_COUNT": 1 byte, gen.cu:14; "julia_c": 2 doubles,
- * julia.cu:3).  Replaces writeToConstantMemory (FractalRenderingModule.java:163-227). */
+ * julia.cu:3; "roots": 6 doubles, "coefficients": 4 doubles (c0..c3),
+ * newton_generic.cu:7-8; "colorMagnifier": int, newton_iterations.cu:9).
+ * Replaces writeToConstantMemory (FractalRenderingModule.java:163-227). */
 int chaos_module_write_constant(chaos_module *m, const char *name, const void *src, size_t size);
-/* Fractal custom parameters as the GUI sends them, e.g. "-0.4;0.6" for Julia
- * (ModuleJulia.setFractalCustomParameters, J/cudarenderer/modules/ModuleJulia.java:28-37). */
+/* Fractal custom parameters as the GUI sends them: "-0.4;0.6" for Julia
+ * (ModuleJulia.setFractalCustomParameters, J/cudarenderer/modules/ModuleJulia.java:28-37);
+ * {"coefficients": [a3, a2, a1, a0], "roots": [[re, im], [re, im], [re, im]],
+ * "colorMagnifier": n} for the generic Newton modules
+ * (ModuleNewtonGeneric.java:30-65, ModuleNewtonIterations.java:15-24). */
 int chaos_module_set_custom_params(chaos_module *m, const char *text);
 /* Default view of the module (supplyDefaultValues, ModuleMandelbrot.java:20-25,
  * ModuleJulia.java:40-49): centre, zoom (plane height), maxIterations, maxSS. */

@@ -38,17 +38,32 @@ def _host_machine():
     return {"x86_64": 62, "aarch64": 183, "arm64": 183}.get(platform.machine())
 
 
+def _cuda_include():
+    for d in (os.environ.get("CUDA_HOME", ""), "/usr/local/cuda"):
+        if d and os.path.isdir(os.path.join(d, "include")):
+            return os.path.join(d, "include")
+    return "/usr/local/cuda/include"
+
+
 def build_oracle():
     os.makedirs(BUILD, exist_ok=True)
     src = os.path.join(HERE, "chaos_oracle.c")
+    src_cpp = os.path.join(HERE, "newton_oracle.cpp")
     out = os.path.join(BUILD, "libchaos_oracle.so")
-    if not (os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src)
-            and _elf_machine(out) == _host_machine()):
+    newest = max(os.path.getmtime(src), os.path.getmtime(src_cpp))
+    if not (os.path.exists(out) and os.path.getmtime(out) >= newest and _elf_machine(out) == _host_machine()):
         # fma()/fmaf() are exact on either CPU; -mfma only makes them one
         # instruction on x86-64 (-ffp-contract=off still forbids contraction).
         isa = ["-mfma"] if platform.machine() == "x86_64" else []
+        inc = _cuda_include()
+        obj_c = os.path.join(BUILD, "chaos_oracle.o")
+        obj_cpp = os.path.join(BUILD, "newton_oracle.o")
         _run([os.environ.get("CC", "gcc"), "-O2", "-ffp-contract=off", "-fno-fast-math", *isa, "-fopenmp", "-fPIC",
-              "-shared", "-std=c11", src, "-o", out, "-lm"])
+              "-std=c11", "-c", src, "-o", obj_c])
+        # thrust::complex on the host, from the CUDA toolkit's headers
+        _run([os.environ.get("CXX", "g++"), "-O2", "-ffp-contract=off", "-fno-fast-math", *isa, "-fPIC",
+              "-std=c++17", "-I", inc, "-I", os.path.join(inc, "cccl"), "-c", src_cpp, "-o", obj_cpp])
+        _run([os.environ.get("CXX", "g++"), "-shared", "-fopenmp", obj_c, obj_cpp, "-o", out, "-lm"])
     return out
 
 
@@ -64,7 +79,9 @@ def build_reference():
     if not have_src:
         return None
     lib = os.path.join(REF_OUT, "libchaos_ref.so")
-    cubins = [os.path.join(REF_OUT, f"ref_{f}{s}.cubin") for f in ("mandelbrot", "julia") for s in ("", "_nofma")]
+    cubins = [os.path.join(REF_OUT, f"ref_{f}{s}.cubin")
+              for f in ("mandelbrot", "julia", "newton_wired", "newton_generic", "newton_iterations")
+              for s in ("", "_nofma")]
     need_host = _elf_machine(lib) != _host_machine()
     need_cubin = not all(os.path.exists(c) for c in cubins)
     if need_host or need_cubin or os.path.isdir(os.path.join(ref_root, "src")):

@@ -20,7 +20,9 @@ C="$REF/src/main/cuda"
 mkdir -p "$OUT/src/fractals"
 if [ -f "$C/fractalRendererGeneric.cu" ]; then
   cp "$C/helpers.cuh" "$OUT/src/helpers.cuh"
-  for f in fractal.cuh mandelbrot.cu julia.cu; do cp "$C/fractals/$f" "$OUT/src/fractals/$f"; done
+  for f in fractal.cuh mandelbrot.cu julia.cu newton_wired.cu newton_generic.cu newton_iterations.cu; do
+    cp "$C/fractals/$f" "$OUT/src/fractals/$f"
+  done
   sed 's/relative_in_old\.cast<float>()/relative_in_old.template cast<float>()/' \
     "$C/fractalRendererGeneric.cu" > "$OUT/src/fractalRendererGeneric.cu"
 fi
@@ -31,11 +33,12 @@ fi
 CXX="${CXX:-g++}"
 # -Dlb=lt -Drt=rb: the Rectangle(Point lt, Point rb) constructor at helpers.cuh:83
 # names lb/rt, which do not exist; nvcc never instantiates it, g++ parses it.
+CUDA_INC="${CUDA_HOME:-/usr/local/cuda}/include"
 "$CXX" -O2 -ffp-contract=off -fopenmp -fPIC -shared -DNDEBUG -Dlb=lt -Drt=rb \
-  -I"$HERE" -I"$OUT/src" "$HERE/ref_host.cpp" -o "$OUT/libchaos_ref.so"
+  -I"$HERE" -I"$OUT/src" -I"$CUDA_INC" -I"$CUDA_INC/cccl" "$HERE/ref_host.cpp" -o "$OUT/libchaos_ref.so"
 if [ "${SKIP_CUBIN:-0}" != "1" ]; then
   NVCC="${NVCC:-nvcc}"
-  for f in mandelbrot julia; do
+  for f in mandelbrot julia newton_wired newton_generic newton_iterations; do
     printf '#include "fractals/%s.cu"\n#include "fractalRendererGeneric.cu"\n' "$f" > "$OUT/src/ref_$f.cu"
     "$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -DNDEBUG -I"$OUT/src" \
       "$OUT/src/ref_$f.cu" -o "$OUT/ref_$f.cubin" &
@@ -43,7 +46,7 @@ if [ "${SKIP_CUBIN:-0}" != "1" ]; then
       "$OUT/src/ref_$f.cu" -o "$OUT/ref_${f}_nofma.cubin" &
   done
   wait
-  for f in mandelbrot julia; do
+  for f in mandelbrot julia newton_wired newton_generic newton_iterations; do
     [ -s "$OUT/ref_$f.cubin" ] && [ -s "$OUT/ref_${f}_nofma.cubin" ] || { echo "cubin build failed" >&2; exit 4; }
   done
 fi

@@ -31,7 +31,23 @@ typedef struct {
     float weight_of_new_samples;
 } orc_pixel_info; /* pixel_info_t, src/main/cuda/helpers.cuh:106-130 (16 bytes) */
 
-enum { ORC_MANDELBROT = 0, ORC_JULIA = 1 };
+enum { ORC_MANDELBROT = 0, ORC_JULIA = 1 }; /* 2..4: the Newton modules (newton_oracle.cpp) */
+
+/* Newton modules' constants (roots, coefficients c0..c3, colorMagnifier). */
+static double g_newton_roots[6] = {1, 0, -0.5, 0.86602540378, -0.5, -0.86602540378};
+static double g_newton_coeffs[4] = {-1, 0, 0, 1};
+static int g_newton_magnifier = 11;
+
+void orc_set_newton(const double roots[6], const double coeffs[4], int magnifier)
+{
+    memcpy(g_newton_roots, roots, sizeof g_newton_roots);
+    memcpy(g_newton_coeffs, coeffs, sizeof g_newton_coeffs);
+    g_newton_magnifier = magnifier;
+}
+
+float orc_newton_compute_f(int fractal, uint32_t max_iter, float x, float y, const double *roots, const double *coeffs);
+float orc_newton_compute_d(int fractal, uint32_t max_iter, double x, double y, const double *roots,
+                           const double *coeffs);
 enum { ORC_ARITH_FMA = 0, ORC_ARITH_PARITY = 1 }; /* same numbering as CHAOS_ARITH_* */
 
 /* kernel flag bits, gen.cu:157-161 */
@@ -125,6 +141,7 @@ float orc_compute_fractal_f(int fractal, int arith, uint32_t max_iter, float px,
 {
     float r2;
     uint32_t i;
+    if (fractal >= 2) return orc_newton_compute_f(fractal, max_iter, px, py, g_newton_roots, g_newton_coeffs);
     if (fractal == ORC_MANDELBROT) {
         i = arith == ORC_ARITH_FMA ? esc_fma_f(max_iter, 0.f, 0.f, px, py, &r2)
                                    : esc_parity_f(max_iter, 0.f, 0.f, px, py, &r2);
@@ -141,6 +158,7 @@ float orc_compute_fractal_d(int fractal, int arith, uint32_t max_iter, double px
 {
     double r2;
     uint32_t i;
+    if (fractal >= 2) return orc_newton_compute_d(fractal, max_iter, px, py, g_newton_roots, g_newton_coeffs);
     if (fractal == ORC_MANDELBROT) {
         i = arith == ORC_ARITH_FMA ? esc_fma_d(max_iter, 0.0, 0.0, px, py, &r2)
                                    : esc_parity_d(max_iter, 0.0, 0.0, px, py, &r2);
@@ -1167,4 +1185,25 @@ uint64_t orc_batch_viewport(const orc_viewport *v, uint32_t *counts, float *smoo
         if (rgba) rgba[q] = pack_mean_rgba(acc, v->spp);
     }
     return total;
+}
+
+/* compose with a module's colouring: mode 0 palette (mandelbrot/julia), 1 one
+ * colour per root (newton_wired.cu:67-80, newton_generic.cu:75-88), 2 palette
+ * with stride colorMagnifier (newton_iterations.cu:70-78). */
+void orc_compose_mode(const void *in, long pitch, uint32_t *out, long out_pitch, uint32_t w, uint32_t h,
+                      const uint32_t *palette, uint32_t palette_len, int mode, int magnifier)
+{
+    for (uint32_t y = 0; y < h; y++) {
+        for (uint32_t x = 0; x < w; x++) {
+            const orc_pixel_info *p = pixel_at((void *)in, pitch, x, y);
+            uint32_t vi = (uint32_t)roundf(p->value), color;
+            if (mode == 1)
+                color = vi == 1 ? 0xff0000ffu : vi == 2 ? 0xff00ff00u : vi == 3 ? 0xffff0000u : 0xff000000u;
+            else if (mode == 2)
+                color = palette[palette_len - (vi * (uint32_t)magnifier % palette_len) - 1];
+            else
+                color = palette[palette_len - (vi % palette_len) - 1];
+            *(uint32_t *)((char *)out + (size_t)y * (size_t)out_pitch + 4 * (size_t)x) = color;
+        }
+    }
 }

@@ -86,6 +86,11 @@ class Oracle:
         L.orc_hp_escape_batch.restype = None
         L.orc_hp_escape_batch.argtypes = [C.c_char_p, C.c_char_p, C.c_long, C.c_void_p, C.c_void_p, C.c_uint32,
                                           C.c_uint32, C.c_void_p, C.c_void_p]
+        L.orc_set_newton.restype = None
+        L.orc_set_newton.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        L.orc_compose_mode.restype = None
+        L.orc_compose_mode.argtypes = [C.c_void_p, C.c_long, C.c_void_p, C.c_long, C.c_uint32, C.c_uint32,
+                                       C.c_void_p, C.c_uint32, C.c_int, C.c_int]
         L.orc_batch_viewport.restype = C.c_uint64
         L.orc_batch_viewport.argtypes = [C.POINTER(Viewport), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_uint32, C.c_uint32]
@@ -206,6 +211,22 @@ class Oracle:
                                             len(pal) if pal is not None else 0, interior_rgba)
         return {"total": int(total), "counts": counts, "smooth": sm, "rgba": rgba}
 
+    def set_newton(self, roots=(1, 0, -0.5, 0.86602540378, -0.5, -0.86602540378), coefficients=(-1, 0, 0, 1),
+                   magnifier=11):
+        """The Newton modules' constants: roots (re, im) x3, coefficients c0..c3, colorMagnifier."""
+        r = np.ascontiguousarray(roots, dtype=np.float64)
+        c = np.ascontiguousarray(coefficients, dtype=np.float64)
+        self.lib.orc_set_newton(_ptr(r), _ptr(c), magnifier)
+
+    def compose_mode(self, pix, palette, mode, magnifier=1):
+        pix = np.ascontiguousarray(pix)
+        h, w = pix.shape
+        pal = np.ascontiguousarray(palette if palette is not None else [0], dtype=np.uint32)
+        out = np.zeros((h, w), dtype=np.uint32)
+        self.lib.orc_compose_mode(_ptr(pix), pix.strides[0], _ptr(out), out.strides[0], w, h, _ptr(pal), len(pal),
+                                  mode, magnifier)
+        return out
+
     def max_threads(self):
         return self.lib.orc_max_threads()
 
@@ -235,6 +256,14 @@ class Reference:
         L.ref_mandelbrot_points_d.restype = C.c_ulonglong
         L.ref_mandelbrot_points_d.argtypes = [C.c_size_t, C.c_void_p, C.c_void_p, C.c_uint, C.c_int, C.c_void_p]
         L.ref_max_threads.restype = C.c_int
+        L.ref_newton_set.restype = None
+        L.ref_newton_set.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        L.ref_newton_f.restype = C.c_float
+        L.ref_newton_f.argtypes = [C.c_int, C.c_uint, C.c_float, C.c_float]
+        L.ref_newton_d.restype = C.c_float
+        L.ref_newton_d.argtypes = [C.c_int, C.c_uint, C.c_double, C.c_double]
+        L.ref_newton_colorize.restype = C.c_uint
+        L.ref_newton_colorize.argtypes = [C.c_int, C.c_void_p, C.c_uint, C.c_float]
 
     def mandelbrot(self, dbl, max_iter, x, y):
         return (self.lib.ref_mandelbrot_d if dbl else self.lib.ref_mandelbrot_f)(max_iter, x, y)
@@ -294,6 +323,18 @@ class Reference:
 
     def max_threads(self):
         return self.lib.ref_max_threads()
+
+    def newton_set(self, roots, coefficients, magnifier):
+        r = np.ascontiguousarray(roots, dtype=np.float64)
+        c = np.ascontiguousarray(coefficients, dtype=np.float64)
+        self.lib.ref_newton_set(_ptr(r), _ptr(c), magnifier)
+
+    def newton(self, kind, dbl, max_iter, x, y):
+        return (self.lib.ref_newton_d if dbl else self.lib.ref_newton_f)(kind, max_iter, x, y)
+
+    def newton_colorize(self, kind, palette, value):
+        pal = np.ascontiguousarray(palette, dtype=np.uint32)
+        return self.lib.ref_newton_colorize(kind, _ptr(pal), len(pal), value)
 
 
 def c1_grid():

@@ -11,15 +11,30 @@
 #include "ref_prelude.h"
 
 #include <omp.h>
+// The Newton modules include thrust/complex.h themselves; included here first,
+// at global scope, their include is a no-op inside the namespaces below.
+#include <thrust/complex.h>
 
 namespace ref_mandelbrot {
 #include "fractals/mandelbrot.cu"
 }
-/* helpers.cuh is guarded by HELPERS; clear the guard so the second
+/* helpers.cuh is guarded by HELPERS; clear the guard so each following
  * namespace gets its own copy of Point/Rectangle. */
 #undef HELPERS
 namespace ref_julia {
 #include "fractals/julia.cu"
+}
+#undef HELPERS
+namespace ref_newton_wired {
+#include "fractals/newton_wired.cu"
+}
+#undef HELPERS
+namespace ref_newton_generic {
+#include "fractals/newton_generic.cu"
+}
+#undef HELPERS
+namespace ref_newton_iterations {
+#include "fractals/newton_iterations.cu"
 }
 
 extern "C" {
@@ -103,4 +118,43 @@ unsigned long long ref_mandelbrot_points_d(size_t n, const double *x, const doub
 }
 
 int ref_max_threads(void) { return omp_get_max_threads(); }
+
+/* The Newton modules' constants (roots as (re, im) x3, coefficients c0..c3,
+ * colorMagnifier), as writeToConstantMemory would set them. */
+void ref_newton_set(const double *roots, const double *coeffs, int magnifier)
+{
+    for (int k = 0; k < 3; k++) {
+        ref_newton_generic::roots[k] = ref_newton_generic::Point<double>(roots[2 * k], roots[2 * k + 1]);
+        ref_newton_iterations::roots[k] = ref_newton_iterations::Point<double>(roots[2 * k], roots[2 * k + 1]);
+    }
+    for (int k = 0; k < 4; k++) {
+        ref_newton_generic::coefficients[k] = coeffs[k];
+        ref_newton_iterations::coefficients[k] = coeffs[k];
+    }
+    ref_newton_iterations::colorMagnifier = magnifier;
+}
+
+/* kind: 2 wired, 3 generic, 4 iterations */
+float ref_newton_f(int kind, unsigned max_iter, float x, float y)
+{
+    if (kind == 2) return ref_newton_wired::computeFractal<float>(max_iter, ref_newton_wired::Point<float>(x, y));
+    if (kind == 3) return ref_newton_generic::computeFractal<float>(max_iter, ref_newton_generic::Point<float>(x, y));
+    return ref_newton_iterations::computeFractal<float>(max_iter, ref_newton_iterations::Point<float>(x, y));
+}
+
+float ref_newton_d(int kind, unsigned max_iter, double x, double y)
+{
+    if (kind == 2) return ref_newton_wired::computeFractal<double>(max_iter, ref_newton_wired::Point<double>(x, y));
+    if (kind == 3)
+        return ref_newton_generic::computeFractal<double>(max_iter, ref_newton_generic::Point<double>(x, y));
+    return ref_newton_iterations::computeFractal<double>(max_iter, ref_newton_iterations::Point<double>(x, y));
+}
+
+unsigned ref_newton_colorize(int kind, const unsigned *palette, unsigned len, float value)
+{
+    cudaSurfaceObject_t s = (cudaSurfaceObject_t)(uintptr_t)palette;
+    if (kind == 2) return ref_newton_wired::colorize(s, len, value);
+    if (kind == 3) return ref_newton_generic::colorize(s, len, value);
+    return ref_newton_iterations::colorize(s, len, value);
+}
 }

@@ -76,6 +76,28 @@ def main():
     out["default_palette_sha256"] = hashlib.sha256(pal.astype("<u4").tobytes()).hexdigest()
     out["colorize_default_palette"] = [{"value": v, "rgba": int(ref.colorize(pal, v))} for v in vals]
 
+    # Newton modules: default parameters and the other set the reference suggests
+    # (ModuleNewtonGeneric.java:67-74), coefficients stored c0..c3
+    newton_params = [
+        {"roots": [1, 0, -0.5, 0.86602540378, -0.5, -0.86602540378], "coefficients": [-1, 0, 0, 1], "magnifier": 11},
+        {"roots": [-1.7692923542386314, 0, 0.884646177119315707620204, 0.589742805022205501647280,
+                   0.884646177119315707, -0.589742805022205501], "coefficients": [2, -2, 0, 1], "magnifier": 7},
+    ]
+    newton = []
+    for pi, prm in enumerate(newton_params):
+        ref.newton_set(prm["roots"], prm["coefficients"], prm["magnifier"])
+        for kind in (2, 3, 4):
+            for _ in range(48):
+                x, y = float(rng.uniform(-2, 2)), float(rng.uniform(-1.5, 1.5))
+                newton.append({"params": pi, "kind": kind, "x": x, "y": y, "max_iter": 200,
+                               "f32": ref.newton(kind, 0, 200, np.float32(x), np.float32(y)),
+                               "f64": ref.newton(kind, 1, 200, x, y)})
+    out["newton_params"] = newton_params
+    out["newton_points"] = newton
+    ref.newton_set(newton_params[0]["roots"], newton_params[0]["coefficients"], 11)
+    out["newton_colorize"] = [{"kind": k, "value": float(v), "rgba": int(ref.newton_colorize(k, pal, float(v)))}
+                              for k in (2, 3, 4) for v in list(range(0, 6)) + [17.0, 99.0, 1234.0]]
+
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_golden.json")
     with open(path, "w") as f:
         json.dump(out, f, indent=1)

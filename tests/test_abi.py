@@ -37,7 +37,8 @@ def test_version_and_fractals(native):
     import chaos_gb300 as cg
 
     assert "sm_103a" in cg.version()
-    assert cg.available_fractals() == ["mandelbrot", "julia"]
+    assert cg.available_fractals() == ["mandelbrot", "julia", "newton wired", "newton generic",
+                                       "newton colored by iterations"]
 
 
 def test_module_registry(native):
@@ -201,3 +202,34 @@ def test_struct_layouts_match_header(native, tmp_path):
         assert got[(cname, "size")] == C.sizeof(py), cname
         for f, _ in py._fields_:
             assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+def test_newton_module_params(native):
+    import chaos_gb300 as cg
+    for name, shown in (("newton_generic", "newton generic"), ("newton colored by iterations",
+                                                              "newton colored by iterations")):
+        m = cg.Module(name)
+        assert m.fractal_name == shown
+        assert m.default_view()[3] == 200
+        m.set_custom_params('{ "coefficients" : [1, 0, -2, 2], "roots" : [ [-1.7692923542386314,0], '
+                            '[0.884646177119315707620204,0.589742805022205501647280] , '
+                            '[0.884646177119315707,-0.589742805022205501] ] }')
+        for bad, msg in (('{"coefficients": [1, 2, 3], "roots": [[1,0],[2,0],[3,0]]}', "4 coefficients"),
+                         ('{"coefficients": [1, 2, 3, 4], "roots": [[1,0],[2,0]]}', "3 roots"),
+                         ('{"coefficients": [1, 2, 3, 4], "roots": [[1,0],[2],[3,0]]}', "[real, imag]"),
+                         ('not json', "JSON")):
+            with pytest.raises(cg.ChaosError) as e:
+                m.set_custom_params(bad)
+            assert msg in e.value.message
+        m.write_constant("roots", np.zeros(6).tobytes())
+        m.write_constant("coefficients", np.zeros(4).tobytes())
+        with pytest.raises(cg.ChaosError):
+            m.write_constant("roots", np.zeros(3).tobytes())
+    it = cg.Module("newton_iterations")
+    it.write_constant("colorMagnifier", np.int32(5).tobytes())
+    it.set_custom_params('{"colorMagnifier": 3, "coefficients": [1, 0, 0, -1], "roots": [[1,0],[-0.5,0.8],[-0.5,-0.8]]}')
+    w = cg.Module("newton wired")
+    w.set_custom_params("anything")  # ModuleNewtonWired ignores its parameters
+    with pytest.raises(cg.ChaosError) as e:
+        w.write_constant("roots", np.zeros(6).tobytes())
+    assert e.value.code == 4

@@ -90,3 +90,29 @@ def test_oracle_matches_reference_live(oracle, reference):
             xv, yv = (x, y) if dbl else (np.float32(x), np.float32(y))
             assert oracle.compute_fractal(JULIA, dbl, ARITH_PARITY, 300, xv, yv, c) == reference.julia(dbl, 300, xv,
                                                                                                       yv, c)
+
+
+def test_newton_points(oracle, golden):
+    bad = []
+    prms = golden["newton_params"]
+    for p in golden["newton_points"]:
+        prm = prms[p["params"]]
+        oracle.set_newton(prm["roots"], prm["coefficients"], prm["magnifier"])
+        f = oracle.compute_fractal(p["kind"], 0, 1, p["max_iter"], np.float32(p["x"]), np.float32(p["y"]))
+        d = oracle.compute_fractal(p["kind"], 1, 1, p["max_iter"], p["x"], p["y"])
+        if f != p["f32"] or d != p["f64"]:
+            bad.append((p, f, d))
+    oracle.set_newton()
+    assert len(golden["newton_points"]) == 288 and not bad, bad[:5]
+
+
+def test_newton_colorize(oracle, golden):
+    from chaos_gb300.palette import default_palette
+    from oracle.oracle import PIXEL_DTYPE
+    pal = default_palette()
+    for kind, mode, mag in ((2, 1, 1), (3, 1, 1), (4, 2, 11)):
+        cases = [c for c in golden["newton_colorize"] if c["kind"] == kind]
+        pix = np.zeros((1, len(cases)), dtype=PIXEL_DTYPE)
+        pix["value"][0] = [c["value"] for c in cases]
+        got = oracle.compose_mode(pix, pal, mode, mag)[0]
+        assert got.tolist() == [c["rgba"] for c in cases], kind
