@@ -461,9 +461,30 @@ def run_batch(args):
     torch.cuda.synchronize()
     plain_ms = s0.elapsed_time(s1)
     plain_value = plain.read_total() / (plain_ms / 1e3) / 1e9
-    diff = sum(int((a != c.cpu().numpy()).sum()) for a, (c, _) in zip(tiered_counts, pbufs))
+    plain_counts = [c.cpu().numpy() for c, _ in pbufs]
+    diff = sum(int((a != c).sum()) for a, c in zip(tiered_counts, plain_counts))
     total = sum(len(a) for a in tiered_counts)
+    plain.close()
     del plain, pbufs
+
+    # binary32 / float-float / perturbation (the deep viewports on reference orbits)
+    deep, dbufs = make(cg.TIER_AUTO_DEEP)
+    deep.launch(stream)
+    torch.cuda.synchronize()
+    deep_ms = []
+    for k in range(2):
+        flush(k)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        deep.launch(stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        deep_ms.append(e0.elapsed_time(e1))
+    deep_value = deep.read_total() / (min(deep_ms) / 1e3) / 1e9
+    deep_tiers = deep.tiers()
+    deep_diff = sum(int((c.cpu().numpy() != a).sum()) for (c, _), a in zip(dbufs, plain_counts))
+    deep.close()
+    del deep, dbufs, plain_counts
 
     # time per tier: the same batch restricted to one tier's viewports
     per_tier = {}
@@ -528,6 +549,12 @@ def run_batch(args):
                                  "what": "fractalRenderMainDouble semantics: binary64, rounded arithmetic, "
                                          "1 sample per pixel, per viewport"},
             "f64_fma_batch": {"value": plain_value, "ms": plain_ms, "speedup_of_tiered": value / plain_value},
+            "tiered_deep": {"value": deep_value, "ms": min(deep_ms),
+                            "tiers": {"f32": deep_tiers.count(0), "floatfloat": deep_tiers.count(2),
+                                      "perturb_f32": deep_tiers.count(3), "perturb_f64": deep_tiers.count(4)},
+                            "escape_count_mismatch_vs_f64_batch": deep_diff / total,
+                            "what": "binary32 / float-float / perturbation on per-viewport reference orbits "
+                                    "(orbits computed at batch creation, outside the timed launch)"},
             "per_tier": per_tier,
             "escape_count_mismatch_vs_f64_batch": diff / total,
             "gpu_launches": args.steps, "clocks": clk}

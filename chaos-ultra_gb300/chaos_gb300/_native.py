@@ -102,6 +102,7 @@ class BatchConfig(C.Structure):
 
 
 TIER_AUTO = 255
+TIER_AUTO_DEEP = 254
 
 
 class SessionDesc(C.Structure):

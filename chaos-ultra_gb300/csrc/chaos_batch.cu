@@ -21,6 +21,10 @@
 namespace chaos {
 
 int api_fail(int code, const char *fmt, ...);  // chaos_api.cu
+int api_orbit_create_d(double center_x, double center_y, uint32_t bits, uint32_t max_iterations,
+                       chaos_orbit **out);  // chaos_perturb.cu
+int api_perturb_enqueue(const chaos_frame_desc *desc, const chaos_orbit *orbit, const chaos_frame_out *out,
+                        cudaStream_t stream, uint32_t *counter);  // chaos_perturb.cu
 
 struct BatchViewport {
     uint32_t w, h, spp, mode, max_iter;
@@ -266,9 +270,17 @@ constexpr int kTiers = 3;  // 0 binary32, 1 float-float, 2 binary64
 int tier_slot(uint32_t tier) { return tier == CHAOS_TIER_F32 ? 0 : tier == CHAOS_TIER_FLOATFLOAT ? 1 : 2; }
 }  // namespace
 
+// A viewport of the batch rendered by perturbation (its own reference orbit).
+struct PerturbJob {
+    chaos_frame_desc desc{};
+    chaos_frame_out out{};
+    chaos_orbit *orbit = nullptr;
+};
+
 struct chaos_batch {
     int device = -1;
     std::vector<uint32_t> tiers;  // chosen tier per viewport
+    std::vector<PerturbJob> perturb;
     BatchViewport *d_vps[kTiers] = {nullptr, nullptr, nullptr};
     uint32_t n_vp[kTiers] = {0, 0, 0}, n_jobs[kTiers] = {0, 0, 0};
     uint32_t *d_counters = nullptr;
@@ -290,25 +302,43 @@ uint32_t chaos_batch_auto_tier(double center_x, double center_y, double pixel_si
     return CHAOS_TIER_F64;
 }
 
+static uint32_t auto_deep_tier(double center_x, double center_y, double pixel_size)
+{
+    uint32_t t = chaos_batch_auto_tier(center_x, center_y, pixel_size);
+    if (t != CHAOS_TIER_F64) return t;
+    return pixel_size >= 1e-30 ? CHAOS_TIER_PERTURB_F32 : CHAOS_TIER_PERTURB_F64;
+}
+
 static void batch_free(chaos_batch *b)
 {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     for (int t = 0; t < kTiers; t++)
         if (b->d_vps[t]) cudaFree(b->d_vps[t]);
+    for (PerturbJob &j : b->perturb)
+        if (j.orbit) chaos_orbit_destroy(j.orbit);
     if (b->d_counters) cudaFree(b->d_counters);
     if (b->d_total) cudaFree(b->d_total);
     delete b;
 }
 
-static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s1, cudaStream_t s2, cudaEvent_t fork,
-                                 cudaEvent_t j1, cudaEvent_t j2)
+// *rc: the status of a perturbation enqueue that failed (its message is the last error)
+static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s1, cudaStream_t s2, cudaStream_t s3,
+                                 cudaEvent_t fork, cudaEvent_t j1, cudaEvent_t j2, cudaEvent_t j3, int *rc)
 {
-    cudaError_t e = cudaMemsetAsync(b->d_counters, 0, kTiers * sizeof(uint32_t), s0);
+    // work counters: one per tier kernel, then one per perturbation viewport
+    cudaError_t e = cudaMemsetAsync(b->d_counters, 0, (kTiers + b->perturb.size()) * sizeof(uint32_t), s0);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_total, 0, sizeof(unsigned long long), s0);
     if (e == cudaSuccess) e = cudaEventRecord(fork, s0);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s1, fork, 0);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, fork, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s3, fork, 0);
+    // perturbation viewports, one after another on the fourth branch
+    for (size_t k = 0; k < b->perturb.size() && e == cudaSuccess; k++) {
+        PerturbJob &j = b->perturb[k];
+        *rc = api_perturb_enqueue(&j.desc, j.orbit, &j.out, s3, b->d_counters + kTiers + k);
+        if (*rc != CHAOS_OK) e = cudaErrorInvalidValue;
+    }
     cudaStream_t st[kTiers] = {s0, s1, s2};
     // binary64 first: its kernels are the longest, the cheaper tiers fill in behind
     const int order[kTiers] = {2, 1, 0};
@@ -331,8 +361,10 @@ static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s
     }
     if (e == cudaSuccess) e = cudaEventRecord(j1, s1);
     if (e == cudaSuccess) e = cudaEventRecord(j2, s2);
+    if (e == cudaSuccess) e = cudaEventRecord(j3, s3);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s0, j1, 0);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s0, j2, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s0, j3, 0);
     return e;
 }
 
@@ -357,10 +389,19 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
         if (!std::isfinite(v.center_x) || !std::isfinite(v.center_y) || !(v.pixel_size > 0) ||
             !std::isfinite(v.pixel_size))
             return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "viewport %u: centre/pixel size", k);
-        uint32_t tier = v.tier == CHAOS_TIER_AUTO ? chaos_batch_auto_tier(v.center_x, v.center_y, v.pixel_size) : v.tier;
-        if (tier != CHAOS_TIER_F32 && tier != CHAOS_TIER_FLOATFLOAT && tier != CHAOS_TIER_F64)
+        uint32_t tier = v.tier == CHAOS_TIER_AUTO        ? chaos_batch_auto_tier(v.center_x, v.center_y, v.pixel_size)
+                        : v.tier == CHAOS_TIER_AUTO_DEEP ? auto_deep_tier(v.center_x, v.center_y, v.pixel_size)
+                                                         : v.tier;
+        if (tier != CHAOS_TIER_F32 && tier != CHAOS_TIER_FLOATFLOAT && tier != CHAOS_TIER_F64 &&
+            tier != CHAOS_TIER_PERTURB_F32 && tier != CHAOS_TIER_PERTURB_F64)
             return api_fail(CHAOS_ERR_UNSUPPORTED, "viewport %u: tier %u not batchable", k, tier);
         tiers[k] = tier;
+        if (tier == CHAOS_TIER_PERTURB_F32 || tier == CHAOS_TIER_PERTURB_F64) {
+            if (tier == CHAOS_TIER_PERTURB_F32 && v.pixel_size < 1e-30)
+                return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "viewport %u: binary32 differences need pixel >= 1e-30", k);
+            any_rgba |= v.rgba != nullptr;
+            continue;  // its orbit is computed below
+        }
         int t = tier_slot(tier);
         BatchViewport bv{};
         bv.w = v.width;
@@ -404,8 +445,40 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
             }
         }
     }
-    cudaError_t e = cudaMalloc(&b->d_counters, kTiers * sizeof(uint32_t));
+    size_t n_perturb = 0;
+    for (uint32_t k = 0; k < n; k++) n_perturb += tiers[k] == CHAOS_TIER_PERTURB_F32 || tiers[k] == CHAOS_TIER_PERTURB_F64;
+    cudaError_t e = cudaMalloc(&b->d_counters, (kTiers + n_perturb) * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_total, sizeof(unsigned long long));
+    // reference orbits of the perturbation viewports (host, multi-word)
+    for (uint32_t k = 0; k < n && e == cudaSuccess; k++) {
+        if (tiers[k] != CHAOS_TIER_PERTURB_F32 && tiers[k] != CHAOS_TIER_PERTURB_F64) continue;
+        const chaos_viewport &v = vps[k];
+        PerturbJob j;
+        double bits = -std::log2(v.pixel_size) + 96.0;
+        uint32_t want = (uint32_t)std::min(1536.0, std::max(128.0, std::ceil(bits / 64.0) * 64.0));
+        int rc = api_orbit_create_d(v.center_x, v.center_y, want, v.max_iterations, &j.orbit);
+        if (rc != CHAOS_OK) {
+            batch_free(b);
+            return rc;
+        }
+        j.desc.width = v.width;
+        j.desc.height = v.height;
+        j.desc.max_iterations = v.max_iterations;
+        j.desc.samples_per_pixel = v.samples_per_pixel;
+        j.desc.sample_mode = v.sample_mode;
+        j.desc.tier = tiers[k];
+        j.desc.fractal = 0;
+        j.desc.seed = v.seed;
+        j.desc.pixel_size = v.pixel_size;
+        j.out.counts = v.counts;
+        j.out.smooth = v.smooth;
+        j.out.rgba = v.rgba;
+        j.out.palette = palette;
+        j.out.palette_len = palette_len;
+        j.out.interior_rgba = interior_rgba;
+        j.out.total_iterations = b->d_total;
+        b->perturb.push_back(j);
+    }
     for (int t = 0; t < kTiers && e == cudaSuccess; t++) {
         b->n_vp[t] = (uint32_t)per[t].size();
         b->n_jobs[t] = (uint32_t)jobs[t];
@@ -415,17 +488,20 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
             e = cudaMemcpy(b->d_vps[t], per[t].data(), per[t].size() * sizeof(BatchViewport), cudaMemcpyHostToDevice);
     }
     // capture the fork-join launch into a graph
-    cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr;
-    cudaEvent_t fork = nullptr, j1 = nullptr, j2 = nullptr;
+    cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr, s3 = nullptr;
+    cudaEvent_t fork = nullptr, j1 = nullptr, j2 = nullptr, j3 = nullptr;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s3, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j1, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j2, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j3, cudaEventDisableTiming);
+    int enqueue_rc = CHAOS_OK;
     if (e == cudaSuccess) e = cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        cudaError_t ee = batch_enqueue(b, s0, s1, s2, fork, j1, j2);
+        cudaError_t ee = batch_enqueue(b, s0, s1, s2, s3, fork, j1, j2, j3, &enqueue_rc);
         e = cudaStreamEndCapture(s0, &b->graph);
         if (ee != cudaSuccess) e = ee;
     }
@@ -433,11 +509,14 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
     if (fork) cudaEventDestroy(fork);
     if (j1) cudaEventDestroy(j1);
     if (j2) cudaEventDestroy(j2);
+    if (j3) cudaEventDestroy(j3);
+    if (s3) cudaStreamDestroy(s3);
     if (s0) cudaStreamDestroy(s0);
     if (s1) cudaStreamDestroy(s1);
     if (s2) cudaStreamDestroy(s2);
     if (e != cudaSuccess) {
         batch_free(b);
+        if (enqueue_rc != CHAOS_OK) return enqueue_rc;
         return api_fail(CHAOS_ERR_CUDA, "batch set-up: %s", cudaGetErrorString(e));
     }
     *out = b;

@@ -359,9 +359,11 @@ int chaos_orbit_destroy(chaos_orbit *o)
     return CHAOS_OK;
 }
 
+// counter: a zeroed work counter the caller owns (a batch graph), or null to
+// take one from the device's ring
 template <class D>
 static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const chaos_frame_out *o, cudaStream_t s,
-                        bool sync)
+                        bool sync, uint32_t *counter)
 {
     PerturbArgs<D> a{};
     a.w = d->width;
@@ -390,8 +392,15 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
     a.total = o->total_iterations;
     a.rebases = o->rebases;
     int sms = 0;
-    int rc = api_device_counter(s, &a.counter, &sms);
-    if (rc) return rc;
+    if (counter) {
+        a.counter = counter;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    } else {
+        int rc = api_device_counter(s, &a.counter, &sms);
+        if (rc) return rc;
+    }
     cudaError_t e = launch_perturb<D>(a, sms, s);
     if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e));
     if (sync) {
@@ -402,7 +411,7 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
 }
 
 static int perturb_entry(const chaos_frame_desc *d, const chaos_orbit *orb, const chaos_frame_out *o, cudaStream_t s,
-                         bool sync)
+                         bool sync, uint32_t *counter = nullptr)
 {
     if (!d || !orb || !o) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL argument");
     if (d->width == 0 || d->height == 0 || (uint64_t)d->width * d->height > (1ull << 31))
@@ -427,15 +436,24 @@ static int perturb_entry(const chaos_frame_desc *d, const chaos_orbit *orb, cons
         if (d->pixel_size < 1e-30)
             return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "binary32 differences need pixel size >= 1e-30 (got %g)",
                             d->pixel_size);
-        return perturb_impl<float>(d, orb, o, s, sync);
+        return perturb_impl<float>(d, orb, o, s, sync, counter);
     }
     if (d->tier == CHAOS_TIER_PERTURB_F64) {
         if (d->pixel_size < 1e-290)
             return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "binary64 differences need pixel size >= 1e-290");
-        return perturb_impl<double>(d, orb, o, s, sync);
+        return perturb_impl<double>(d, orb, o, s, sync, counter);
     }
     return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "tier %u is not a perturbation tier", d->tier);
 }
+
+namespace chaos {
+// Enqueue a perturbation frame with a work counter the caller zeroes (batch graphs).
+int api_perturb_enqueue(const chaos_frame_desc *desc, const chaos_orbit *orbit, const chaos_frame_out *out,
+                        cudaStream_t stream, uint32_t *counter)
+{
+    return perturb_entry(desc, orbit, out, stream, false, counter);
+}
+}  // namespace chaos
 
 int chaos_render_frame_perturb_async(const chaos_frame_desc *desc, const chaos_orbit *orbit,
                                      const chaos_frame_out *out, void *stream)

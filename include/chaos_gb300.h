@@ -275,7 +275,8 @@ int chaos_render_frame_host(const chaos_frame_desc *desc, const uint32_t *palett
 
 /* ---- batches: many viewports in one CUDA-graph launch -------------------- */
 
-#define CHAOS_TIER_AUTO 255
+#define CHAOS_TIER_AUTO 255      /* binary32 / float-float / binary64 by pixel size */
+#define CHAOS_TIER_AUTO_DEEP 254 /* binary32 / float-float / perturbation where AUTO would pick binary64 */
 
 /* One viewport of a batch.  Samples as in chaos_frame_desc (the plane point is
  * computed in binary64, then rounded to the viewport's tier).  Outputs are
@@ -286,7 +287,7 @@ typedef struct chaos_viewport {
     uint32_t max_iterations;
     uint32_t samples_per_pixel;
     uint32_t sample_mode;
-    uint32_t tier; /* CHAOS_TIER_F32, _FLOATFLOAT, _F64 or CHAOS_TIER_AUTO */
+    uint32_t tier; /* CHAOS_TIER_F32, _FLOATFLOAT, _F64, _PERTURB_F32, _PERTURB_F64, _AUTO or _AUTO_DEEP */
     uint64_t seed;
     double center_x, center_y, pixel_size;
     uint32_t *counts;
@@ -307,7 +308,10 @@ typedef struct chaos_batch chaos_batch;
  * 2^-18 m, float-float down to 2^-42 m, binary64 below (m = max(|cx|, |cy|, 1/256)). */
 uint32_t chaos_batch_auto_tier(double center_x, double center_y, double pixel_size);
 /* Upload the viewport table and build one CUDA graph: a memset of the work
- * counters, then one persistent kernel per tier present, forked and joined. */
+ * counters, then one persistent kernel per tier present, forked and joined;
+ * perturbation viewports get a reference orbit each (computed here, on the
+ * host, at -log2(pixel) + 96 bits) and run one after another on a fourth
+ * branch of the graph. */
 int chaos_batch_create(const chaos_viewport *viewports, uint32_t n, const uint32_t *palette, uint32_t palette_len,
                        uint32_t interior_rgba, const chaos_batch_config *config, chaos_batch **out);
 /* One cudaGraphLaunch on `stream` (does not synchronise). */

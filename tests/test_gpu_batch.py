@@ -90,3 +90,115 @@ def test_batch_rejects_bad_config(cuda):
         build(cuda, VIEWS[:2], seeded_palette(16), cg.BatchConfig((100, 0, 0), (0, 0, 0)))
     with pytest.raises(cg.ChaosError):
         build(cuda, VIEWS[:2], seeded_palette(16), cg.BatchConfig((0, 0, 0), (12, 0, 0)))
+
+
+DEEP_VIEWS = [
+    (64, 36, 1, 0, 600, 254, (-0.5, 0.0), 3.0),                                 # auto-deep -> binary32
+    (48, 32, 1, 1, 2000, 254, (-0.748, 0.1), 1.4e-5),                           # auto-deep -> float-float
+    (80, 45, 1, 1, 3000, 254, (-0.74364388703715, 0.13182590420531), 8e-12),    # auto-deep -> perturbation, binary32
+    (40, 24, 2, 1, 3000, 4, (0.0, 1.0), 4e-36),                                   # forced perturbation, binary64 (c = i)
+]
+
+
+def orbit_bits(ps):
+    """The orbit precision a batch picks for a perturbation viewport: -log2(pixel) + 96 bits, in 64-bit words."""
+    import math
+    return int(min(1536, max(128, math.ceil((-math.log2(ps) + 96) / 64) * 64)))
+
+
+def test_batch_perturbation_matches_single_frames(cuda):
+    """Perturbation viewports inside a batch graph give the same bits as the
+    single-frame perturbation entry point with an orbit of the same centre and
+    precision (that entry point is held to the multi-word oracle by its own
+    tests); the other tiers still match plain batches."""
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import seeded_palette
+    torch = cuda
+    pal = seeded_palette(128, seed=9)
+    b, bufs, dpal = build(cuda, DEEP_VIEWS, pal)
+    tiers = b.tiers()
+    assert tiers == [cg.TIER_F32, cg.TIER_FLOATFLOAT, cg.TIER_PERTURB_F32, cg.TIER_PERTURB_F64]
+    got = run(cuda, b, bufs)
+    for k in (2, 3):
+        w, h, spp, mode, mi, _, c, span = DEEP_VIEWS[k]
+        ps = span / w
+        bits = orbit_bits(ps)
+        orbit = cg.Orbit(cg.to_hex_fixed(c[0], bits), cg.to_hex_fixed(c[1], bits), bits, mi)
+        counts = torch.zeros(w * h * spp, dtype=torch.int32, device="cuda:0")
+        smooth = torch.zeros(w * h * spp, dtype=torch.float32, device="cuda:0")
+        rgba = torch.zeros(w * h, dtype=torch.int32, device="cuda:0")
+        out = cg.FrameOut(counts=counts.data_ptr(), smooth=smooth.data_ptr(), rgba=rgba.data_ptr(),
+                          palette=dpal.data_ptr(), palette_len=len(pal), interior_rgba=0xFF000000)
+        desc = cg.FrameDesc(width=w, height=h, max_iterations=mi, samples_per_pixel=spp, sample_mode=mode,
+                            tier=tiers[k], fractal=cg.MANDELBROT, seed=17 + w, pixel_size=ps)
+        cg.render_frame_perturb(desc, orbit, out)
+        orbit.close()
+        gc, gs, gr = got[k]
+        assert np.array_equal(gc, counts.cpu().numpy().view(np.uint32)), k
+        assert np.array_equal(gs.view(np.uint32), smooth.cpu().numpy().view(np.uint32)), k
+        assert np.array_equal(gr, rgba.cpu().numpy().view(np.uint32)), k
+        assert len(np.unique(gc)) > 4, k  # the view shows structure
+    # the shallow viewports equal the same viewports in a plain batch
+    b2, bufs2, _ = build(cuda, [v[:5] + (255,) + v[6:] for v in DEEP_VIEWS[:2]], pal)
+    ref = run(cuda, b2, bufs2)
+    for (c1, _, r1), (c2, _, r2) in zip(got[:2], ref):
+        assert np.array_equal(c1, c2) and np.array_equal(r1, r2)
+    assert b.read_total() == sum(int(c.astype(np.int64).sum()) for c, _, _ in got)
+    again = run(cuda, b, bufs)
+    for (c1, _, _), (c2, _, _) in zip(got, again):
+        assert np.array_equal(c1, c2)
+    b.close()
+    b2.close()
+
+
+def test_batch_rejects_shallow_binary32_perturbation(cuda):
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import seeded_palette
+    v = (16, 16, 1, 0, 100, cg.TIER_PERTURB_F32, (-0.74, 0.13), 1e-31 * 16)
+    with pytest.raises(cg.ChaosError):
+        build(cuda, [v], seeded_palette(16))
+
+
+def test_c4_deep_viewports_against_multiword_oracle(cuda, oracle):
+    """The C4 viewports that plain tier choice sends to binary64 (pixel below
+    |c| * 2^-42), rendered by the binary64 tier and by perturbation, against the
+    multi-word oracle at sampled pixels.  Near the set boundary at these depths
+    binary64 iteration is itself off (the point c rounds to a double and the
+    orbit is chaotic), so the bar is that perturbation, which keeps c exact,
+    is no further from the oracle than binary64."""
+    import chaos_gb300 as cg
+    from chaos_gb300.workloads import c4_viewports
+    torch = cuda
+    specs = [s for s in c4_viewports()
+             if cg.auto_tier(s["center"][0], s["center"][1], s["span"] / s["width"]) == cg.TIER_F64]
+    assert len(specs) == 9
+    views = [(s["width"], s["height"], 1, cg.SAMPLES_CENTER, s["max_iter"], 0, s["center"], s["span"]) for s in specs]
+    rates = {}
+    for tier in (cg.TIER_F64, cg.TIER_AUTO_DEEP):
+        bufs, vps = [], []
+        for s, v in zip(specs, views):
+            counts = torch.zeros(v[0] * v[1], dtype=torch.int32, device="cuda:0")
+            bufs.append(counts)
+            vps.append(cg.Viewport(width=v[0], height=v[1], max_iterations=v[4], samples_per_pixel=1,
+                                   sample_mode=cg.SAMPLES_CENTER, tier=tier, seed=s["seed"], center_x=v[6][0],
+                                   center_y=v[6][1], pixel_size=v[7] / v[0], counts=counts.data_ptr()))
+        b = cg.Batch(vps)
+        b.launch()
+        torch.cuda.synchronize()
+        bad = n = 0
+        for s, v, counts in zip(specs, views, bufs):
+            w, h, ps = v[0], v[1], v[7] / v[0]
+            pix = np.sort(np.random.default_rng(s["seed"]).choice(w * h, 384, replace=False))
+            parts = [oracle.frame_offsets(w, h, 1, cg.SAMPLES_CENTER, s["seed"], ps, int(p), 1) for p in pix]
+            bits = orbit_bits(ps) + 64
+            want = oracle.hp_escape_batch(cg.to_hex_fixed(v[6][0], bits), cg.to_hex_fixed(v[6][1], bits),
+                                          np.concatenate([p[0] for p in parts]),
+                                          np.concatenate([p[1] for p in parts]), bits, v[4])[0]
+            got = counts.cpu().numpy().view(np.uint32)[pix]
+            bad += int((got != want).sum())
+            n += len(pix)
+        rates[tier] = bad / n
+        b.close()
+    print("c4 deep viewports, escape-count mismatch vs multi-word oracle:",
+          {"f64": rates[cg.TIER_F64], "perturbation": rates[cg.TIER_AUTO_DEEP]})
+    assert rates[cg.TIER_AUTO_DEEP] <= rates[cg.TIER_F64] + 0.01
