@@ -561,6 +561,163 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+DEEP_W, DEEP_H, DEEP_MAX_ITER, DEEP_SPANS, DEEP_ORBIT_BITS = 1920, 1080, 100000, (1e-60, 1e-200), 1088
+
+
+def run_deep(args):
+    """C3: perturbation deep zoom, 1920x1080, spans 1e-60 and 1e-200, maxIter
+    100000, centre = the committed seeded Misiurewicz point (1024-bit fixed
+    point), one sample per pixel at pixel centres.  One step = both spans'
+    frames with binary32 differences (rescaled by 2^e at these depths); the
+    reference orbit (1088 bits) is computed once, outside the timed region of
+    `value`, and inside the e2e loop."""
+    import numpy as np
+    import torch
+
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import seeded_palette
+    from chaos_gb300.workloads import deep_zoom_centre
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    d = deep_zoom_centre()
+    n = DEEP_W * DEEP_H
+    pal_host = seeded_palette(256, seed=3)
+    pal = torch.from_numpy(pal_host.view(np.int32)).to(dev)
+    rgba = torch.zeros(n, dtype=torch.int32, device=dev)
+    total = torch.zeros(1, dtype=torch.int64, device=dev)
+    rebases = torch.zeros(1, dtype=torch.int64, device=dev)
+    out = cg.FrameOut(rgba=rgba.data_ptr(), palette=pal.data_ptr(), palette_len=len(pal_host),
+                      interior_rgba=0xFF000000, total_iterations=total.data_ptr(), rebases=rebases.data_ptr())
+    stream = torch.cuda.current_stream()
+    flush = _l2_flush(torch, dev)
+    t_orbit = time.perf_counter()
+    orbit = cg.Orbit(d["center_x"], d["center_y"], DEEP_ORBIT_BITS, DEEP_MAX_ITER)
+    t_orbit = time.perf_counter() - t_orbit
+
+    def desc(span, tier):
+        return cg.FrameDesc(width=DEEP_W, height=DEEP_H, max_iterations=DEEP_MAX_ITER, samples_per_pixel=1,
+                            sample_mode=cg.SAMPLES_CENTER, tier=tier, fractal=cg.MANDELBROT, seed=0,
+                            pixel_size=span / DEEP_W)
+
+    def timed(tier, steps, warm):
+        descs = [desc(sp, tier) for sp in DEEP_SPANS]
+        for _ in range(warm):
+            for dd in descs:
+                cg.render_frame_perturb(dd, orbit, out, stream=stream, sync=False)
+        torch.cuda.synchronize()
+        total.zero_()
+        rebases.zero_()
+        per_span_ms = [0.0] * len(descs)
+        ev = []
+        for k in range(steps):
+            flush(k)
+            row = []
+            for dd in descs:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                cg.render_frame_perturb(dd, orbit, out, stream=stream, sync=False)
+                e1.record(stream)
+                row.append((e0, e1))
+            ev.append(row)
+        torch.cuda.synchronize()
+        for row in ev:
+            for j, (e0, e1) in enumerate(row):
+                per_span_ms[j] += e0.elapsed_time(e1)
+        return int(total.item()), per_span_ms, int(rebases.item())
+
+    # per-span iteration counts (for per-span throughput)
+    span_iters = []
+    for sp in DEEP_SPANS:
+        total.zero_()
+        cg.render_frame_perturb(desc(sp, cg.TIER_PERTURB_F32), orbit, out, stream=stream)
+        span_iters.append(int(total.item()))
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    iters, span_ms, rb = timed(cg.TIER_PERTURB_F32, args.steps, args.warmup)
+    clk = clocks.stop()
+    kernel_ms = sum(span_ms)
+    value = iters / (kernel_ms / 1e3) / 1e9
+    f64_iters, f64_ms, f64_rb = timed(cg.TIER_PERTURB_F64, 1, 1)
+
+    # end to end: orbit from the hex centre, palette upload, both frames, images to host
+    host = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    e0 = time.perf_counter()
+    e2e_iters = 0
+    for _ in range(args.steps):
+        o2 = cg.Orbit(d["center_x"], d["center_y"], DEEP_ORBIT_BITS, DEEP_MAX_ITER)
+        pal.copy_(torch.from_numpy(pal_host.view(np.int32)), non_blocking=False)
+        for sp in DEEP_SPANS:
+            total.zero_()
+            cg.render_frame_perturb(desc(sp, cg.TIER_PERTURB_F32), o2, out, stream=stream, sync=False)
+            host.copy_(rgba, non_blocking=True)
+            torch.cuda.synchronize()
+            e2e_iters += int(total.item())
+        o2.close()
+    e2e_s = time.perf_counter() - e0
+
+    # roofline: FP32 pipe.  A rescaled step is 2 FFMA (2Z + 2^e w), 4 FFMA (w'),
+    # 2 FFMA (z = Z + 2^e w'), 1 FMUL + 1 FFMA (|z|^2), 1 FMNMX of |w'x|, |w'y|
+    # and 1 compare for the renormalisation test: 12 FP32-pipe instructions per
+    # iteration.
+    peak = cg.measure_fma_peak(cg.TIER_F32)
+    ops = 12
+    achieved = iters / (kernel_ms / 1e3) * ops
+    roof = {"bound": "fp32-pipe", "achieved": achieved / 1e12, "peak": peak / 2 / 1e12, "unit": "Top/s",
+            "frac": achieved / (peak / 2), "traffic": None,
+            "peak_source": "measured in this run: chaos_measure_fma_peak (full-occupancy FFMA chains)",
+            "ops_per_iteration": ops, "kernel": "k_perturb<float,16,rescaled>"}
+
+    # CPU leg: the oracle's multi-word direct iteration on a bounded sample of pixels
+    from oracle.oracle import Oracle
+    o = Oracle()
+    rng = np.random.default_rng(5)
+    nsamp = 64
+    while True:
+        pix = rng.choice(n, nsamp, replace=False)
+        parts = [o.frame_offsets(DEEP_W, DEEP_H, 1, cg.SAMPLES_CENTER, 0, DEEP_SPANS[1] / DEEP_W, int(p), 1)
+                 for p in pix]
+        dcx = np.concatenate([p[0] for p in parts])
+        dcy = np.concatenate([p[1] for p in parts])
+        t0 = time.perf_counter()
+        cc, _ = o.hp_escape_batch(d["center_x"], d["center_y"], dcx, dcy, DEEP_ORBIT_BITS, DEEP_MAX_ITER)
+        dt = time.perf_counter() - t0
+        if dt > 3.0 or nsamp >= 1 << 16:
+            break
+        nsamp = min(1 << 16, int(nsamp * max(2.0, 3.0 / max(dt, 1e-3))))
+    cpu = {"value": float(cc.astype(np.int64).sum()) / dt / 1e9, "unit": "Gpixel-iter/s", "cores": o.max_threads(),
+           "kind": "port",
+           "sample": f"{nsamp} seeded pixels of the span-1e-200 frame, direct iteration at {DEEP_ORBIT_BITS} bits "
+                     f"(the oracle; the reference has no multi-word path), {int(cc.sum())} pixel-iterations "
+                     f"in {dt:.2f} s"}
+
+    line = {"metric": "Gpixel-iter/s (perturbation deep zoom)", "value": value, "unit": "Gpixel-iter/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (rescaled differences)",
+            "data": "synthetic: seeded Misiurewicz centre (1024-bit), seeded palette",
+            "config": {"workload": f"C3: Mandelbrot {DEEP_W}x{DEEP_H}, spans 1e-60 and 1e-200 (one frame each per "
+                                   f"step), maxIter {DEEP_MAX_ITER}, 1 sample per pixel centre, perturbation",
+                       "centre": {"preperiod": d["preperiod"], "period": d["period"], "approx": d["approx"]},
+                       "orbit_bits": DEEP_ORBIT_BITS, "l2": "flushed between steps"},
+            "pixel_iterations_per_step": iters // args.steps,
+            "per_span": {f"{sp:g}": {"pixel_iterations": it, "ms": ms / args.steps,
+                                     "Gpixel_iter_s": it / (ms / args.steps / 1e3) / 1e9}
+                         for sp, it, ms in zip(DEEP_SPANS, span_iters, span_ms)},
+            "rebases_per_step": rb // args.steps,
+            "f64_differences": {"value": f64_iters / (sum(f64_ms) / 1e3) / 1e9, "ms_per_step": sum(f64_ms),
+                                "per_span_ms": f64_ms, "rebases": f64_rb},
+            "orbit_seconds": t_orbit,
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_iters / e2e_s / 1e9, "unit": "Gpixel-iter/s", "h2d_bytes_per_step": 4 * len(pal_host),
+                    "d2h_bytes_per_step": 2 * 4 * n,
+                    "call": "chaos_orbit_create + chaos_render_frame_perturb x2 + image reads",
+                    "seconds_per_step": e2e_s / args.steps},
+            "gpu_launches": 2 * args.steps, "clocks": clk}
+    print(json.dumps(line), flush=True)
+    orbit.close()
+
+
 def run_serve(args):
     """C5: 16 zoom sessions (720p..2160p), 1.02x zoom per frame toward seeded
     boundary points, Poisson arrivals at 60 Hz per session, HBM-budget admission,
@@ -637,7 +794,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["c2", "c2-crop", "c4", "c5"], default="c2",
+    ap.add_argument("--workload", choices=["c2", "c2-crop", "c3", "c4", "c5"], default="c2",
                     help="c2-crop: the central 480x270 pixels of the same frame (for profiler captures)")
     args = ap.parse_args()
     if args.workload == "c2-crop":
@@ -645,6 +802,8 @@ def main():
         W, H = 480, 270
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c3":
+        run_deep(args)
     elif args.workload == "c4":
         run_batch(args)
     elif args.workload == "c5":

@@ -3,20 +3,29 @@ chaos-ultra's fractal-kernel path.
 
 Python face of libchaos_gb300.so: `Module` mirrors FractalRenderingModule and
 its kernels, `Renderer` mirrors CudaFractalRenderer (renderQuality /
-renderFast), `render_frame` is the jittered-supersampling frame path.  Device
-buffers are passed as raw device pointers (e.g. torch tensor data_ptr()).
+renderFast), `render_frame` is the jittered-supersampling frame path, `Batch`
+renders many viewports in one CUDA-graph launch, `Server` serves concurrent
+zoom sessions, `Orbit` / `render_frame_perturb` are the deep-zoom tier.
+Device buffers are passed as raw device pointers (e.g. torch tensor
+data_ptr()).
 """
 from ._native import (ARITH_FMA, ARITH_PARITY, DROPIN_DIR, DROPIN_PARITY_DIR, FLAG_ADAPTIVE_SS, FLAG_FOVEATION,
                       FLAG_IS_ZOOMING, FLAG_SAMPLE_REUSE, FLAG_VISUALIZE_SAMPLE_COUNT, FLAG_ZOOMING_IN, JULIA,
                       LIB_PATH, MANDELBROT, PRECISION_DOUBLE, PRECISION_SINGLE, PRECISION_TOO_BIG, SAMPLES_CENTER,
-                      SAMPLES_JITTER, TIER_AUTO, TIER_AUTO_DEEP, TIER_F32, TIER_F64, TIER_FLOATFLOAT, TIER_PERTURB_F32, TIER_PERTURB_F64, BatchConfig, ChaosError, FrameDesc, FrameOut, FrameRecord, RenderingModel, SessionDesc, Viewport, lib)
-from .api import (Batch, Module, Orbit, Server, auto_tier, Renderer, available_fractals, measure_fma_peak, render_frame, render_frame_host,
-                  render_frame_perturb, select_precision, to_hex_fixed, version)
+                      SAMPLES_JITTER, TIER_AUTO, TIER_AUTO_DEEP, TIER_F32, TIER_F64, TIER_FLOATFLOAT,
+                      TIER_PERTURB_F32, TIER_PERTURB_F64, BatchConfig, ChaosError, FrameDesc, FrameOut, FrameRecord,
+                      RenderingModel, SessionDesc, Viewport, lib)
+from .api import (Batch, Module, Orbit, Renderer, Server, auto_tier, available_fractals,
+                  measure_fma_peak, render_frame, render_frame_host, render_frame_perturb, select_precision,
+                  to_hex_fixed, version)
 
 __all__ = [
     "ARITH_FMA", "ARITH_PARITY", "DROPIN_DIR", "DROPIN_PARITY_DIR", "FLAG_ADAPTIVE_SS", "FLAG_FOVEATION",
     "FLAG_IS_ZOOMING", "FLAG_SAMPLE_REUSE", "FLAG_VISUALIZE_SAMPLE_COUNT", "FLAG_ZOOMING_IN", "JULIA", "LIB_PATH",
     "MANDELBROT", "PRECISION_DOUBLE", "PRECISION_SINGLE", "PRECISION_TOO_BIG", "SAMPLES_CENTER", "SAMPLES_JITTER",
-    "TIER_AUTO", "TIER_AUTO_DEEP", "TIER_F32", "TIER_F64", "TIER_FLOATFLOAT", "TIER_PERTURB_F32", "TIER_PERTURB_F64", "BatchConfig", "Viewport", "SessionDesc", "FrameRecord", "ChaosError", "FrameDesc", "FrameOut", "RenderingModel", "lib", "Module", "Renderer",
-    "Batch", "Server", "auto_tier", "Orbit", "render_frame_perturb", "to_hex_fixed", "available_fractals", "measure_fma_peak", "render_frame", "render_frame_host", "select_precision", "version",
+    "TIER_AUTO", "TIER_AUTO_DEEP", "TIER_F32", "TIER_F64", "TIER_FLOATFLOAT", "TIER_PERTURB_F32", "TIER_PERTURB_F64",
+    "BatchConfig", "ChaosError", "FrameDesc", "FrameOut", "FrameRecord", "RenderingModel", "SessionDesc", "Viewport",
+    "lib", "Batch", "Module", "Orbit", "Renderer", "Server", "auto_tier", "available_fractals",
+    "measure_fma_peak", "render_frame", "render_frame_host", "render_frame_perturb", "select_precision",
+    "to_hex_fixed", "version",
 ]

@@ -305,8 +305,7 @@ uint32_t chaos_batch_auto_tier(double center_x, double center_y, double pixel_si
 static uint32_t auto_deep_tier(double center_x, double center_y, double pixel_size)
 {
     uint32_t t = chaos_batch_auto_tier(center_x, center_y, pixel_size);
-    if (t != CHAOS_TIER_F64) return t;
-    return pixel_size >= 1e-30 ? CHAOS_TIER_PERTURB_F32 : CHAOS_TIER_PERTURB_F64;
+    return t == CHAOS_TIER_F64 ? CHAOS_TIER_PERTURB_F32 : t;
 }
 
 static void batch_free(chaos_batch *b)
@@ -397,8 +396,8 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
             return api_fail(CHAOS_ERR_UNSUPPORTED, "viewport %u: tier %u not batchable", k, tier);
         tiers[k] = tier;
         if (tier == CHAOS_TIER_PERTURB_F32 || tier == CHAOS_TIER_PERTURB_F64) {
-            if (tier == CHAOS_TIER_PERTURB_F32 && v.pixel_size < 1e-30)
-                return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "viewport %u: binary32 differences need pixel >= 1e-30", k);
+            if (!(v.pixel_size >= 1e-290))
+                return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "viewport %u: perturbation needs pixel >= 1e-290", k);
             any_rgba |= v.rgba != nullptr;
             continue;  // its orbit is computed below
         }

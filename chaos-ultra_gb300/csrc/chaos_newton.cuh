@@ -58,8 +58,8 @@ template <class R> __device__ __forceinline__ uint32_t newton_root(thrust::compl
 // computeFractal of the three modules, as an unsigned value (the float the
 // reference returns is an integer): the root index (wired, generic) or the
 // iteration count (iterations).
-template <class R, int F>
-__device__ __forceinline__ uint32_t newton_compute(uint32_t max_iterations, R zx, R zy, const NewtonParams &p)
+// (declared __forceinline__ in chaos_device.cuh; the attribute is not repeated here)
+template <class R, int F> __device__ uint32_t newton_compute(uint32_t max_iterations, R zx, R zy, const NewtonParams &p)
 {
     thrust::complex<R> x(zx, zy);
     const double *roots = F == FRACTAL_NEWTON_WIRED ? kWiredRoots : p.roots;

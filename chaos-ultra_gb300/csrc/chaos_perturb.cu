@@ -9,7 +9,20 @@
 // Glitch test and repair (rebasing): when |z| < |d| the difference has lost
 // its precision relative to z, so the sample restarts from the start of the
 // orbit with d = z (Z_0 = 0); the same happens when m reaches the end of a
-// reference orbit that escaped early.  Rebases are counted.
+// reference orbit that escaped early.  Rebases are counted.  The squares of
+// the glitch test underflow at depth (|d| < 1e-19 in binary32, 1e-154 in
+// binary64), so when |z|^2 is that small the test is redone with scaled or
+// wider operands.
+//
+// Binary32 differences below the binary32 range (pixel < 1e-30) are rescaled:
+// d = w 2^e, dc = u 2^e with w, u binary32 near 1 and e an integer per sample,
+//     w' = (2 Z + 2^e w) w + u
+// (the 2^e w term is dropped once 2^e is below the binary32 normal range, where
+// it is below binary32 resolution against 2 Z), renormalised by 2^24 when |w|
+// leaves [2^-24, 2^24].  Once 2^e reaches 2^-100 the sample continues with
+// plain binary32 differences d = w 2^e.  While rescaled, |d| < 2^-76, so a
+// glitch needs |Z_m| below 2^-50: that rare case is tested on the binary64
+// orbit in units of 2^e.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -39,6 +52,7 @@ template <class D> struct PerturbArgs {
     uint64_t seed;
     double ps, half_w, half_h;
     const typename Vec2T<D>::type *orbit;  // Z_0 .. Z_{orbit_last}
+    const double2 *orbit64;                // the same orbit in binary64 (rescaled glitch test)
     uint32_t orbit_last;
     uint32_t *counts;
     float *smooth;
@@ -81,8 +95,27 @@ __device__ __forceinline__ void perturb_palette(const uint32_t *pal, uint32_t le
     }
 }
 
-template <class D, int K> __global__ void __launch_bounds__(256) k_perturb(PerturbArgs<D> a)
+// |z| < |d| for the glitch test, exact where the squares would underflow.
+__device__ __forceinline__ bool glitch_test(float zx, float zy, float dx, float dy, float r2)
 {
+    if (r2 >= 0x1p-60f) return r2 < __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+    double z2 = (double)zx * zx + (double)zy * zy, d2 = (double)dx * dx + (double)dy * dy;
+    return z2 < d2;
+}
+__device__ __forceinline__ bool glitch_test(double zx, double zy, double dx, double dy, double r2)
+{
+    if (r2 >= 0x1p-500) return r2 < __fma_rn(dx, dx, __dmul_rn(dy, dy));
+    const double k = 0x1p600;  // exact scaling; an infinite |d|^2 means |d| >> |z|
+    zx *= k, zy *= k, dx *= k, dy *= k;
+    return zx * zx + zy * zy < dx * dx + dy * dy;
+}
+
+// 2^e as a binary32, or 0 below the normal range
+__device__ __forceinline__ float pow2f(int e) { return e >= -126 ? __int_as_float((e + 127) << 23) : 0.f; }
+
+template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_perturb(PerturbArgs<D> a)
+{
+    static_assert(!S || sizeof(D) == 4, "rescaling is for binary32 differences");
     using O = Op<D>;
     constexpr uint32_t FULLM = 0xffffffffu;
     __shared__ uint32_t s_pal[4096];
@@ -96,7 +129,10 @@ template <class D, int K> __global__ void __launch_bounds__(256) k_perturb(Pertu
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt_mask = (1u << lane) - 1u;
     uint32_t pix = 0xffffffffu, s = 0, i = 0, m = 0;
+    // rescaled samples keep w in (dx, dy) and u in (dcx, dcy), with d = w 2^e
     D dx = D(0), dy = D(0), dcx = D(0), dcy = D(0), Zx = D(0), Zy = D(0);
+    int e = 0;
+    bool scaled = false;
     bool need = true, begin = false;
     float acc_v = 0.f, acc[4] = {0.f, 0.f, 0.f, 0.f};
     unsigned long long iters = 0, rebases = 0;
@@ -135,6 +171,19 @@ template <class D, int K> __global__ void __launch_bounds__(256) k_perturb(Pertu
                 double ddy = __dmul_rn(-__dsub_rn(__dadd_rn((double)py, oy), a.half_h), a.ps);
                 dcx = (D)ddx;
                 dcy = (D)ddy;
+                scaled = false;
+                if constexpr (S) {
+                    // exponent of the larger component (binary64 field), u = dc 2^-e
+                    double big = fmax(fabs(ddx), fabs(ddy));
+                    int e0 = (int)((__double_as_longlong(big) >> 52) & 0x7ff) - 1023;
+                    if (big != 0.0 && e0 < -100) {
+                        double k = __longlong_as_double((long long)(1023 - e0) << 52);
+                        dcx = (D)(ddx * k);
+                        dcy = (D)(ddy * k);
+                        e = e0;
+                        scaled = true;
+                    }
+                }
                 dx = D(0);
                 dy = D(0);
                 Zx = D(0);
@@ -145,6 +194,66 @@ template <class D, int K> __global__ void __launch_bounds__(256) k_perturb(Pertu
             }
 #pragma unroll 4
             for (int k = 0; k < K && !done; k++) {
+                if constexpr (S) if (scaled) {
+                    // w' = (2Z + 2^e w) w + u
+                    const float q = pow2f(e);
+                    float ax = __fmaf_rn(q, (float)dx, 2.f * (float)Zx), ay = __fmaf_rn(q, (float)dy, 2.f * (float)Zy);
+                    float nwx = __fmaf_rn(ax, (float)dx, __fmaf_rn(-ay, (float)dy, (float)dcx));
+                    float nwy = __fmaf_rn(ax, (float)dy, __fmaf_rn(ay, (float)dx, (float)dcy));
+                    ++m;
+                    ++i;
+                    typename Vec2T<D>::type Z = a.orbit[m];
+                    float zx = __fmaf_rn(nwx, q, (float)Z.x), zy = __fmaf_rn(nwy, q, (float)Z.y);
+                    r2 = O::fma(zx, zx, O::mul(zy, zy));
+                    if (!(r2 < D(4)) || i == a.max_iter) {
+                        done = true;
+                        break;
+                    }
+                    if (m == a.orbit_last) {
+                        // the orbit ends: continue unscaled from z
+                        dx = zx;
+                        dy = zy;
+                        dcx = (D)((float)dcx * q);
+                        dcy = (D)((float)dcy * q);
+                        scaled = false;
+                        Zx = Zy = D(0);
+                        m = 0;
+                        ++rebases;
+                        continue;
+                    }
+                    if (r2 < 0x1p-100f) {
+                        // |Z| < 2^-50: glitch test in units of 2^e on the binary64 orbit
+                        const double2 Zd = a.orbit64[m];
+                        const double k2 = __longlong_as_double((long long)(1023 - e) << 52);
+                        double sx = fma(Zd.x, k2, (double)nwx), sy = fma(Zd.y, k2, (double)nwy);
+                        if (sx * sx + sy * sy < (double)nwx * nwx + (double)nwy * nwy) {
+                            dx = (D)sx;
+                            dy = (D)sy;
+                            Zx = Zy = D(0);
+                            m = 0;
+                            ++rebases;
+                            continue;
+                        }
+                    }
+                    dx = nwx;
+                    dy = nwy;
+                    Zx = Z.x;
+                    Zy = Z.y;
+                    const float mag = fmaxf(fabsf(nwx), fabsf(nwy));
+                    if (mag > 0x1p24f) {
+                        dx *= D(0x1p-24f), dy *= D(0x1p-24f), dcx *= D(0x1p-24f), dcy *= D(0x1p-24f);
+                        e += 24;
+                        if (e > -100) {
+                            const float q2 = pow2f(e);
+                            dx *= q2, dy *= q2, dcx *= q2, dcy *= q2;
+                            scaled = false;
+                        }
+                    } else if (mag < 0x1p-24f && mag > 0.f && e > -1000) {
+                        dx *= D(0x1p24f), dy *= D(0x1p24f), dcx *= D(0x1p24f), dcy *= D(0x1p24f);
+                        e -= 24;
+                    }
+                    continue;
+                }
                 // d' = (2Z + d) d + dc
                 D wx = O::fma(D(2), Zx, dx), wy = O::fma(D(2), Zy, dy);
                 D ndx = O::fma(wx, dx, O::fma(-wy, dy, dcx));
@@ -158,8 +267,7 @@ template <class D, int K> __global__ void __launch_bounds__(256) k_perturb(Pertu
                     done = true;
                     break;
                 }
-                D d2 = O::fma(ndx, ndx, O::mul(ndy, ndy));
-                if (r2 < d2 || m == a.orbit_last) {
+                if (m == a.orbit_last || glitch_test(zx, zy, ndx, ndy, r2)) {
                     dx = zx;
                     dy = zy;
                     Zx = D(0);
@@ -230,11 +338,12 @@ template <class D, int K> __global__ void __launch_bounds__(256) k_perturb(Pertu
     }
 }
 
-template <class D> static cudaError_t launch_perturb(const PerturbArgs<D> &a, int sms, cudaStream_t s)
+template <class D, bool S> static cudaError_t launch_perturb(const PerturbArgs<D> &a, int sms, cudaStream_t s)
 {
     static const int occ = [] {
         int n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_perturb<D, 16>, 256, 0) != cudaSuccess || n < 1) n = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_perturb<D, 16, S>, 256, 0) != cudaSuccess || n < 1)
+            n = 1;
         return n;
     }();
     unsigned long long warps = ((unsigned long long)a.n_pix + 31ull) / 32ull;
@@ -242,7 +351,7 @@ template <class D> static cudaError_t launch_perturb(const PerturbArgs<D> &a, in
     unsigned long long cap = (unsigned long long)occ * (unsigned long long)sms;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    k_perturb<D, 16><<<(unsigned)blocks, 256, 0, s>>>(a);
+    k_perturb<D, 16, S><<<(unsigned)blocks, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -381,6 +490,7 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
     else
         a.orbit = reinterpret_cast<const typename Vec2T<D>::type *>(orb->z64);
     a.orbit_last = orb->last;
+    a.orbit64 = orb->z64;
     a.counts = o->counts;
     a.smooth = o->smooth;
     a.pixels = reinterpret_cast<PixelInfo *>(o->pixels);
@@ -401,7 +511,12 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
         int rc = api_device_counter(s, &a.counter, &sms);
         if (rc) return rc;
     }
-    cudaError_t e = launch_perturb<D>(a, sms, s);
+    // binary32 differences are rescaled below pixel 1e-30 (2^-100)
+    cudaError_t e;
+    if constexpr (std::is_same<D, float>::value)
+        e = d->pixel_size < 1e-30 ? launch_perturb<float, true>(a, sms, s) : launch_perturb<float, false>(a, sms, s);
+    else
+        e = launch_perturb<D, false>(a, sms, s);
     if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e));
     if (sync) {
         e = cudaStreamSynchronize(s);
@@ -433,9 +548,8 @@ static int perturb_entry(const chaos_frame_desc *d, const chaos_orbit *orb, cons
         return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "rgba output needs a palette");
     if (d->tier == CHAOS_TIER_PERTURB_F32) {
         // the differences must stay normal binary32 numbers
-        if (d->pixel_size < 1e-30)
-            return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "binary32 differences need pixel size >= 1e-30 (got %g)",
-                            d->pixel_size);
+        if (d->pixel_size < 1e-290)
+            return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "rescaled binary32 differences need pixel size >= 1e-290");
         return perturb_impl<float>(d, orb, o, s, sync, counter);
     }
     if (d->tier == CHAOS_TIER_PERTURB_F64) {

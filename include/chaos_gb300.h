@@ -216,7 +216,7 @@ int chaos_renderer_destroy(chaos_renderer *r);
 #define CHAOS_TIER_F32 0         /* escape loop in binary32 */
 #define CHAOS_TIER_F64 1         /* escape loop in binary64 */
 #define CHAOS_TIER_FLOATFLOAT 2  /* float-float (two binary32 words, ~48 bits), batched viewports */
-#define CHAOS_TIER_PERTURB_F32 3 /* perturbation, binary32 differences (pixel size >= 1e-30) */
+#define CHAOS_TIER_PERTURB_F32 3 /* perturbation, binary32 differences, rescaled by 2^e below pixel 1e-30 (>= 1e-290) */
 #define CHAOS_TIER_PERTURB_F64 4 /* perturbation, binary64 differences (pixel size >= 1e-290) */
 
 /* One frame of the plain escape-time renderer.  Sample s of pixel (px, py)

@@ -151,10 +151,10 @@ def test_batch_perturbation_matches_single_frames(cuda):
     b2.close()
 
 
-def test_batch_rejects_shallow_binary32_perturbation(cuda):
+def test_batch_rejects_perturbation_below_binary64_range(cuda):
     import chaos_gb300 as cg
     from chaos_gb300.palette import seeded_palette
-    v = (16, 16, 1, 0, 100, cg.TIER_PERTURB_F32, (-0.74, 0.13), 1e-31 * 16)
+    v = (16, 16, 1, 0, 100, cg.TIER_PERTURB_F32, (-0.74, 0.13), 1e-295 * 16)
     with pytest.raises(cg.ChaosError):
         build(cuda, [v], seeded_palette(16))
 

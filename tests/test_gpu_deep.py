@@ -1,0 +1,77 @@
+"""Perturbation deep zoom at 1920x1080, spans 1e-60 and 1e-200, maxIter
+100000, centred on the committed seeded Misiurewicz point (1024-bit fixed
+point), one sample per pixel at pixel centres: binary32 differences (rescaled
+by 2^e below pixel 1e-30) and binary64 differences, against the oracle's
+multi-word direct iteration at 1088 bits on 4096 seeded pixels.
+
+Bars: escape-count mismatch rate at most 0.1% (the workload's bar); for
+matching escaped samples the smooth count within 1e-3 of the oracle's on every
+sample with binary64 differences.  With binary32 differences the median
+deviation is at most 1e-4 and at most 2% of samples deviate by more than 1e-3:
+measured 0.8% (1e-60) and 1.5% (1e-200), up to 0.19, where binary64
+differences of the same samples stay within 3e-5: binary32 rounding of the
+differences, not the method."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+W, H, MAX_ITER, N_SAMPLE = 1920, 1080, 100000, 4096
+ORBIT_BITS, ORACLE_BITS = 1088, 1088
+
+
+@pytest.fixture(scope="module")
+def deep(cuda, oracle):
+    import chaos_gb300 as cg
+    from chaos_gb300.workloads import deep_zoom_centre
+    d = deep_zoom_centre()
+    orbit = cg.Orbit(d["center_x"], d["center_y"], ORBIT_BITS, MAX_ITER)
+    pix = np.sort(np.random.default_rng(3).choice(W * H, N_SAMPLE, replace=False))
+    want = {}
+    for span in (1e-60, 1e-200):
+        ps = span / W
+        parts = [oracle.frame_offsets(W, H, 1, cg.SAMPLES_CENTER, 0, ps, int(p), 1) for p in pix]
+        dcx = np.concatenate([p[0] for p in parts])
+        dcy = np.concatenate([p[1] for p in parts])
+        want[span] = oracle.hp_escape_batch(d["center_x"], d["center_y"], dcx, dcy, ORACLE_BITS, MAX_ITER)
+    yield cg, orbit, pix, want
+    orbit.close()
+
+
+def render(cuda, cg, orbit, span, tier):
+    torch = cuda
+    counts = torch.zeros(W * H, dtype=torch.int32, device="cuda:0")
+    smooth = torch.zeros(W * H, dtype=torch.float32, device="cuda:0")
+    total = torch.zeros(1, dtype=torch.int64, device="cuda:0")
+    rebases = torch.zeros(1, dtype=torch.int64, device="cuda:0")
+    out = cg.FrameOut(counts=counts.data_ptr(), smooth=smooth.data_ptr(), total_iterations=total.data_ptr(),
+                      rebases=rebases.data_ptr())
+    desc = cg.FrameDesc(width=W, height=H, max_iterations=MAX_ITER, samples_per_pixel=1,
+                        sample_mode=cg.SAMPLES_CENTER, tier=tier, fractal=cg.MANDELBROT, seed=0, pixel_size=span / W)
+    cg.render_frame_perturb(desc, orbit, out)
+    c = counts.cpu().numpy().view(np.uint32)
+    assert int(total.item()) == int(c.astype(np.int64).sum())
+    return c, smooth.cpu().numpy(), int(rebases.item())
+
+
+@pytest.mark.parametrize("span", [1e-60, 1e-200])
+@pytest.mark.parametrize("tier_name", ["PERTURB_F32", "PERTURB_F64"])
+def test_deep_zoom_against_multiword_oracle(cuda, deep, span, tier_name):
+    cg, orbit, pix, want = deep
+    counts, smooth, rebases = render(cuda, cg, orbit, span, getattr(cg, "TIER_" + tier_name))
+    wc, wr2 = want[span]
+    got = counts[pix]
+    rate = float((got != wc).mean())
+    esc = (got == wc) & (wc < MAX_ITER)
+    nu = wc[esc] + 1.0 - np.log2(0.5 * np.log2(wr2[esc]))
+    dev = np.abs(smooth[pix][esc] - nu)
+    over = float((dev > 1e-3).mean())
+    print(f"deep zoom span {span:g} {tier_name}: mismatch {rate:.5f} on {len(pix)} pixels, smooth dev max "
+          f"{dev.max():.2e} median {np.median(dev):.2e} over-1e-3 {over:.5f}, rebases {rebases}, "
+          f"counts {int(wc.min())}..{int(wc.max())}")
+    assert len(np.unique(wc)) > 20  # the view has structure
+    assert rate <= 0.001, rate
+    if tier_name == "PERTURB_F64":
+        assert over == 0.0, over
+    else:
+        assert over <= 0.02 and np.median(dev) <= 1e-4, (over, np.median(dev))
