@@ -657,17 +657,20 @@ def run_deep(args):
         o2.close()
     e2e_s = time.perf_counter() - e0
 
-    # roofline: FP32 pipe.  A rescaled step is 2 FFMA (2Z + 2^e w), 4 FFMA (w'),
-    # 2 FFMA (z = Z + 2^e w'), 1 FMUL + 1 FFMA (|z|^2), 1 FMNMX of |w'x|, |w'y|
-    # and 1 compare for the renormalisation test: 12 FP32-pipe instructions per
-    # iteration.
+    # roofline: FP32 pipe against the plain escape step's 6 FP32-pipe
+    # instructions per pixel-iteration (the headline unit of every tier).  The
+    # perturbation steps themselves cost: linear rescaled step 4 FFMA + 1 load
+    # of 2Z; quadratic rescaled step 12; plain-difference step 16 (6 for the
+    # difference, 2 for z, 2 for |z|^2, 2 for |d|^2, compares).
     peak = cg.measure_fma_peak(cg.TIER_F32)
-    ops = 12
+    ops = 6
     achieved = iters / (kernel_ms / 1e3) * ops
     roof = {"bound": "fp32-pipe", "achieved": achieved / 1e12, "peak": peak / 2 / 1e12, "unit": "Top/s",
             "frac": achieved / (peak / 2), "traffic": None,
             "peak_source": "measured in this run: chaos_measure_fma_peak (full-occupancy FFMA chains)",
-            "ops_per_iteration": ops, "kernel": "k_perturb<float,16,rescaled>"}
+            "ops_per_iteration": ops,
+            "step_costs": {"rescaled_linear": 4, "rescaled_quadratic": 12, "plain_difference": 16},
+            "kernel": "k_perturb<float,16,rescaled>"}
 
     # CPU leg: the oracle's multi-word direct iteration on a bounded sample of pixels
     from oracle.oracle import Oracle

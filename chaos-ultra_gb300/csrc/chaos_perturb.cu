@@ -22,7 +22,12 @@
 // leaves [2^-24, 2^24].  Once 2^e reaches 2^-100 the sample continues with
 // plain binary32 differences d = w 2^e.  While rescaled, |d| < 2^-76, so a
 // glitch needs |Z_m| below 2^-50: that rare case is tested on the binary64
-// orbit in units of 2^e.
+// orbit in units of 2^e.  While 2^e is below the normal range the step is
+// linear, w' = 2 Z w + u, and the tests of a step depend on the orbit index
+// alone (escape only where binary32 |Z|^2 >= 4, the glitch test only where it
+// is below 2^-100, the orbit's end), so the orbit carries, per index, the next
+// index where one of them can fire, and steps up to it run as a block of
+// 4 FFMA each on a stored 2Z.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -53,6 +58,8 @@ template <class D> struct PerturbArgs {
     double ps, half_w, half_h;
     const typename Vec2T<D>::type *orbit;  // Z_0 .. Z_{orbit_last}
     const double2 *orbit64;                // the same orbit in binary64 (rescaled glitch test)
+    const float2 *orbit2;                  // 2 Z_m in binary32 (rescaled linear steps)
+    const uint32_t *next_event;            // first index >= m where a rescaled step's test can fire
     uint32_t orbit_last;
     uint32_t *counts;
     float *smooth;
@@ -194,6 +201,42 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
             }
 #pragma unroll 4
             for (int k = 0; k < K && !done; k++) {
+                if constexpr (S) if (scaled && e < -126) {
+                    // linear steps up to (not onto) the next index whose tests can fire
+                    constexpr uint32_t B = 8;
+                    const uint32_t ev = a.next_event[m + 1];
+                    const uint32_t n = min(min(B, ev - (m + 1)), a.max_iter - 1u - i);
+                    if (n > 0) {
+                        float wx = (float)dx, wy = (float)dy;
+                        const float ux = (float)dcx, uy = (float)dcy;
+#pragma unroll
+                        for (uint32_t j = 0; j < B; j++) {
+                            if (j < n) {
+                                const float2 Z2 = a.orbit2[m + j];
+                                const float nx = __fmaf_rn(Z2.x, wx, __fmaf_rn(-Z2.y, wy, ux));
+                                const float ny = __fmaf_rn(Z2.x, wy, __fmaf_rn(Z2.y, wx, uy));
+                                wx = nx;
+                                wy = ny;
+                            }
+                        }
+                        m += n;
+                        i += n;
+                        const typename Vec2T<D>::type Z = a.orbit[m];
+                        Zx = Z.x;
+                        Zy = Z.y;
+                        dx = wx;
+                        dy = wy;
+                        const float mag = fmaxf(fabsf(wx), fabsf(wy));
+                        if (mag > 0x1p24f) {
+                            dx *= D(0x1p-24f), dy *= D(0x1p-24f), dcx *= D(0x1p-24f), dcy *= D(0x1p-24f);
+                            e += 24;
+                        } else if (mag < 0x1p-24f && mag > 0.f && e > -1000) {
+                            dx *= D(0x1p24f), dy *= D(0x1p24f), dcx *= D(0x1p24f), dcy *= D(0x1p24f);
+                            e -= 24;
+                        }
+                        continue;
+                    }
+                }
                 if constexpr (S) if (scaled) {
                     // w' = (2Z + 2^e w) w + u
                     const float q = pow2f(e);
@@ -370,6 +413,8 @@ struct chaos_orbit {
     double center_x = 0, center_y = 0;  // rounded centre, for reporting
     float2 *z32 = nullptr;
     double2 *z64 = nullptr;
+    float2 *z2 = nullptr;            // 2 Z in binary32
+    uint32_t *next_event = nullptr;  // see the rescaled linear steps of k_perturb
 };
 
 static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t max_iterations, chaos_orbit **out);
@@ -424,8 +469,23 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
             break;
         }
     }
-    std::vector<float2> z32(z64.size());
-    for (size_t k = 0; k < z64.size(); k++) z32[k] = make_float2((float)z64[k].x, (float)z64[k].y);
+    std::vector<float2> z32(z64.size()), z2(z64.size());
+    for (size_t k = 0; k < z64.size(); k++) {
+        z32[k] = make_float2((float)z64[k].x, (float)z64[k].y);
+        z2[k] = make_float2(2.f * z32[k].x, 2.f * z32[k].y);
+    }
+    // next_event[m]: first index j >= m where a rescaled step's test can fire,
+    // evaluated as the kernel does (binary32 |Z_j|^2 with one fused add)
+    std::vector<uint32_t> next_event(z64.size());
+    {
+        const size_t last = z64.size() - 1;
+        uint32_t next = (uint32_t)last;
+        for (size_t j = last + 1; j-- > 0;) {
+            const float r2 = std::fmaf(z32[j].x, z32[j].x, z32[j].y * z32[j].y);
+            if (j == last || !(r2 < 4.f) || r2 < 0x1p-100f) next = (uint32_t)j;
+            next_event[j] = next;
+        }
+    }
 
     chaos_orbit *o = new (std::nothrow) chaos_orbit();
     if (!o) return api_fail(CHAOS_ERR_OUT_OF_MEMORY, "out of host memory");
@@ -440,9 +500,16 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
     if (e == cudaSuccess) e = cudaMalloc(&o->z32, z32.size() * sizeof(float2));
     if (e == cudaSuccess) e = cudaMemcpy(o->z64, z64.data(), z64.size() * sizeof(double2), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(o->z32, z32.data(), z32.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&o->z2, z2.size() * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMemcpy(o->z2, z2.data(), z2.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&o->next_event, next_event.size() * sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(o->next_event, next_event.data(), next_event.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         if (o->z64) cudaFree(o->z64);
         if (o->z32) cudaFree(o->z32);
+        if (o->z2) cudaFree(o->z2);
+        if (o->next_event) cudaFree(o->next_event);
         delete o;
         return api_fail(CHAOS_ERR_CUDA, "reference orbit upload: %s", cudaGetErrorString(e));
     }
@@ -464,6 +531,8 @@ int chaos_orbit_destroy(chaos_orbit *o)
     if (!o) return CHAOS_OK;
     if (o->z64) cudaFree(o->z64);
     if (o->z32) cudaFree(o->z32);
+    if (o->z2) cudaFree(o->z2);
+    if (o->next_event) cudaFree(o->next_event);
     delete o;
     return CHAOS_OK;
 }
@@ -491,6 +560,8 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
         a.orbit = reinterpret_cast<const typename Vec2T<D>::type *>(orb->z64);
     a.orbit_last = orb->last;
     a.orbit64 = orb->z64;
+    a.orbit2 = orb->z2;
+    a.next_event = orb->next_event;
     a.counts = o->counts;
     a.smooth = o->smooth;
     a.pixels = reinterpret_cast<PixelInfo *>(o->pixels);
