@@ -415,7 +415,7 @@ def run_batch(args):
     pal = c4_palette()
     dpal = torch.from_numpy(pal.view(np.int32)).to(dev)
 
-    def make(force_tier):
+    def make(force_tier, config=None):
         bufs, vps = [], []
         for k, sp in enumerate(specs):
             n = sp["width"] * sp["height"]
@@ -427,9 +427,18 @@ def run_batch(args):
                                    tier=force_tier, seed=sp["seed"], center_x=sp["center"][0],
                                    center_y=sp["center"][1], pixel_size=sp["span"] / sp["width"],
                                    counts=counts.data_ptr(), rgba=rgba.data_ptr()))
-        return cg.Batch(vps, dpal.data_ptr(), len(pal), 0xFF000000), bufs
+        return cg.Batch(vps, dpal.data_ptr(), len(pal), 0xFF000000, config), bufs
 
-    batch, bufs = make(cg.TIER_AUTO)
+    # launch shapes per tier from the autotuner (outside the timed region)
+    t_tune = time.perf_counter()
+    tune_vps = [cg.Viewport(width=sp["width"], height=sp["height"], max_iterations=sp["max_iter"],
+                            samples_per_pixel=1, sample_mode=cg.SAMPLES_CENTER, tier=cg.TIER_AUTO, seed=sp["seed"],
+                            center_x=sp["center"][0], center_y=sp["center"][1],
+                            pixel_size=sp["span"] / sp["width"]) for sp in specs]
+    tuned, _ = cg.autotune_batch(tune_vps)
+    t_tune = time.perf_counter() - t_tune
+
+    batch, bufs = make(cg.TIER_AUTO, tuned)
     stream = torch.cuda.current_stream()
     flush = _l2_flush(torch, dev)
     for _ in range(args.warmup):
@@ -450,6 +459,22 @@ def run_batch(args):
     value = per_launch * args.steps / (sum(ms) / 1e3) / 1e9
     tiers = batch.tiers()
     tiered_counts = [c.cpu().numpy() for c, _ in bufs]
+
+    # the same batch with the default launch shape (256 threads, 16-step blocks, chunk 1)
+    untuned, ubufs = make(cg.TIER_AUTO)
+    untuned.launch(stream)
+    torch.cuda.synchronize()
+    u_ms = []
+    for k in range(2):
+        flush(k)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        untuned.launch(stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        u_ms.append(e0.elapsed_time(e1))
+    untuned.close()
+    del untuned, ubufs
 
     plain, pbufs = make(cg.TIER_F64)
     plain.launch(stream)
@@ -502,7 +527,7 @@ def run_batch(args):
                                        samples_per_pixel=1, sample_mode=cg.SAMPLES_CENTER, tier=tier_id,
                                        seed=sp["seed"], center_x=sp["center"][0], center_y=sp["center"][1],
                                        pixel_size=sp["span"] / sp["width"], rgba=rgba.data_ptr()))
-        sb = cg.Batch(sub_vps, dpal.data_ptr(), len(pal), 0xFF000000)
+        sb = cg.Batch(sub_vps, dpal.data_ptr(), len(pal), 0xFF000000, tuned)
         sb.launch(stream)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -549,6 +574,12 @@ def run_batch(args):
                                  "what": "fractalRenderMainDouble semantics: binary64, rounded arithmetic, "
                                          "1 sample per pixel, per viewport"},
             "f64_fma_batch": {"value": plain_value, "ms": plain_ms, "speedup_of_tiered": value / plain_value},
+            "autotune": {"seconds": t_tune,
+                         "shape": {name: {"threads": tuned.block_threads[k], "escape_block": tuned.escape_block[k],
+                                          "chunk": tuned.chunk[k]}
+                                   for k, name in enumerate(("f32", "floatfloat", "f64"))},
+                         "default_shape_ms": min(u_ms), "tuned_ms": min(ms),
+                         "default_shape_value": per_launch / (min(u_ms) / 1e3) / 1e9},
             "tiered_deep": {"value": deep_value, "ms": min(deep_ms),
                             "tiers": {"f32": deep_tiers.count(0), "floatfloat": deep_tiers.count(2),
                                       "perturb_f32": deep_tiers.count(3), "perturb_f64": deep_tiers.count(4)},

@@ -15,7 +15,7 @@ from ._native import (ARITH_FMA, ARITH_PARITY, DROPIN_DIR, DROPIN_PARITY_DIR, FL
                       SAMPLES_JITTER, TIER_AUTO, TIER_AUTO_DEEP, TIER_F32, TIER_F64, TIER_FLOATFLOAT,
                       TIER_PERTURB_F32, TIER_PERTURB_F64, BatchConfig, ChaosError, FrameDesc, FrameOut, FrameRecord,
                       RenderingModel, SessionDesc, Viewport, lib)
-from .api import (Batch, Module, Orbit, Renderer, Server, auto_tier, available_fractals,
+from .api import (Batch, Module, Orbit, Renderer, Server, auto_tier, autotune_batch, available_fractals,
                   measure_fma_peak, render_frame, render_frame_host, render_frame_perturb, select_precision,
                   to_hex_fixed, version)
 
@@ -25,7 +25,7 @@ __all__ = [
     "MANDELBROT", "PRECISION_DOUBLE", "PRECISION_SINGLE", "PRECISION_TOO_BIG", "SAMPLES_CENTER", "SAMPLES_JITTER",
     "TIER_AUTO", "TIER_AUTO_DEEP", "TIER_F32", "TIER_F64", "TIER_FLOATFLOAT", "TIER_PERTURB_F32", "TIER_PERTURB_F64",
     "BatchConfig", "ChaosError", "FrameDesc", "FrameOut", "FrameRecord", "RenderingModel", "SessionDesc", "Viewport",
-    "lib", "Batch", "Module", "Orbit", "Renderer", "Server", "auto_tier", "available_fractals",
+    "lib", "Batch", "Module", "Orbit", "Renderer", "Server", "auto_tier", "autotune_batch", "available_fractals",
     "measure_fma_peak", "render_frame", "render_frame_host", "render_frame_perturb", "select_precision",
     "to_hex_fixed", "version",
 ]

@@ -98,7 +98,7 @@ class Viewport(C.Structure):
 
 
 class BatchConfig(C.Structure):
-    _fields_ = [("block_threads", C.c_uint32 * 3), ("escape_block", C.c_uint32 * 3)]
+    _fields_ = [("block_threads", C.c_uint32 * 3), ("escape_block", C.c_uint32 * 3), ("chunk", C.c_uint32 * 3)]
 
 
 TIER_AUTO = 255
@@ -163,6 +163,7 @@ SIGNATURES = {
     "chaos_batch_auto_tier": (_u32, [C.c_double, C.c_double, C.c_double]),
     "chaos_batch_create": (_int, [C.POINTER(Viewport), _u32, _vp, _u32, _u32, C.POINTER(BatchConfig),
                                   C.POINTER(_vp)]),
+    "chaos_batch_autotune": (_int, [C.POINTER(Viewport), _u32, C.c_char_p, C.POINTER(BatchConfig), C.POINTER(_u32)]),
     "chaos_batch_launch": (_int, [_vp, _vp]),
     "chaos_batch_tiers": (_int, [_vp, C.POINTER(_u32), _u32]),
     "chaos_batch_total": (_int, [_vp, C.POINTER(_vp)]),

@@ -262,6 +262,17 @@ class Batch:
             pass
 
 
+def autotune_batch(viewports, cache_path=None):
+    """chaos_batch_autotune: the fastest launch shape per tier for these
+    viewports, as (BatchConfig, from_cache)."""
+    arr = (Viewport * len(viewports))(*viewports)
+    cfg = BatchConfig()
+    hit = C.c_uint32(0)
+    check(lib().chaos_batch_autotune(arr, len(viewports), cache_path.encode() if cache_path else None,
+                                     C.byref(cfg), C.byref(hit)))
+    return cfg, bool(hit.value)
+
+
 def auto_tier(center_x, center_y, pixel_size):
     return lib().chaos_batch_auto_tier(center_x, center_y, pixel_size)
 

@@ -12,7 +12,9 @@
 // regular blocks.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "../../include/chaos_gb300.h"
@@ -39,6 +41,7 @@ struct BatchViewport {
 struct BatchArgs {
     const BatchViewport *vps;
     uint32_t n_vp, n_jobs;
+    uint32_t chunk;  // consecutive jobs a lane claims per work-counter update
     uint32_t *counter;
     unsigned long long *total;
     const uint32_t *palette;
@@ -93,40 +96,44 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
 
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt_mask = (1u << lane) - 1u;
-    uint32_t job = 0xffffffffu, vp = 0, pix = 0, s = 0, i = 0, window = 0, max_iter = 0, spp = 1;
+    uint32_t job = 0xffffffffu, job_end = 0, vp = 0, pix = 0, s = 0, i = 0, window = 0, max_iter = 0, spp = 1;
     T x = P::zero(), y = P::zero(), cx = P::zero(), cy = P::zero();
     bool blk = false, need = true, begin = false;
     float acc_v = 0.f, acc[4] = {0.f, 0.f, 0.f, 0.f};
     unsigned long long iters = 0;
+
+    // a job's viewport: the last one whose job_base <= job
+    auto start_job = [&]() {
+        uint32_t lo = 0, hi = a.n_vp;
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (s_base[mid] <= job)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        vp = lo;
+        pix = job - s_base[lo];
+        max_iter = a.vps[lo].max_iter;
+        spp = a.vps[lo].spp;
+        begin = true;
+        s = 0;
+        acc_v = 0.f;
+        acc[0] = acc[1] = acc[2] = acc[3] = 0.f;
+    };
 
     for (;;) {
         uint32_t need_mask = __ballot_sync(FULLM, need);
         if (need_mask) {
             uint32_t leader = __ffs(need_mask) - 1u;
             uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(a.counter, (uint32_t)__popc(need_mask));
+            if (lane == leader) base = atomicAdd(a.counter, (uint32_t)__popc(need_mask) * a.chunk);
             base = __shfl_sync(FULLM, base, leader);
             if (need) {
-                job = base + (uint32_t)__popc(need_mask & lt_mask);
+                job = base + (uint32_t)__popc(need_mask & lt_mask) * a.chunk;
+                job_end = job + a.chunk;
                 need = false;
-                if (job < a.n_jobs) {
-                    uint32_t lo = 0, hi = a.n_vp;  // last viewport with job_base <= job
-                    while (hi - lo > 1) {
-                        uint32_t mid = (lo + hi) >> 1;
-                        if (s_base[mid] <= job)
-                            lo = mid;
-                        else
-                            hi = mid;
-                    }
-                    vp = lo;
-                    pix = job - s_base[lo];
-                    max_iter = a.vps[lo].max_iter;
-                    spp = a.vps[lo].spp;
-                    begin = true;
-                    s = 0;
-                    acc_v = 0.f;
-                    acc[0] = acc[1] = acc[2] = acc[3] = 0.f;
-                }
+                if (job < a.n_jobs) start_job();
             }
         }
         const bool active = job < a.n_jobs;
@@ -228,7 +235,12 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
             ++s;
             if (s == spp) {
                 if (v.rgba) v.rgba[pix] = frame_pack_rgba(acc, spp);
-                need = true;
+                if (job + 1u < job_end && job + 1u < a.n_jobs) {
+                    ++job;  // the next job of this lane's chunk
+                    start_job();
+                } else {
+                    need = true;
+                }
             } else {
                 begin = true;
             }
@@ -244,7 +256,8 @@ template <class N, int K> static cudaError_t launch_batch_k(const BatchArgs &a, 
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch<N, K>, threads, 0) != cudaSuccess || occ < 1)
         occ = 1;
-    unsigned long long warps = ((unsigned long long)a.n_jobs + 31ull) / 32ull;
+    const unsigned long long per_warp = 32ull * a.chunk;
+    unsigned long long warps = ((unsigned long long)a.n_jobs + per_warp - 1ull) / per_warp;
     unsigned long long per_block = (unsigned long long)threads / 32ull;
     unsigned long long blocks = (warps + per_block - 1) / per_block;
     unsigned long long cap = (unsigned long long)occ * (unsigned long long)sms;
@@ -287,7 +300,7 @@ struct chaos_batch {
     unsigned long long *d_total = nullptr;
     const uint32_t *palette = nullptr;
     uint32_t palette_len = 0, interior = 0;
-    int threads[kTiers] = {256, 256, 256}, k[kTiers] = {16, 16, 16};
+    int threads[kTiers] = {256, 256, 256}, k[kTiers] = {16, 16, 16}, chunk[kTiers] = {1, 1, 1};
     int sms = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -349,6 +362,7 @@ static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s
         a.n_vp = b->n_vp[t];
         a.n_jobs = b->n_jobs[t];
         a.counter = b->d_counters + t;
+        a.chunk = (uint32_t)b->chunk[t];
         a.total = b->d_total;
         a.palette = b->palette;
         a.palette_len = b->palette_len;
@@ -436,11 +450,12 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
         for (int t = 0; t < kTiers; t++) {
             if (cfg->block_threads[t]) b->threads[t] = (int)cfg->block_threads[t];
             if (cfg->escape_block[t]) b->k[t] = (int)cfg->escape_block[t];
+            if (cfg->chunk[t]) b->chunk[t] = (int)cfg->chunk[t];
             if (b->threads[t] % 32 || b->threads[t] < 32 || b->threads[t] > 512 ||
-                (b->k[t] != 8 && b->k[t] != 16 && b->k[t] != 32)) {
+                (b->k[t] != 8 && b->k[t] != 16 && b->k[t] != 32) || b->chunk[t] < 1 || b->chunk[t] > 64) {
                 batch_free(b);
-                return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "tier %d: threads 32..512 (multiple of 32), block 8/16/32",
-                                t);
+                return api_fail(CHAOS_ERR_INVALID_ARGUMENT,
+                                "tier %d: threads 32..512 (multiple of 32), block 8/16/32, chunk 1..64", t);
             }
         }
     }
@@ -555,5 +570,184 @@ int chaos_batch_read_total(const chaos_batch *b, unsigned long long *total)
 int chaos_batch_destroy(chaos_batch *b)
 {
     if (b) batch_free(b);
+    return CHAOS_OK;
+}
+
+// ---- autotuner ------------------------------------------------------------------
+//
+// Per tier slot present in the viewport list, time every launch shape of the
+// search space on a sample of that tier's viewports (each cut to its central
+// window of at most 96 x 96 pixels, same pixel size, samples and iteration
+// limit) and keep the fastest.  Results are cached in a text file, one line
+// per key: "<key> <threads> <escape block> <chunk> <ms>", the key being the
+// device name, its SM count, the tier slot and a hash of that tier's viewport
+// parameters.
+
+namespace {
+
+uint64_t fnv1a(uint64_t h, const void *p, size_t n)
+{
+    const unsigned char *c = static_cast<const unsigned char *>(p);
+    for (size_t k = 0; k < n; k++) {
+        h ^= c[k];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+struct TuneEntry {
+    int threads, k, chunk;
+    double ms;
+};
+
+std::vector<std::pair<std::string, TuneEntry>> read_tune_cache(const char *path)
+{
+    std::vector<std::pair<std::string, TuneEntry>> out;
+    if (!path) return out;
+    FILE *f = std::fopen(path, "r");
+    if (!f) return out;
+    char key[512];
+    TuneEntry e{};
+    while (std::fscanf(f, "%511s %d %d %d %lf", key, &e.threads, &e.k, &e.chunk, &e.ms) == 5) out.push_back({key, e});
+    std::fclose(f);
+    return out;
+}
+
+// Launch time of `vps` (one tier, forced) under one shape: the faster of two
+// launches after a warm-up.  Negative on failure.
+double time_shape(const std::vector<chaos_viewport> &vps, int slot, int threads, int k, int chunk, cudaStream_t s)
+{
+    chaos_batch_config cfg{};
+    cfg.block_threads[slot] = (uint32_t)threads;
+    cfg.escape_block[slot] = (uint32_t)k;
+    cfg.chunk[slot] = (uint32_t)chunk;
+    chaos_batch *b = nullptr;
+    if (chaos_batch_create(vps.data(), (uint32_t)vps.size(), nullptr, 0, 0, &cfg, &b) != CHAOS_OK) return -1.0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    double best = -1.0;
+    if (cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess &&
+        chaos_batch_launch(b, s) == CHAOS_OK) {
+        for (int rep = 0; rep < 2; rep++) {
+            float ms = 0.f;
+            if (cudaEventRecord(e0, s) != cudaSuccess || chaos_batch_launch(b, s) != CHAOS_OK ||
+                cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+                best = -1.0;
+                break;
+            }
+            if (best < 0 || ms < best) best = ms;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    chaos_batch_destroy(b);
+    return best;
+}
+
+}  // namespace
+
+int chaos_batch_autotune(const chaos_viewport *vps, uint32_t n, const char *cache_path, chaos_batch_config *config,
+                         uint32_t *from_cache)
+{
+    if (!vps || !config || n == 0) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "viewports and config required");
+    if (n > BATCH_MAX_VIEWPORTS) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "at most %u viewports", BATCH_MAX_VIEWPORTS);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "device properties");
+    sms = prop.multiProcessorCount;
+    std::string devname = prop.name;
+    for (char &c : devname)
+        if (c == ' ' || c == '\t') c = '_';
+
+    // the tuning sample per tier slot
+    std::vector<chaos_viewport> sample[kTiers];
+    uint64_t sig[kTiers] = {1469598103934665603ull, 1469598103934665603ull, 1469598103934665603ull};
+    size_t pixels[kTiers] = {0, 0, 0};
+    for (uint32_t k = 0; k < n; k++) {
+        const chaos_viewport &v = vps[k];
+        uint32_t tier = v.tier == CHAOS_TIER_AUTO        ? chaos_batch_auto_tier(v.center_x, v.center_y, v.pixel_size)
+                        : v.tier == CHAOS_TIER_AUTO_DEEP ? auto_deep_tier(v.center_x, v.center_y, v.pixel_size)
+                                                         : v.tier;
+        if (tier != CHAOS_TIER_F32 && tier != CHAOS_TIER_FLOATFLOAT && tier != CHAOS_TIER_F64) continue;
+        const int t = tier_slot(tier);
+        chaos_viewport c = v;
+        c.tier = tier;
+        c.width = std::min<uint32_t>(v.width, 96);
+        c.height = std::min<uint32_t>(v.height, 96);
+        c.counts = nullptr;
+        c.smooth = nullptr;
+        c.rgba = nullptr;
+        const uint32_t fields[5] = {c.width, c.height, c.samples_per_pixel, c.sample_mode, c.max_iterations};
+        sig[t] = fnv1a(sig[t], fields, sizeof(fields));
+        const double geo[3] = {c.center_x, c.center_y, c.pixel_size};
+        sig[t] = fnv1a(sig[t], geo, sizeof(geo));
+        pixels[t] += (size_t)c.width * c.height * c.samples_per_pixel;
+        sample[t].push_back(c);
+    }
+    auto cache = read_tune_cache(cache_path);
+    std::vector<std::string> new_lines;
+    *config = chaos_batch_config{};
+    bool all_cached = true;
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+        return api_fail(CHAOS_ERR_CUDA, "stream create");
+    // the counts go to one scratch buffer, viewport after viewport
+    uint32_t *scratch = nullptr;
+    size_t most = std::max(pixels[0], std::max(pixels[1], pixels[2]));
+    if (most && cudaMalloc(&scratch, most * sizeof(uint32_t)) != cudaSuccess) {
+        cudaStreamDestroy(s);
+        return api_fail(CHAOS_ERR_OUT_OF_MEMORY, "autotune scratch");
+    }
+    static const int kThreads[] = {128, 256, 512}, kBlocks[] = {8, 16, 32}, kChunks[] = {1, 2, 4};
+    int rc = CHAOS_OK;
+    for (int t = 0; t < kTiers && rc == CHAOS_OK; t++) {
+        if (sample[t].empty()) continue;
+        char key[512];
+        std::snprintf(key, sizeof(key), "%s|sm%d|slot%d|%016llx", devname.c_str(), sms, t, (unsigned long long)sig[t]);
+        bool hit = false;
+        for (auto &kv : cache)
+            if (kv.first == key) {
+                config->block_threads[t] = (uint32_t)kv.second.threads;
+                config->escape_block[t] = (uint32_t)kv.second.k;
+                config->chunk[t] = (uint32_t)kv.second.chunk;
+                hit = true;
+            }
+        if (hit) continue;
+        all_cached = false;
+        size_t off = 0;
+        for (chaos_viewport &c : sample[t]) {
+            c.counts = scratch + off;
+            off += (size_t)c.width * c.height * c.samples_per_pixel;
+        }
+        TuneEntry best{0, 0, 0, -1.0};
+        for (int th : kThreads)
+            for (int kb : kBlocks)
+                for (int ch : kChunks) {
+                    double ms = time_shape(sample[t], t, th, kb, ch, s);
+                    if (ms >= 0 && (best.ms < 0 || ms < best.ms)) best = {th, kb, ch, ms};
+                }
+        if (best.ms < 0) {
+            rc = api_fail(CHAOS_ERR_CUDA, "autotune: no launch shape ran for tier slot %d", t);
+            break;
+        }
+        config->block_threads[t] = (uint32_t)best.threads;
+        config->escape_block[t] = (uint32_t)best.k;
+        config->chunk[t] = (uint32_t)best.chunk;
+        char line[640];
+        std::snprintf(line, sizeof(line), "%s %d %d %d %.6f\n", key, best.threads, best.k, best.chunk, best.ms);
+        new_lines.push_back(line);
+    }
+    if (scratch) cudaFree(scratch);
+    cudaStreamDestroy(s);
+    if (rc != CHAOS_OK) return rc;
+    if (cache_path && !new_lines.empty()) {
+        FILE *f = std::fopen(cache_path, "a");
+        if (f) {
+            for (const std::string &l : new_lines) std::fputs(l.c_str(), f);
+            std::fclose(f);
+        }
+    }
+    if (from_cache) *from_cache = all_cached ? 1u : 0u;
     return CHAOS_OK;
 }

@@ -296,10 +296,11 @@ typedef struct chaos_viewport {
 } chaos_viewport;
 
 /* Launch shape per tier (index 0 binary32, 1 float-float, 2 binary64); zero
- * keeps the default (256 threads, 16-step escape blocks). */
+ * keeps the default (256 threads, 16-step escape blocks, chunk 1). */
 typedef struct chaos_batch_config {
     uint32_t block_threads[3]; /* 32..512, multiple of 32 */
     uint32_t escape_block[3];  /* 8, 16 or 32 */
+    uint32_t chunk[3];         /* 1..64 consecutive pixels a lane claims per work-counter update */
 } chaos_batch_config;
 
 typedef struct chaos_batch chaos_batch;
@@ -314,6 +315,18 @@ uint32_t chaos_batch_auto_tier(double center_x, double center_y, double pixel_si
  * branch of the graph. */
 int chaos_batch_create(const chaos_viewport *viewports, uint32_t n, const uint32_t *palette, uint32_t palette_len,
                        uint32_t interior_rgba, const chaos_batch_config *config, chaos_batch **out);
+/* Autotuner: for each tier slot present among the viewports (binary32,
+ * float-float, binary64; perturbation viewports are not tuned), time every
+ * launch shape of threads {128, 256, 512} x escape block {8, 16, 32} x chunk
+ * {1, 2, 4} on a sample of that tier's viewports (each cut to its central
+ * 96 x 96 window, same pixel size, samples and iteration limit) and write the
+ * fastest into *config (slots without viewports stay 0 = default).  With a
+ * cache_path, shapes found before for the same device, SM count, slot and
+ * viewport parameters are read from that text file and new ones appended;
+ * *from_cache (optional) is 1 when nothing had to be timed.  Synchronous;
+ * allocates a scratch buffer for the sample's counts. */
+int chaos_batch_autotune(const chaos_viewport *viewports, uint32_t n, const char *cache_path,
+                         chaos_batch_config *config, uint32_t *from_cache);
 /* One cudaGraphLaunch on `stream` (does not synchronise). */
 int chaos_batch_launch(chaos_batch *batch, void *stream);
 /* The tier each viewport got (n >= number of viewports). */

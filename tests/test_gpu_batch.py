@@ -69,12 +69,12 @@ def test_batch_matches_oracle(cuda, oracle):
     b.close()
 
 
-@pytest.mark.parametrize("threads,block", [(128, 8), (512, 32), (64, 16)])
-def test_batch_launch_config_does_not_change_results(cuda, oracle, threads, block):
+@pytest.mark.parametrize("threads,block,chunk", [(128, 8, 4), (512, 32, 1), (64, 16, 16)])
+def test_batch_launch_config_does_not_change_results(cuda, oracle, threads, block, chunk):
     import chaos_gb300 as cg
     from chaos_gb300.palette import seeded_palette
     pal = seeded_palette(64, seed=1)
-    cfg = cg.BatchConfig((threads, threads, threads), (block, block, block))
+    cfg = cg.BatchConfig((threads, threads, threads), (block, block, block), (chunk, chunk, chunk))
     b, bufs, _ = build(cuda, VIEWS[:6], pal, cfg)
     got = run(cuda, b, bufs)
     b2, bufs2, _ = build(cuda, VIEWS[:6], pal)
@@ -90,6 +90,41 @@ def test_batch_rejects_bad_config(cuda):
         build(cuda, VIEWS[:2], seeded_palette(16), cg.BatchConfig((100, 0, 0), (0, 0, 0)))
     with pytest.raises(cg.ChaosError):
         build(cuda, VIEWS[:2], seeded_palette(16), cg.BatchConfig((0, 0, 0), (12, 0, 0)))
+    with pytest.raises(cg.ChaosError):
+        build(cuda, VIEWS[:2], seeded_palette(16), cg.BatchConfig((0, 0, 0), (0, 0, 0), (0, 65, 0)))
+
+
+def test_autotune_picks_a_shape_and_caches_it(cuda, tmp_path):
+    """The autotuner returns a shape from its search space for each tier slot
+    present, the batch built with it gives the default shape's bits, and a
+    second call with the same cache file times nothing."""
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import seeded_palette
+    pal = seeded_palette(64, seed=2)
+    views = VIEWS[:6]
+    b, bufs, _ = build(cuda, views, pal)
+    ref = run(cuda, b, bufs)
+    tiers = b.tiers()
+    b.close()
+    cache = str(tmp_path / "tune.txt")
+    vps = [cg.Viewport(width=w, height=h, max_iterations=mi, samples_per_pixel=spp, sample_mode=mode, tier=t,
+                       seed=17 + w, center_x=c[0], center_y=c[1], pixel_size=span / w)
+           for w, h, spp, mode, mi, t, c, span in views]
+    cfg, hit = cg.autotune_batch(vps, cache)
+    assert not hit
+    slots = {0: 0, 2: 1, 1: 2}  # tier id -> config slot
+    for t in set(tiers):
+        k = slots[t]
+        assert cfg.block_threads[k] in (128, 256, 512) and cfg.escape_block[k] in (8, 16, 32)
+        assert cfg.chunk[k] in (1, 2, 4)
+    cfg2, hit2 = cg.autotune_batch(vps, cache)
+    assert hit2 and bytes(cfg2) == bytes(cfg)
+    assert len(open(cache).read().splitlines()) == len(set(tiers))
+    b2, bufs2, _ = build(cuda, views, pal, cfg)
+    got = run(cuda, b2, bufs2)
+    for (c1, _, r1), (c2, _, r2) in zip(ref, got):
+        assert np.array_equal(c1, c2) and np.array_equal(r1, r2)
+    b2.close()
 
 
 DEEP_VIEWS = [
