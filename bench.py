@@ -412,6 +412,12 @@ def run_batch(args):
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
     specs = c4_viewports()
+    if args.workload == "c4-crop":
+        # the central 256 x 256 window of each viewport at the same pixel size (profiler captures)
+        for sp in specs:
+            side = min(sp["width"], 256)
+            sp["span"] = sp["span"] * side / sp["width"]
+            sp["width"] = sp["height"] = side
     pal = c4_palette()
     dpal = torch.from_numpy(pal.view(np.int32)).to(dev)
 
@@ -567,7 +573,8 @@ def run_batch(args):
             "data": "synthetic: seeded viewports and boundary centres",
             "config": {"workload": "C4: 64 Mandelbrot viewports, side log-uniform 256..2048, span log-uniform "
                                    "1e-12..1e-3, maxIter log-uniform 500..50000, one CUDA-graph launch",
-                       "pixels": total, "l2": "flushed between launches"},
+                       "pixels": total, "l2": "flushed between launches",
+                       "crop": "central 256x256 of each viewport" if args.workload == "c4-crop" else None},
             "tiers": {"f32": tiers.count(0), "floatfloat": tiers.count(2), "f64": tiers.count(1)},
             "pixel_iterations_per_step": per_launch,
             "plain_f64_dropin": {"value": dropin_value, "ms": dm_ms, "speedup_of_tiered": value / dropin_value,
@@ -828,8 +835,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["c2", "c2-crop", "c3", "c4", "c5"], default="c2",
-                    help="c2-crop: the central 480x270 pixels of the same frame (for profiler captures)")
+    ap.add_argument("--workload", choices=["c2", "c2-crop", "c3", "c4", "c4-crop", "c5"], default="c2",
+                    help="c2-crop / c4-crop: the central 480x270 pixels of the frame / 256x256 of each viewport "
+                         "(for profiler captures)")
     args = ap.parse_args()
     if args.workload == "c2-crop":
         global W, H
@@ -838,7 +846,7 @@ def main():
         run_reference(args)
     elif args.workload == "c3":
         run_deep(args)
-    elif args.workload == "c4":
+    elif args.workload in ("c4", "c4-crop"):
         run_batch(args)
     elif args.workload == "c5":
         run_serve(args)
