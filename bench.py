@@ -326,9 +326,11 @@ def run_ours(args):
 
     # roofline: FP64 pipe
     peak = cg.measure_fma_peak(cg.TIER_F64)  # FLOP/s with an FMA = 2
-    # rounded arithmetic: x*x, y*y, xx-yy, +cx, x+x, *y, +cy = 7 FP64-pipe
-    # instructions per untested step; the escape test adds 1 add per 16 steps
-    ops_per_iter = 7
+    # rounded arithmetic as the kernel runs it: x*x, y*y, xx-yy, +cx, x*y,
+    # fma(2, x*y, cy) = 6 FP64-pipe instructions per untested step (the
+    # reference's literal (2x)*y + cy is 7; both round identically, see
+    # step_rounded6); the escape test adds 3 per 16-step block
+    ops_per_iter = 6
     achieved_ops = iters_per_frame / (kernel_ms / args.steps / 1e3) * ops_per_iter
     roof = {"bound": "fp64-pipe", "achieved": achieved_ops / 1e12, "peak": peak / 2 / 1e12, "unit": "Top/s",
             "frac": achieved_ops / (peak / 2), "traffic": None,

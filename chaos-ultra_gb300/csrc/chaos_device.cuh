@@ -114,6 +114,30 @@ template <class R, int A> __device__ __forceinline__ void step(R &x, R &y, R cx,
     }
 }
 
+// The rounded step in 6 operations instead of 7: y' = fma(2, round(x*y), cy).
+// Doubling is exact, so round((2x)*y) = 2 round(x*y) whenever round(x*y) is at
+// least twice the smallest normal number, and the fused add rounds 2p + cy
+// once, as the reference's add does.  emin collects the exponent field of
+// every product (integer ops, off the floating-point pipe and off the step's
+// dependency chain); a block whose emin is below 2 (a product that small) is
+// redone with step<R, ARITH_PARITY>.
+__device__ __forceinline__ uint32_t exponent_bits(float p) { return __float_as_uint(p) & 0x7f800000u; }
+__device__ __forceinline__ uint32_t exponent_bits(double p) { return (uint32_t)__double2hiint(p) & 0x7ff00000u; }
+template <class R> __device__ __forceinline__ uint32_t exponent_bits_two();
+template <> __device__ __forceinline__ uint32_t exponent_bits_two<float>() { return 2u << 23; }
+template <> __device__ __forceinline__ uint32_t exponent_bits_two<double>() { return 2u << 20; }
+
+template <class R> __device__ __forceinline__ void step_rounded6(R &x, R &y, R cx, R cy, uint32_t &emin)
+{
+    using O = Op<R>;
+    R xx = O::mul(x, x), yy = O::mul(y, y);
+    R xn = O::add(O::sub(xx, yy), cx);
+    R p = O::mul(x, y);
+    y = O::fma(R(2), p, cy);
+    x = xn;
+    emin = min(emin, exponent_bits(p));
+}
+
 // Escape loop with the reference's semantics:
 //     i = 0; while (i < max_iter && r2(z) < 4) { z = z^2 + c; ++i; }  return i
 // run as blocks of ESCAPE_BLOCK untested steps.  A block is kept when its last

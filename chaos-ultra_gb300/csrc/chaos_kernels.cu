@@ -169,13 +169,13 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
         const bool stepping = active && !done;
         const bool partial = stepping && lim < (uint32_t)K;
         const bool any_partial = __any_sync(FULL, partial);
-        if (stepping) {
-            const R sx = x, sy = y;
+        // K steps of `stepper`, keeping the state after lim steps on partial lanes
+        auto run_block = [&](auto stepper) {
             if (any_partial) {
                 R kx = x, ky = y;
 #pragma unroll
                 for (int k = 0; k < K; k++) {
-                    step<R, A>(x, y, cx, cy);
+                    stepper(x, y);
                     if (((k + 1) & k) == 0 && k + 1 < K && (uint32_t)(k + 1) == lim) {
                         kx = x;
                         ky = y;
@@ -187,7 +187,22 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
                 }
             } else {
 #pragma unroll
-                for (int k = 0; k < K; k++) step<R, A>(x, y, cx, cy);
+                for (int k = 0; k < K; k++) stepper(x, y);
+            }
+        };
+        if (stepping) {
+            const R sx = x, sy = y;
+            if constexpr (A == ARITH_PARITY) {
+                uint32_t emin = 0xffffffffu;
+                run_block([&](R &u, R &v) { step_rounded6<R>(u, v, cx, cy, emin); });
+                if (emin < exponent_bits_two<R>()) {
+                    // a product below twice the smallest normal: redo the block literally
+                    x = sx;
+                    y = sy;
+                    run_block([&](R &u, R &v) { step<R, A>(u, v, cx, cy); });
+                }
+            } else {
+                run_block([&](R &u, R &v) { step<R, A>(u, v, cx, cy); });
             }
             r2 = radius2<R, A>(x, y);
             if (r2 < R(4)) {

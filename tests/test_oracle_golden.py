@@ -116,3 +116,30 @@ def test_newton_colorize(oracle, golden):
         pix["value"][0] = [c["value"] for c in cases]
         got = oracle.compose_mode(pix, pal, mode, mag)[0]
         assert got.tolist() == [c["rgba"] for c in cases], kind
+
+
+def test_rounded_step_doubling_identity():
+    """The kernels' rounded step computes (2x)*y + cy as fma(2, x*y, cy): equal
+    whenever x*y rounds to at least 2^-1021 (the kernels take the literal form
+    below that).  Checked on random and edge operands with the C library's fma."""
+    import ctypes
+
+    import numpy as np
+    libm = ctypes.CDLL("libm.so.6")
+    libm.fma.restype = ctypes.c_double
+    libm.fma.argtypes = [ctypes.c_double] * 3
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([rng.uniform(-2, 2, 3000), rng.standard_normal(1000) * 1e-150,
+                         np.ldexp(rng.uniform(1, 2, 1000), rng.integers(-520, -500, 1000))])
+    ys = np.concatenate([rng.uniform(-2, 2, 3000), rng.standard_normal(1000) * 1e-150,
+                         np.ldexp(rng.uniform(1, 2, 1000), rng.integers(-520, -500, 1000))])
+    cys = np.concatenate([rng.uniform(-2, 2, 3000), rng.uniform(-1e-300, 1e-300, 1000),
+                          np.ldexp(rng.uniform(-2, 2, 1000), rng.integers(-1030, -1000, 1000))])
+    checked = 0
+    for x, y, cy in zip(xs.tolist(), ys.tolist(), cys.tolist()):
+        p = x * y
+        if p != 0.0 and abs(p) < 2.0 ** -1021:
+            continue  # the literal form runs there
+        assert libm.fma(2.0, p, cy) == (2.0 * x) * y + cy, (x, y, cy)
+        checked += 1
+    assert checked > 4000
