@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/chaos_gb300.h"
@@ -162,6 +163,18 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
                 i = 0;
                 window = 0;
                 if (max_iter == 0) done = true;
+                if constexpr (std::is_same<N, double>::value) {
+                    // start at z = c, the first step's result (+0 for -0), so that no
+                    // block begins with x = 0 (which the integer doubling redoes)
+                    if (max_iter > 0) {
+                        x = __dadd_rn(cx, 0.0);
+                        y = __dadd_rn(cy, 0.0);
+                        i = 1;
+                        const double rr = P::r2(x, y);
+                        r2 = (float)rr;
+                        if (i == max_iter || !(rr < 4.0)) done = true;
+                    }
+                }
             }
             if (!done) {
                 if (!blk) {
@@ -177,13 +190,13 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
         const bool stepping = active && !done;
         const bool partial = stepping && lim < (uint32_t)K;
         const bool any_partial = __any_sync(FULLM, partial);
-        if (stepping) {
-            const T sx = x, sy = y;
+        // K steps of `stepper`, keeping the state after lim steps on partial lanes
+        auto run_block = [&](auto stepper) {
             if (any_partial) {
                 T kx = x, ky = y;
 #pragma unroll
                 for (int k = 0; k < K; k++) {
-                    P::step(x, y, cx, cy);
+                    stepper(x, y);
                     if (((k + 1) & k) == 0 && k + 1 < K && (uint32_t)(k + 1) == lim) {
                         kx = x;
                         ky = y;
@@ -195,7 +208,22 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
                 }
             } else {
 #pragma unroll
-                for (int k = 0; k < K; k++) P::step(x, y, cx, cy);
+                for (int k = 0; k < K; k++) stepper(x, y);
+            }
+        };
+        if (stepping) {
+            const T sx = x, sy = y;
+            if constexpr (std::is_same<N, double>::value) {
+                // 2x on the integer pipe; blocks it cannot double exactly are redone
+                uint32_t emin = 0xffffffffu;
+                run_block([&](T &u, T &v) { step_fma3(u, v, cx, cy, emin); });
+                if (emin == 0u) {
+                    x = sx;
+                    y = sy;
+                    run_block([&](T &u, T &v) { P::step(u, v, cx, cy); });
+                }
+            } else {
+                run_block([&](T &u, T &v) { P::step(u, v, cx, cy); });
             }
             auto rr = P::r2(x, y);
             r2 = (float)rr;

@@ -138,6 +138,29 @@ template <class R> __device__ __forceinline__ void step_rounded6(R &x, R &y, R c
     emin = min(emin, exponent_bits(p));
 }
 
+// The binary64 fused step with 2x formed on the integer pipe: adding 1 to the
+// exponent field doubles a normal number exactly, and x + x is the binary64
+// pipe's fourth operation per step.  emin collects the exponent field of
+// every x; a block that met x = 0 or a subnormal x (field 0) is redone with
+// step<double, ARITH_FMA>.  At the top of the range the integer doubling
+// gives inf or NaN where 2x overflows (a NaN where x + x gives inf): both
+// only arise after an escape and never test below 4, which is all the
+// blocked escape loop asks of the steps past an escape.  Everything else is
+// step<double, ARITH_FMA> bit for bit.
+__device__ __forceinline__ double twice_on_int(double x, uint32_t &emin)
+{
+    const int hi = __double2hiint(x), lo = __double2loint(x);
+    emin = min(emin, (uint32_t)hi & 0x7ff00000u);
+    return __hiloint2double(hi + 0x00100000, lo);
+}
+__device__ __forceinline__ void step_fma3(double &x, double &y, double cx, double cy, uint32_t &emin)
+{
+    double t = __fma_rn(-y, y, cx);
+    double xn = __fma_rn(x, x, t);
+    y = __fma_rn(twice_on_int(x, emin), y, cy);
+    x = xn;
+}
+
 // Escape loop with the reference's semantics:
 //     i = 0; while (i < max_iter && r2(z) < 4) { z = z^2 + c; ++i; }  return i
 // run as blocks of ESCAPE_BLOCK untested steps.  A block is kept when its last

@@ -134,11 +134,20 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
                 begin = false;
                 R px, py;
                 frame_point(a, pix, s, px, py);
+                i = 0;
                 if (F == FRACTAL_MANDELBROT) {
-                    x = R(0);
-                    y = R(0);
                     cx = px;
                     cy = py;
+                    // the first step from z = 0 gives z = c (+0 in place of -0, as the
+                    // step's own additions do); starting there spares every sample a
+                    // step whose products are 0
+                    x = R(0);
+                    y = R(0);
+                    if (a.max_iter > 0) {
+                        x = Op<R>::add(cx, R(0));
+                        y = Op<R>::add(cy, R(0));
+                        i = 1;
+                    }
                 } else {
                     x = px;
                     y = py;
@@ -146,10 +155,9 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
                     cy = a.jcy;
                 }
                 blk = blockable_c(cx, cy);
-                i = 0;
                 window = 0;
                 r2 = radius2<R, A>(x, y);
-                if (a.max_iter == 0 || !(r2 < R(4))) done = true;
+                if (i == a.max_iter || !(r2 < R(4))) done = true;
             }
             if (!done) {
                 if (!blk) {
@@ -197,6 +205,15 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
                 run_block([&](R &u, R &v) { step_rounded6<R>(u, v, cx, cy, emin); });
                 if (emin < exponent_bits_two<R>()) {
                     // a product below twice the smallest normal: redo the block literally
+                    x = sx;
+                    y = sy;
+                    run_block([&](R &u, R &v) { step<R, A>(u, v, cx, cy); });
+                }
+            } else if constexpr (sizeof(R) == 8) {
+                uint32_t emin = 0xffffffffu;
+                run_block([&](R &u, R &v) { step_fma3(u, v, cx, cy, emin); });
+                if (emin == 0u) {
+                    // x = 0 or subnormal: redo the block with x + x
                     x = sx;
                     y = sy;
                     run_block([&](R &u, R &v) { step<R, A>(u, v, cx, cy); });
