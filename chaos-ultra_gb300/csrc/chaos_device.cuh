@@ -172,20 +172,44 @@ __device__ __forceinline__ void step_fma3(double &x, double &y, double cx, doubl
 // tests below 4, so a block whose last state tests below 4 contains no
 // escape.  Otherwise `blockable` is false and every step is tested.
 // r2_exit is r2 of the final state.
+// Binary64 blocks run step_rounded6 / step_fma3 (the same values as step<>)
+// and are redone with step<> when the integer checks ask for it.  i0 is the
+// iteration count of the state passed in (1 when a Mandelbrot caller starts
+// at z1 = c).
 template <class R, int A>
-__device__ __forceinline__ uint32_t escape(uint32_t max_iter, R x, R y, R cx, R cy, bool blockable, R &r2_exit)
+__device__ __forceinline__ uint32_t escape(uint32_t max_iter, R x, R y, R cx, R cy, bool blockable, R &r2_exit,
+                                           uint32_t i0 = 0)
 {
     R r2 = radius2<R, A>(x, y);
-    if (max_iter == 0 || !(r2 < R(4))) {
+    if (i0 >= max_iter || !(r2 < R(4))) {
         r2_exit = r2;
-        return 0;
+        return i0 < max_iter ? i0 : max_iter;
     }
-    uint32_t i = 0;
+    uint32_t i = i0;
     if (blockable) {
         while (max_iter - i >= (uint32_t)ESCAPE_BLOCK) {
             R sx = x, sy = y;
+            bool redo = false;
+            if constexpr (sizeof(R) == 8 && A == ARITH_PARITY) {
+                uint32_t emin = 0xffffffffu;
 #pragma unroll
-            for (int k = 0; k < ESCAPE_BLOCK; k++) step<R, A>(x, y, cx, cy);
+                for (int k = 0; k < ESCAPE_BLOCK; k++) step_rounded6<R>(x, y, cx, cy, emin);
+                redo = emin < exponent_bits_two<R>();
+            } else if constexpr (sizeof(R) == 8) {
+                uint32_t emin = 0xffffffffu;
+#pragma unroll
+                for (int k = 0; k < ESCAPE_BLOCK; k++) step_fma3(x, y, cx, cy, emin);
+                redo = emin == 0u;
+            } else {
+#pragma unroll
+                for (int k = 0; k < ESCAPE_BLOCK; k++) step<R, A>(x, y, cx, cy);
+            }
+            if (redo) {
+                x = sx;
+                y = sy;
+#pragma unroll
+                for (int k = 0; k < ESCAPE_BLOCK; k++) step<R, A>(x, y, cx, cy);
+            }
             if (!(radius2<R, A>(x, y) < R(4))) {
                 x = sx;
                 y = sy;
@@ -216,7 +240,10 @@ template <class R, int A, int F> __device__ __forceinline__ uint32_t compute_fra
 {
     R r2;
     if (F == FRACTAL_MANDELBROT) {
-        uint32_t i = escape<R, A>(max_iter, R(0), R(0), px, py, blockable_c(px, py), r2);
+        // from z1 = c, the first step's exact result (+0 in place of -0)
+        uint32_t i = max_iter == 0 ? 0u
+                                   : escape<R, A>(max_iter, Op<R>::add(px, R(0)), Op<R>::add(py, R(0)), px, py,
+                                                  blockable_c(px, py), r2, 1u);
         return i == max_iter ? 0u : i;
     }
     return escape<R, A>(max_iter, px, py, jcx, jcy, blockable_c(jcx, jcy), r2);
