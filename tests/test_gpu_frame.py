@@ -111,3 +111,32 @@ def test_tiny_and_ragged_frames(cuda, oracle):
         g = run_frame(cuda, w, h, 300, 3, cg.SAMPLES_JITTER, cg.TIER_F32, cg.ARITH_FMA, seed=5, ps=0.01)
         o = oracle.frame(w, h, 300, 3, 1, False, cg.ARITH_FMA, MANDELBROT, 5, (-0.5, 0.0), 0.01)
         assert np.array_equal(g["counts"], o["counts"]), (w, h)
+
+
+@pytest.mark.parametrize("center", [(0.0, 0.0), (-0.75, 0.0), (-1.25, 0.0), (0.0, 0.75)])
+@pytest.mark.parametrize("tier", [0, 1])
+@pytest.mark.parametrize("arith", [0, 1])
+def test_axis_pixels_exact(cuda, oracle, center, tier, arith):
+    """Odd-sized frames whose middle row and column sit exactly on the axes
+    (c = x + 0i, c = 0 + iy): x or x*y is exactly 0 on every step there, the
+    case where the binary64 kernels fall back from the fused six-op rounded
+    step and the integer doubling to the literal step."""
+    import chaos_gb300 as cg
+    w, h, mi = 101, 77, 700
+    ps = 0.9 / w
+    g = run_frame(cuda, w, h, mi, 1, cg.SAMPLES_CENTER, tier, arith, center=center, ps=ps)
+    o = oracle.frame(w, h, mi, 1, 0, tier == 1, arith, MANDELBROT, 0, center, ps)
+    assert np.array_equal(g["counts"], o["counts"])
+    assert g["total"] == int(o["counts"].astype(np.int64).sum())
+
+
+@pytest.mark.parametrize("arith", [0, 1])
+def test_julia_through_origin_exact(cuda, oracle, arith):
+    """Julia frames whose pixel grid contains z0 = 0 and the axes."""
+    import chaos_gb300 as cg
+    w, h = 81, 61
+    for jc in ((-0.8, 0.156), (0.0, 0.8), (-1.0, 0.0)):
+        g = run_frame(cuda, w, h, 500, 1, cg.SAMPLES_CENTER, cg.TIER_F64, arith, fractal=JULIA, center=(0.0, 0.0),
+                      ps=3.0 / w, julia_c=jc)
+        o = oracle.frame(w, h, 500, 1, 0, True, arith, JULIA, 0, (0.0, 0.0), 3.0 / w, julia_c=jc)
+        assert np.array_equal(g["counts"], o["counts"]), jc
