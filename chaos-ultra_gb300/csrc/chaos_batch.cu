@@ -32,6 +32,7 @@ int api_perturb_enqueue(const chaos_frame_desc *desc, const chaos_orbit *orbit, 
 struct BatchViewport {
     uint32_t w, h, spp, mode, max_iter;
     uint32_t job_base;  // first job of this viewport in its tier's job space
+    uint32_t w_magic;   // div_magic(w)
     uint64_t seed;
     double center_x, center_y, ps;
     uint32_t *counts;
@@ -147,7 +148,8 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
             if (begin) {
                 begin = false;
                 const BatchViewport &v = a.vps[vp];
-                uint32_t px = pix % v.w, py = pix / v.w;
+                uint32_t px, py;
+                divmod_magic(pix, v.w, v.w_magic, py, px);
                 double ox = 0.5, oy = 0.5;
                 if (v.mode == SAMPLES_JITTER) {
                     ox = unit_interval_t<double>(sample_hash(v.seed, pix, s, 0));
@@ -446,6 +448,7 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
         int t = tier_slot(tier);
         BatchViewport bv{};
         bv.w = v.width;
+        bv.w_magic = div_magic(v.width);
         bv.h = v.height;
         bv.spp = v.samples_per_pixel;
         bv.mode = v.sample_mode;

@@ -66,6 +66,24 @@ constexpr uint32_t ADAPTIVE_THRESHOLD = 10;  // gen.cu:93
 // Iterations run between two escape tests on the fast path (see escape()).
 constexpr int ESCAPE_BLOCK = 16;
 
+// n / d and n % d for a divisor fixed per launch: m = floor(2^32 / d) (2^32 - 1
+// for d = 1) gives a quotient at most one short for any 32-bit n, fixed by one
+// comparison -- a multiply-high and a few integer operations instead of a
+// division.
+__host__ __device__ __forceinline__ uint32_t div_magic(uint32_t d)
+{
+    return d <= 1u ? 0xffffffffu : (uint32_t)(0x100000000ull / d);
+}
+__device__ __forceinline__ void divmod_magic(uint32_t n, uint32_t d, uint32_t m, uint32_t &q, uint32_t &r)
+{
+    q = __umulhi(n, m);
+    r = n - q * d;
+    if (r >= d) {
+        ++q;
+        r -= d;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Correctly rounded scalar operations.  Every product and sum is rounded on its
 // own unless an fma is written out, so the compiler cannot contract (the

@@ -135,6 +135,7 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
 
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt_mask = (1u << lane) - 1u;
+    const uint32_t w_magic = div_magic(a.w);
     uint32_t pix = 0xffffffffu, s = 0, i = 0, m = 0;
     // rescaled samples keep w in (dx, dy) and u in (dcx, dcy), with d = w 2^e
     D dx = D(0), dy = D(0), dcx = D(0), dcy = D(0), Zx = D(0), Zy = D(0);
@@ -168,7 +169,8 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
         if (active) {
             if (begin) {
                 begin = false;
-                uint32_t px = pix % a.w, py = pix / a.w;
+                uint32_t px, py;
+                divmod_magic(pix, a.w, w_magic, py, px);
                 double ox = 0.5, oy = 0.5;
                 if (a.mode == SAMPLES_JITTER) {
                     ox = unit53(sample_hash(a.seed, pix, s, 0));
@@ -349,7 +351,8 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
             }
             ++s;
             if (s == a.spp) {
-                uint32_t px = pix % a.w, py = pix / a.w;
+                uint32_t px, py;
+                divmod_magic(pix, a.w, w_magic, py, px);
                 if (a.pixels)
                     store_pixel(pixel_ptr(a.pixels, a.pixels_pitch, px, py),
                                 make_pixel(__fdiv_rn(acc_v, (float)a.spp), (float)a.spp));

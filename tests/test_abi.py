@@ -233,3 +233,23 @@ def test_newton_module_params(native):
     with pytest.raises(cg.ChaosError) as e:
         w.write_constant("roots", np.zeros(6).tobytes())
     assert e.value.code == 4
+
+
+def test_pixel_divmod_by_magic_number():
+    """The kernels split a pixel index n into (n / w, n % w) as q = mulhi(n,
+    floor(2^32 / w)) plus one correction (chaos_device.cuh divmod_magic):
+    exact for every 32-bit n, here on random and edge cases."""
+    import random
+    rng = random.Random(3)
+    divisors = [1, 2, 3, 7, 255, 256, 1000, 1023, 1920, 3840, 4095, 65535, 65536, 99991, 2**31 - 1, 2**31, 2**32 - 1]
+    divisors += [rng.randrange(1, 1 << 20) for _ in range(200)]
+    for d in divisors:
+        m = 0xFFFFFFFF if d <= 1 else (1 << 32) // d
+        for n in [0, 1, d - 1, d, d + 1, 2**31 - 1, 2**32 - 1] + [rng.randrange(0, 1 << 32) for _ in range(50)]:
+            n &= 0xFFFFFFFF
+            q = (n * m) >> 32
+            r = (n - q * d) & 0xFFFFFFFF
+            if r >= d:
+                q += 1
+                r -= d
+            assert (q, r) == divmod(n, d), (n, d)
