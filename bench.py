@@ -601,6 +601,123 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+C1_N, C1_MAX_ITER, C1_TOTAL, C1_INTERIOR = 1024, 1000, 181_032_650, 175_986
+
+
+def run_c1(args):
+    """C1: plain Mandelbrot 1024x1024 in binary32, centre (-0.5, 0), span 3.0,
+    maxIter 1000, one sample per pixel centre, escape counts + smooth counts.
+    The headline tier is binary32 with the reference's rounding (bit-exact to
+    its computeFractal<float>: 181,032,650 pixel-iterations, 175,986 interior
+    pixels); the fused tier is reported beside it.  The CPU leg runs the
+    reference's own host-built computeFractal<float> over the whole frame."""
+    import numpy as np
+    import torch
+
+    import chaos_gb300 as cg
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    n = C1_N * C1_N
+    counts = torch.zeros(n, dtype=torch.int32, device=dev)
+    smooth = torch.zeros(n, dtype=torch.float32, device=dev)
+    total = torch.zeros(1, dtype=torch.int64, device=dev)
+    out = cg.FrameOut(counts=counts.data_ptr(), smooth=smooth.data_ptr(), total_iterations=total.data_ptr())
+    stream = torch.cuda.current_stream()
+    flush = _l2_flush(torch, dev)
+
+    def desc(arith):
+        return cg.FrameDesc(width=C1_N, height=C1_N, max_iterations=C1_MAX_ITER, samples_per_pixel=1,
+                            sample_mode=cg.SAMPLES_CENTER, tier=cg.TIER_F32, arith=arith, fractal=cg.MANDELBROT,
+                            seed=0, center_x=-0.5, center_y=0.0, pixel_size=3.0 / C1_N)
+
+    def timed(arith, steps, warmup):
+        d = desc(arith)
+        for _ in range(warmup):
+            cg.render_frame(d, out, stream=stream, sync=False)
+        torch.cuda.synchronize()
+        total.zero_()
+        ev = []
+        for k in range(steps):
+            flush(k)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            cg.render_frame(d, out, stream=stream, sync=False)
+            e1.record(stream)
+            ev.append((e0, e1))
+        torch.cuda.synchronize()
+        return int(total.item()), sum(a.elapsed_time(b) for a, b in ev)
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    iters, ms = timed(cg.ARITH_PARITY, args.steps, args.warmup)
+    clk = clocks.stop()
+    per_frame = iters // args.steps
+    c = counts.cpu().numpy().view(np.uint32)
+    known = {"pixel_iterations": per_frame, "interior": int((c == C1_MAX_ITER).sum()),
+             "matches_reference_known_answer": per_frame == C1_TOTAL and int((c == C1_MAX_ITER).sum()) == C1_INTERIOR}
+    value = iters / (ms / 1e3) / 1e9
+    f_iters, f_ms = timed(cg.ARITH_FMA, max(args.steps, 3), 1)
+
+    # end to end through the host-buffer call (palette in, RGBA image out)
+    from chaos_gb300.palette import seeded_palette
+    pal = seeded_palette(256, seed=1)
+    host = torch.empty(n, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    d = desc(cg.ARITH_PARITY)
+    cg.render_frame_host(d, pal, 0xFF000000, host)
+    e0 = time.perf_counter()
+    e_iters = sum(cg.render_frame_host(d, pal, 0xFF000000, host) for _ in range(args.steps))
+    e_s = time.perf_counter() - e0
+
+    # roofline: FP32 pipe against the plain step's 6 instructions (the binary32
+    # rounded step itself is the reference's literal 7: x*x, y*y, -, +cx, 2*x, *y, +cy)
+    peak = cg.measure_fma_peak(cg.TIER_F32)
+    ops = 6
+    achieved = per_frame / (ms / args.steps / 1e3) * ops
+    roof = {"bound": "fp32-pipe", "achieved": achieved / 1e12, "peak": peak / 2 / 1e12, "unit": "Top/s",
+            "frac": achieved / (peak / 2), "traffic": None, "ops_per_iteration": ops,
+            "peak_source": "measured in this run: chaos_measure_fma_peak (full-occupancy FFMA chains)",
+            "kernel": "k_frame<float,PARITY,mandelbrot,32>"}
+
+    # CPU leg: the reference's computeFractal<float> over the whole frame, all host threads
+    cpu = None
+    try:
+        from oracle import build_oracle
+        from oracle.oracle import REF_LIB, Reference
+        build_oracle.build_oracle()
+        try:
+            build_oracle.build_reference()
+        except RuntimeError:
+            pass
+        if os.path.exists(REF_LIB):
+            ref = Reference()
+            t0 = time.perf_counter()
+            tot, _ = ref.grid(False, C1_N, C1_N, -2.0 + 0.5 * 3.0 / C1_N, 1.5 - 0.5 * 3.0 / C1_N, 3.0 / C1_N,
+                              3.0 / C1_N, C1_MAX_ITER, counts=False)
+            dt = time.perf_counter() - t0
+            cpu = {"value": tot / dt / 1e9, "unit": "Gpixel-iter/s", "cores": ref.max_threads(),
+                   "kind": "reference",
+                   "sample": f"the whole frame ({tot} pixel-iterations, reference computeFractal<float>) "
+                             f"in {dt:.3f} s"}
+    except (ImportError, OSError):
+        cpu = None
+
+    line = {"metric": "Gpixel-iter/s (plain binary32 frame)", "value": value, "unit": "Gpixel-iter/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: the C1 plane rectangle",
+            "config": {"workload": f"C1: Mandelbrot {C1_N}x{C1_N} binary32, centre (-0.5, 0), span 3.0, maxIter "
+                                   f"{C1_MAX_ITER}, 1 sample per pixel centre", "arith": "rounded (reference)",
+                       "l2": "flushed between steps"},
+            "known_answer": known,
+            "tiers": {"f32-fma": {"value": f_iters / (f_ms / 1e3) / 1e9, "unit": "Gpixel-iter/s"}},
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e_iters / e_s / 1e9, "unit": "Gpixel-iter/s", "h2d_bytes_per_step": 4 * len(pal),
+                    "d2h_bytes_per_step": 4 * n + 8, "call": "chaos_render_frame_host"},
+            "gpu_launches": args.steps, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 DEEP_W, DEEP_H, DEEP_MAX_ITER, DEEP_SPANS, DEEP_ORBIT_BITS = 1920, 1080, 100000, (1e-60, 1e-200), 1088
 
 
@@ -837,7 +954,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["c2", "c2-crop", "c3", "c4", "c4-crop", "c5"], default="c2",
+    ap.add_argument("--workload", choices=["c1", "c2", "c2-crop", "c3", "c4", "c4-crop", "c5"], default="c2",
                     help="c2-crop / c4-crop: the central 480x270 pixels of the frame / 256x256 of each viewport "
                          "(for profiler captures)")
     args = ap.parse_args()
@@ -846,6 +963,8 @@ def main():
         W, H = 480, 270
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c1":
+        run_c1(args)
     elif args.workload == "c3":
         run_deep(args)
     elif args.workload in ("c4", "c4-crop"):

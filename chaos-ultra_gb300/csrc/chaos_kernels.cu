@@ -203,7 +203,9 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
         };
         if (stepping) {
             const R sx = x, sy = y;
-            if constexpr (A == ARITH_PARITY) {
+            if constexpr (A == ARITH_PARITY && sizeof(R) == 8) {
+                // binary64: one binary64 operation fewer per step for two integer ones
+                // (binary32 keeps the literal step: there the integer pipe is the busier one)
                 uint32_t emin = 0xffffffffu;
                 run_block([&](R &u, R &v) { step_rounded6<R>(u, v, cx, cy, emin); });
                 if (emin < exponent_bits_two<R>()) {
