@@ -587,6 +587,7 @@ def run_batch(args):
                          "shape": {name: {"threads": tuned.block_threads[k], "escape_block": tuned.escape_block[k],
                                           "chunk": tuned.chunk[k]}
                                    for k, name in enumerate(("f32", "floatfloat", "f64"))},
+                         "fp64_warps_per_sm_when_shared": tuned.fp64_warps_per_sm,
                          "default_shape_ms": min(u_ms), "tuned_ms": min(ms),
                          "default_shape_value": per_launch / (min(u_ms) / 1e3) / 1e9},
             "tiered_deep": {"value": deep_value, "ms": min(deep_ms),
@@ -597,7 +598,8 @@ def run_batch(args):
                                     "(orbits computed at batch creation, outside the timed launch)"},
             "per_tier": per_tier,
             "escape_count_mismatch_vs_f64_batch": diff / total,
-            "gpu_launches": args.steps, "clocks": clk}
+            "gpu_launches": args.steps * sum(1 for t in (0, 1, 2) if t in tiers),
+            "gpu_launches_note": "one persistent kernel per tier present per graph launch", "clocks": clk}
     print(json.dumps(line), flush=True)
 
 

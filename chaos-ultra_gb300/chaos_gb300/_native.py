@@ -98,7 +98,8 @@ class Viewport(C.Structure):
 
 
 class BatchConfig(C.Structure):
-    _fields_ = [("block_threads", C.c_uint32 * 3), ("escape_block", C.c_uint32 * 3), ("chunk", C.c_uint32 * 3)]
+    _fields_ = [("block_threads", C.c_uint32 * 3), ("escape_block", C.c_uint32 * 3), ("chunk", C.c_uint32 * 3),
+                ("fp64_warps_per_sm", C.c_uint32)]
 
 
 TIER_AUTO = 255

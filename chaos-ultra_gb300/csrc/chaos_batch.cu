@@ -95,6 +95,9 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
     for (uint32_t k = threadIdx.x; k < a.n_vp; k += blockDim.x) s_base[k] = a.vps[k].job_base;
     if (threadIdx.x == 0) s_base[a.n_vp] = a.n_jobs;
     __syncthreads();
+    // a kernel launched after this one with programmatic serialization (the next
+    // tier sharing the SMs) may start now: it reads nothing this kernel writes
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt_mask = (1u << lane) - 1u;
@@ -279,13 +282,23 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) iters += __shfl_down_sync(FULLM, iters, o);
     if (lane == 0 && iters && a.total) atomicAdd(a.total, iters);
+    // when launched after a kernel that is still running (programmatic dependent
+    // launch), end only after it has completed, so that the stream's later work
+    // sees both; without such a predecessor this returns at once.  The
+    // predecessor never waits on this kernel, so the wait always ends.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
-template <class N, int K> static cudaError_t launch_batch_k(const BatchArgs &a, int threads, int sms, cudaStream_t s)
+// blocks_per_sm > 0 caps the persistent grid at that many blocks per SM (the
+// share of each SM a co-resident tier leaves this kernel); 0 = as many as fit.
+template <class N, int K>
+static cudaError_t launch_batch_k(const BatchArgs &a, int threads, int sms, int blocks_per_sm, bool after_started,
+                                  cudaStream_t s)
 {
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch<N, K>, threads, 0) != cudaSuccess || occ < 1)
         occ = 1;
+    if (blocks_per_sm > 0 && blocks_per_sm < occ) occ = blocks_per_sm;
     const unsigned long long per_warp = 32ull * a.chunk;
     unsigned long long warps = ((unsigned long long)a.n_jobs + per_warp - 1ull) / per_warp;
     unsigned long long per_block = (unsigned long long)threads / 32ull;
@@ -293,16 +306,77 @@ template <class N, int K> static cudaError_t launch_batch_k(const BatchArgs &a, 
     unsigned long long cap = (unsigned long long)occ * (unsigned long long)sms;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    k_batch<N, K><<<(unsigned)blocks, threads, 0, s>>>(a);
-    return cudaGetLastError();
+    cudaLaunchConfig_t lc{};
+    lc.gridDim = dim3((unsigned)blocks);
+    lc.blockDim = dim3((unsigned)threads);
+    lc.stream = s;
+    // after_started: start as soon as every block of the previous kernel in the
+    // stream has started (programmatic dependent launch), not when it ends
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = after_started ? 1 : 0;
+    lc.attrs = attr;
+    lc.numAttrs = after_started ? 1 : 0;
+    return cudaLaunchKernelEx(&lc, k_batch<N, K>, a);
 }
 
-template <class N> static cudaError_t launch_batch(const BatchArgs &a, int threads, int k, int sms, cudaStream_t s)
+template <class N>
+static cudaError_t launch_batch(const BatchArgs &a, int threads, int k, int sms, int blocks_per_sm, bool after_started,
+                                cudaStream_t s)
 {
-    if (k == 8) return launch_batch_k<N, 8>(a, threads, sms, s);
-    if (k == 32) return launch_batch_k<N, 32>(a, threads, sms, s);
-    return launch_batch_k<N, 16>(a, threads, sms, s);
+    if (k == 8) return launch_batch_k<N, 8>(a, threads, sms, blocks_per_sm, after_started, s);
+    if (k == 32) return launch_batch_k<N, 32>(a, threads, sms, blocks_per_sm, after_started, s);
+    return launch_batch_k<N, 16>(a, threads, sms, blocks_per_sm, after_started, s);
 }
+
+// Every tier kernel asks for the same shared-memory carveout (all of it): blocks
+// of two kernels can share an SM only when the SM's L1/shared split suits
+// both, and a split picked per kernel would keep them apart.
+template <class N, int K> static void set_carveout()
+{
+    cudaFuncSetAttribute(k_batch<N, K>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         (int)cudaSharedmemCarveoutMaxShared);
+}
+static void prepare_batch_kernels()
+{
+    static const bool done = [] {
+        set_carveout<float, 8>(), set_carveout<float, 16>(), set_carveout<float, 32>();
+        set_carveout<FF, 8>(), set_carveout<FF, 16>(), set_carveout<FF, 32>();
+        set_carveout<double, 8>(), set_carveout<double, 16>(), set_carveout<double, 32>();
+        return true;
+    }();
+    (void)done;
+}
+
+// Per-SM footprint of one block of a tier kernel.
+struct Footprint {
+    int regs = 0, smem = 0, warps = 0, alone = 1;  // alone: blocks per SM with the SM to itself
+};
+template <class N, int K> static Footprint footprint_k(int threads)
+{
+    Footprint f;
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, k_batch<N, K>) != cudaSuccess) return f;
+    f.warps = threads / 32;
+    f.regs = ((fa.numRegs * 32 + 255) / 256) * 256 * f.warps;  // registers are allocated per warp, 256 at a time
+    f.smem = (int)fa.sharedSizeBytes + 1024;                     // plus the per-block reservation
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f.alone, k_batch<N, K>, threads, 0) != cudaSuccess ||
+        f.alone < 1)
+        f.alone = 1;
+    return f;
+}
+template <class N> static Footprint footprint(int threads, int k)
+{
+    if (k == 8) return footprint_k<N, 8>(threads);
+    if (k == 32) return footprint_k<N, 32>(threads);
+    return footprint_k<N, 16>(threads);
+}
+
+// Binary64 tier warps per SM when it shares the SMs with a binary32-pipe tier
+// (chaos_batch_config.fp64_warps_per_sm, default 8): the binary64 pipe is
+// saturated by a few warps (a warp-wide DFMA occupies it for ~19 cycles), so
+// the binary64 kernel takes that many warps per SM and the float-float /
+// binary32 kernels the rest, and the two pipes work at once.
 
 }  // namespace chaos
 
@@ -331,6 +405,7 @@ struct chaos_batch {
     const uint32_t *palette = nullptr;
     uint32_t palette_len = 0, interior = 0;
     int threads[kTiers] = {256, 256, 256}, k[kTiers] = {16, 16, 16}, chunk[kTiers] = {1, 1, 1};
+    int fp64_warps = 8;  // binary64 warps per SM when it shares the SMs
     int sms = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -384,6 +459,41 @@ static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s
     cudaStream_t st[kTiers] = {s0, s1, s2};
     // binary64 first: its kernels are the longest, the cheaper tiers fill in behind
     const int order[kTiers] = {2, 1, 0};
+    // co-residency: with a binary64 tier and a binary32-pipe tier present, the
+    // binary64 grid is capped at fp64_warps warps per SM and launched first; the
+    // binary32-pipe kernels follow in the same stream as programmatic dependent
+    // launches, so they start once every binary64 block is resident and fill
+    // the rest of each SM.  Their grids keep their full size: blocks that do
+    // not fit beside the binary64 ones wait and take their place when the
+    // binary64 work runs out.
+    int per_sm[kTiers] = {0, 0, 0};
+    bool shared = false;
+    if (b->n_jobs[2] && (b->n_jobs[0] || b->n_jobs[1])) {
+        Footprint f64 = footprint<double>(b->threads[2], b->k[2]);
+        int b64 = std::max(1, std::min(f64.alone, b->fp64_warps / std::max(1, f64.warps)));
+        int dev = 0, smem_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        const int regs_left = 65536 - b64 * f64.regs, smem_left = smem_sm - b64 * f64.smem;
+        const int warps_left = 64 - b64 * f64.warps, blocks_left = 32 - b64;
+        bool fits = true;
+        for (int t = 0; t < 2; t++) {
+            if (!b->n_jobs[t]) continue;
+            Footprint f = t == 0 ? footprint<float>(b->threads[t], b->k[t]) : footprint<FF>(b->threads[t], b->k[t]);
+            int n = f.alone;
+            if (f.regs > 0) n = std::min(n, regs_left / f.regs);
+            if (f.smem > 0) n = std::min(n, smem_left / f.smem);
+            if (f.warps > 0) n = std::min(n, warps_left / f.warps);
+            n = std::min(n, blocks_left);
+            if (n < 1) fits = false;
+            per_sm[t] = n;
+        }
+        per_sm[0] = per_sm[1] = 0;
+        if (fits) {
+            per_sm[2] = b64;
+            shared = true;
+        }
+    }
     for (int oi = 0; oi < kTiers && e == cudaSuccess; oi++) {
         int t = order[oi];
         if (!b->n_jobs[t]) continue;
@@ -397,10 +507,11 @@ static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s
         a.palette = b->palette;
         a.palette_len = b->palette_len;
         a.interior_rgba = b->interior;
-        cudaStream_t s = st[oi];
-        if (t == 0) e = launch_batch<float>(a, b->threads[t], b->k[t], b->sms, s);
-        if (t == 1) e = launch_batch<FF>(a, b->threads[t], b->k[t], b->sms, s);
-        if (t == 2) e = launch_batch<double>(a, b->threads[t], b->k[t], b->sms, s);
+        cudaStream_t s = shared ? s0 : st[oi];
+        const bool after = shared && t != 2;
+        if (t == 0) e = launch_batch<float>(a, b->threads[t], b->k[t], b->sms, per_sm[t], after, s);
+        if (t == 1) e = launch_batch<FF>(a, b->threads[t], b->k[t], b->sms, per_sm[t], after, s);
+        if (t == 2) e = launch_batch<double>(a, b->threads[t], b->k[t], b->sms, per_sm[t], after, s);
     }
     if (e == cudaSuccess) e = cudaEventRecord(j1, s1);
     if (e == cudaSuccess) e = cudaEventRecord(j2, s2);
@@ -489,6 +600,11 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
                                 "tier %d: threads 32..512 (multiple of 32), block 8/16/32, chunk 1..64", t);
             }
         }
+        if (cfg->fp64_warps_per_sm) b->fp64_warps = (int)cfg->fp64_warps_per_sm;
+        if (b->fp64_warps < 1 || b->fp64_warps > 32) {
+            batch_free(b);
+            return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "fp64_warps_per_sm must be 1..32");
+        }
     }
     size_t n_perturb = 0;
     for (uint32_t k = 0; k < n; k++) n_perturb += tiers[k] == CHAOS_TIER_PERTURB_F32 || tiers[k] == CHAOS_TIER_PERTURB_F64;
@@ -532,6 +648,7 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
         if (e == cudaSuccess)
             e = cudaMemcpy(b->d_vps[t], per[t].data(), per[t].size() * sizeof(BatchViewport), cudaMemcpyHostToDevice);
     }
+    prepare_batch_kernels();
     // capture the fork-join launch into a graph
     cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr, s3 = nullptr;
     cudaEvent_t fork = nullptr, j1 = nullptr, j2 = nullptr, j3 = nullptr;
@@ -608,8 +725,10 @@ int chaos_batch_destroy(chaos_batch *b)
 //
 // Per tier slot present in the viewport list, time every launch shape of the
 // search space on a sample of that tier's viewports (each cut to its central
-// window of at most 96 x 96 pixels, same pixel size, samples and iteration
-// limit) and keep the fastest.  Results are cached in a text file, one line
+// window of 1/8 of its width and height, at least 32 pixels, same pixel size,
+// samples and iteration limit) and keep the fastest; then, when binary64
+// shares the batch with a binary32-pipe tier, tune the shared launch on the
+// joint sample.  Results are cached in a text file, one line
 // per key: "<key> <threads> <escape block> <chunk> <ms>", the key being the
 // device name, its SM count, the tier slot and a hash of that tier's viewport
 // parameters.
@@ -644,14 +763,10 @@ std::vector<std::pair<std::string, TuneEntry>> read_tune_cache(const char *path)
     return out;
 }
 
-// Launch time of `vps` (one tier, forced) under one shape: the faster of two
-// launches after a warm-up.  Negative on failure.
-double time_shape(const std::vector<chaos_viewport> &vps, int slot, int threads, int k, int chunk, cudaStream_t s)
+// Launch time of a batch of `vps` under `cfg`: the faster of two launches
+// after a warm-up.  Negative on failure.
+double time_config(const std::vector<chaos_viewport> &vps, const chaos_batch_config &cfg, cudaStream_t s)
 {
-    chaos_batch_config cfg{};
-    cfg.block_threads[slot] = (uint32_t)threads;
-    cfg.escape_block[slot] = (uint32_t)k;
-    cfg.chunk[slot] = (uint32_t)chunk;
     chaos_batch *b = nullptr;
     if (chaos_batch_create(vps.data(), (uint32_t)vps.size(), nullptr, 0, 0, &cfg, &b) != CHAOS_OK) return -1.0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -673,6 +788,16 @@ double time_shape(const std::vector<chaos_viewport> &vps, int slot, int threads,
     if (e1) cudaEventDestroy(e1);
     chaos_batch_destroy(b);
     return best;
+}
+
+// One tier's viewports (forced) under one shape.
+double time_shape(const std::vector<chaos_viewport> &vps, int slot, int threads, int k, int chunk, cudaStream_t s)
+{
+    chaos_batch_config cfg{};
+    cfg.block_threads[slot] = (uint32_t)threads;
+    cfg.escape_block[slot] = (uint32_t)k;
+    cfg.chunk[slot] = (uint32_t)chunk;
+    return time_config(vps, cfg, s);
 }
 
 }  // namespace
@@ -704,8 +829,10 @@ int chaos_batch_autotune(const chaos_viewport *vps, uint32_t n, const char *cach
         const int t = tier_slot(tier);
         chaos_viewport c = v;
         c.tier = tier;
-        c.width = std::min<uint32_t>(v.width, 96);
-        c.height = std::min<uint32_t>(v.height, 96);
+        // the central window of 1/8 of the width and height (at least 32 pixels), so
+        // that the sample keeps the viewports' proportions of work
+        c.width = std::min<uint32_t>(v.width, std::max<uint32_t>(32, v.width / 8));
+        c.height = std::min<uint32_t>(v.height, std::max<uint32_t>(32, v.height / 8));
         c.counts = nullptr;
         c.smooth = nullptr;
         c.rgba = nullptr;
@@ -723,12 +850,20 @@ int chaos_batch_autotune(const chaos_viewport *vps, uint32_t n, const char *cach
     cudaStream_t s = nullptr;
     if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
         return api_fail(CHAOS_ERR_CUDA, "stream create");
-    // the counts go to one scratch buffer, viewport after viewport
+    // the counts go to one scratch buffer, tier after tier, viewport after viewport
     uint32_t *scratch = nullptr;
-    size_t most = std::max(pixels[0], std::max(pixels[1], pixels[2]));
-    if (most && cudaMalloc(&scratch, most * sizeof(uint32_t)) != cudaSuccess) {
+    size_t all = pixels[0] + pixels[1] + pixels[2];
+    if (all && cudaMalloc(&scratch, all * sizeof(uint32_t)) != cudaSuccess) {
         cudaStreamDestroy(s);
         return api_fail(CHAOS_ERR_OUT_OF_MEMORY, "autotune scratch");
+    }
+    {
+        size_t off = 0;
+        for (int t = 0; t < kTiers; t++)
+            for (chaos_viewport &c : sample[t]) {
+                c.counts = scratch + off;
+                off += (size_t)c.width * c.height * c.samples_per_pixel;
+            }
     }
     static const int kThreads[] = {128, 256, 512}, kBlocks[] = {8, 16, 32}, kChunks[] = {1, 2, 4};
     int rc = CHAOS_OK;
@@ -746,11 +881,6 @@ int chaos_batch_autotune(const chaos_viewport *vps, uint32_t n, const char *cach
             }
         if (hit) continue;
         all_cached = false;
-        size_t off = 0;
-        for (chaos_viewport &c : sample[t]) {
-            c.counts = scratch + off;
-            off += (size_t)c.width * c.height * c.samples_per_pixel;
-        }
         TuneEntry best{0, 0, 0, -1.0};
         for (int th : kThreads)
             for (int kb : kBlocks)
@@ -768,6 +898,92 @@ int chaos_batch_autotune(const chaos_viewport *vps, uint32_t n, const char *cach
         char line[640];
         std::snprintf(line, sizeof(line), "%s %d %d %d %.6f\n", key, best.threads, best.k, best.chunk, best.ms);
         new_lines.push_back(line);
+    }
+    // the shared launch: binary64 next to a binary32-pipe tier.  Cache line
+    // "<key> <binary32-pipe threads> <binary64 threads> <binary64 warps per SM
+    // + 65536 x binary64 escape block> <ms>".
+    if (rc == CHAOS_OK && !sample[2].empty() && (!sample[0].empty() || !sample[1].empty())) {
+        char key[512];
+        std::snprintf(key, sizeof(key), "%s|sm%d|shared|%016llx", devname.c_str(), sms,
+                      (unsigned long long)(sig[0] ^ (sig[1] * 31ull) ^ (sig[2] * 1009ull)));
+        bool hit = false;
+        for (auto &kv : cache)
+            if (kv.first == key) {
+                for (int t = 0; t < 2; t++)
+                    if (!sample[t].empty()) config->block_threads[t] = (uint32_t)kv.second.threads;
+                config->block_threads[2] = (uint32_t)kv.second.k;
+                config->fp64_warps_per_sm = (uint32_t)(kv.second.chunk & 0xffff);
+                if (kv.second.chunk >> 16) config->escape_block[2] = (uint32_t)(kv.second.chunk >> 16);
+                hit = true;
+            }
+        if (!hit) {
+            all_cached = false;
+            // a larger sample than the per-tier one (1/4 of each side, at least 64
+            // pixels): the shared launch's balance depends on the tail of each tier
+            std::vector<chaos_viewport> joint;
+            size_t jpix = 0;
+            for (uint32_t k = 0; k < n; k++) {
+                const chaos_viewport &v = vps[k];
+                uint32_t tier = v.tier == CHAOS_TIER_AUTO ? chaos_batch_auto_tier(v.center_x, v.center_y, v.pixel_size)
+                                : v.tier == CHAOS_TIER_AUTO_DEEP
+                                    ? auto_deep_tier(v.center_x, v.center_y, v.pixel_size)
+                                    : v.tier;
+                if (tier != CHAOS_TIER_F32 && tier != CHAOS_TIER_FLOATFLOAT && tier != CHAOS_TIER_F64) continue;
+                chaos_viewport c = v;
+                c.tier = tier;
+                c.width = std::min<uint32_t>(v.width, std::max<uint32_t>(64, v.width / 4));
+                c.height = std::min<uint32_t>(v.height, std::max<uint32_t>(64, v.height / 4));
+                c.counts = nullptr;
+                c.smooth = nullptr;
+                c.rgba = nullptr;
+                jpix += (size_t)c.width * c.height * c.samples_per_pixel;
+                joint.push_back(c);
+            }
+            uint32_t *jscratch = nullptr;
+            if (cudaMalloc(&jscratch, jpix * sizeof(uint32_t)) != cudaSuccess) joint.clear();
+            size_t joff = 0;
+            for (chaos_viewport &c : joint) {
+                c.counts = jscratch + joff;
+                joff += (size_t)c.width * c.height * c.samples_per_pixel;
+            }
+            // 512-thread blocks of the binary32-pipe kernels are left out: beside the
+            // binary64 blocks only one fits (16 warps, against 24 for 256-thread
+            // blocks), and on the full C4 batch they lost every pairing (586 ms vs
+            // 544 ms); 32-step binary64 blocks likewise (596 vs 544).
+            static const int kSideThreads[] = {128, 256}, kF64Threads[] = {128, 256}, kF64Block[] = {16},
+                             kF64Warps[] = {8, 12, 16};
+            TuneEntry best{0, 0, 0, -1.0};
+            int best_k64 = config->escape_block[2];
+            for (int ts : kSideThreads)
+                for (int t64 : kF64Threads)
+                    for (int k64 : kF64Block)
+                        for (int w64 : kF64Warps) {
+                            chaos_batch_config c = *config;
+                            for (int t = 0; t < 2; t++)
+                                if (!sample[t].empty()) c.block_threads[t] = (uint32_t)ts;
+                            c.block_threads[2] = (uint32_t)t64;
+                            c.escape_block[2] = (uint32_t)k64;
+                            c.fp64_warps_per_sm = (uint32_t)w64;
+                            double ms = joint.empty() ? -1.0 : time_config(joint, c, s);
+                            if (ms >= 0 && (best.ms < 0 || ms < best.ms)) {
+                                best = {ts, t64, w64, ms};
+                                best_k64 = k64;
+                            }
+                        }
+            if (jscratch) cudaFree(jscratch);
+            if (best.ms >= 0) {
+                for (int t = 0; t < 2; t++)
+                    if (!sample[t].empty()) config->block_threads[t] = (uint32_t)best.threads;
+                config->block_threads[2] = (uint32_t)best.k;
+                config->escape_block[2] = (uint32_t)best_k64;
+                config->fp64_warps_per_sm = (uint32_t)best.chunk;
+                char line[640];
+                // the binary64 escape block rides in the warps field's upper half
+                std::snprintf(line, sizeof(line), "%s %d %d %d %.6f\n", key, best.threads, best.k,
+                              best.chunk | (best_k64 << 16), best.ms);
+                new_lines.push_back(line);
+            }
+        }
     }
     if (scratch) cudaFree(scratch);
     cudaStreamDestroy(s);

@@ -296,11 +296,16 @@ typedef struct chaos_viewport {
 } chaos_viewport;
 
 /* Launch shape per tier (index 0 binary32, 1 float-float, 2 binary64); zero
- * keeps the default (256 threads, 16-step escape blocks, chunk 1). */
+ * keeps the default (256 threads, 16-step escape blocks, chunk 1).  When a
+ * batch holds binary64 viewports and binary32 or float-float ones, their
+ * kernels share every SM: the binary64 kernel gets fp64_warps_per_sm warps
+ * per SM (default 8; its pipe is saturated by few warps) and the others the
+ * rest, so the binary64 and binary32 pipes work at the same time. */
 typedef struct chaos_batch_config {
     uint32_t block_threads[3]; /* 32..512, multiple of 32 */
     uint32_t escape_block[3];  /* 8, 16 or 32 */
     uint32_t chunk[3];         /* 1..64 consecutive pixels a lane claims per work-counter update */
+    uint32_t fp64_warps_per_sm; /* 1..32, 0 = 8 */
 } chaos_batch_config;
 
 typedef struct chaos_batch chaos_batch;
@@ -319,8 +324,12 @@ int chaos_batch_create(const chaos_viewport *viewports, uint32_t n, const uint32
  * float-float, binary64; perturbation viewports are not tuned), time every
  * launch shape of threads {128, 256, 512} x escape block {8, 16, 32} x chunk
  * {1, 2, 4} on a sample of that tier's viewports (each cut to its central
- * 96 x 96 window, same pixel size, samples and iteration limit) and write the
- * fastest into *config (slots without viewports stay 0 = default).  With a
+ * window of 1/8 of its width and height, at least 32 pixels, same pixel size,
+ * samples and iteration limit) and write the
+ * fastest into *config (slots without viewports stay 0 = default).  When
+ * binary64 shares the batch with another tier, the shared launch is then
+ * tuned on a joint sample (1/4 of each side): threads {128, 256} of each
+ * tier, 16-step binary64 blocks and fp64_warps_per_sm {8, 12, 16}.  With a
  * cache_path, shapes found before for the same device, SM count, slot and
  * viewport parameters are read from that text file and new ones appended;
  * *from_cache (optional) is 1 when nothing had to be timed.  Synchronous;
