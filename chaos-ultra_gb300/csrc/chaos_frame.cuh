@@ -77,34 +77,6 @@ __device__ __forceinline__ FF ff_fast_two_sum(float a, float b)  // |a| >= |b|
     return FF{s, e};
 }
 
-__device__ __forceinline__ FF ff_add(FF a, FF b)
-{
-    float s = __fadd_rn(a.hi, b.hi);
-    float bb = __fsub_rn(s, a.hi);
-    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
-    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
-    return ff_fast_two_sum(s, e);
-}
-
-__device__ __forceinline__ FF ff_neg(FF a) { return FF{-a.hi, -a.lo}; }
-
-__device__ __forceinline__ FF ff_mul(FF a, FF b)
-{
-    float p = __fmul_rn(a.hi, b.hi);
-    float e = __fmaf_rn(a.hi, b.hi, -p);
-    e = __fmaf_rn(a.hi, b.lo, e);
-    e = __fmaf_rn(a.lo, b.hi, e);
-    return ff_fast_two_sum(p, e);
-}
-
-__device__ __forceinline__ FF ff_sqr(FF a)
-{
-    float p = __fmul_rn(a.hi, a.hi);
-    float e = __fmaf_rn(a.hi, a.hi, -p);
-    e = __fmaf_rn(__fadd_rn(a.hi, a.hi), a.lo, e);
-    return ff_fast_two_sum(p, e);
-}
-
 __host__ __device__ __forceinline__ FF ff_from_double(double d)
 {
     float hi = (float)d;
@@ -112,13 +84,48 @@ __host__ __device__ __forceinline__ FF ff_from_double(double d)
     return FF{hi, lo};
 }
 
-// One z <- z^2 + c step in float-float (56 binary32 operations).
+// Knuth's two-sum: s + err == a + b exactly.
+__device__ __forceinline__ float ff_two_sum(float a, float b, float &err)
+{
+    float s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+}
+
+// One z <- z^2 + c step in float-float, 43 binary32 operations.  The three
+// products stay unnormalised (leading product + error term by fused
+// multiply-add), the leading terms meet in two-sums, all error terms are
+// summed in one fixed order, and each coordinate is normalised once at the
+// end:
+//   x' = fast_two_sum(t, ((ex - ey) + e1) + e2 + cx.lo),
+//        s = two_sum(px, -py; e1), t = two_sum(s, cx.hi; e2)
+//   y' = fast_two_sum(u, fma(2, exy, e3) + cy.lo),  u = two_sum(2 pxy, cy.hi; e3)
 __device__ __forceinline__ void ff_step(FF &x, FF &y, FF cx, FF cy)
 {
-    FF xx = ff_sqr(x), yy = ff_sqr(y), xy = ff_mul(x, y);
-    FF xn = ff_add(ff_add(xx, ff_neg(yy)), cx);
-    FF xy2{__fadd_rn(xy.hi, xy.hi), __fadd_rn(xy.lo, xy.lo)};
-    y = ff_add(xy2, cy);
+    const float px = __fmul_rn(x.hi, x.hi);
+    float ex = __fmaf_rn(x.hi, x.hi, -px);
+    ex = __fmaf_rn(__fadd_rn(x.hi, x.hi), x.lo, ex);
+    const float py = __fmul_rn(y.hi, y.hi);
+    float ey = __fmaf_rn(y.hi, y.hi, -py);
+    ey = __fmaf_rn(__fadd_rn(y.hi, y.hi), y.lo, ey);
+    const float pxy = __fmul_rn(x.hi, y.hi);
+    float exy = __fmaf_rn(x.hi, y.hi, -pxy);
+    exy = __fmaf_rn(x.hi, y.lo, exy);
+    exy = __fmaf_rn(x.lo, y.hi, exy);
+
+    float e1, e2, e3;
+    const float s = ff_two_sum(px, -py, e1);
+    const float t = ff_two_sum(s, cx.hi, e2);
+    float e = __fsub_rn(ex, ey);
+    e = __fadd_rn(e, e1);
+    e = __fadd_rn(e, e2);
+    e = __fadd_rn(e, cx.lo);
+    const FF xn = ff_fast_two_sum(t, e);
+
+    const float u = ff_two_sum(__fadd_rn(pxy, pxy), cy.hi, e3);
+    const float f = __fadd_rn(__fmaf_rn(2.f, exy, e3), cy.lo);
+    y = ff_fast_two_sum(u, f);
     x = xn;
 }
 

@@ -1079,34 +1079,49 @@ static ff_t ff_fast_two_sum(float a, float b)
     ff_t r = {s, b - (s - a)};
     return r;
 }
-static ff_t ff_add(ff_t a, ff_t b)
-{
-    float s = a.hi + b.hi;
-    float bb = s - a.hi;
-    float e = (a.hi - (s - bb)) + (b.hi - bb);
-    e = e + (a.lo + b.lo);
-    return ff_fast_two_sum(s, e);
-}
-static ff_t ff_mul(ff_t a, ff_t b)
-{
-    float p = a.hi * b.hi;
-    float e = fmaf(a.hi, b.hi, -p);
-    e = fmaf(a.hi, b.lo, e);
-    e = fmaf(a.lo, b.hi, e);
-    return ff_fast_two_sum(p, e);
-}
-static ff_t ff_sqr(ff_t a)
-{
-    float p = a.hi * a.hi;
-    float e = fmaf(a.hi, a.hi, -p);
-    e = fmaf(a.hi + a.hi, a.lo, e);
-    return ff_fast_two_sum(p, e);
-}
 static ff_t ff_from_double(double d)
 {
     float hi = (float)d;
     ff_t r = {hi, (float)(d - (double)hi)};
     return r;
+}
+
+/* Knuth's two-sum. */
+static float ff_two_sum(float a, float b, float *err)
+{
+    float s = a + b;
+    float bb = s - a;
+    *err = (a - (s - bb)) + (b - bb);
+    return s;
+}
+
+/* The library's float-float step (chaos_frame.cuh ff_step): unnormalised
+ * products, two-sums of the leading terms, error terms summed in a fixed
+ * order, one normalisation per coordinate. */
+static void ff_step(ff_t *x, ff_t *y, ff_t cx, ff_t cy)
+{
+    float px = x->hi * x->hi;
+    float ex = fmaf(x->hi, x->hi, -px);
+    ex = fmaf(x->hi + x->hi, x->lo, ex);
+    float py = y->hi * y->hi;
+    float ey = fmaf(y->hi, y->hi, -py);
+    ey = fmaf(y->hi + y->hi, y->lo, ey);
+    float pxy = x->hi * y->hi;
+    float exy = fmaf(x->hi, y->hi, -pxy);
+    exy = fmaf(x->hi, y->lo, exy);
+    exy = fmaf(x->lo, y->hi, exy);
+    float e1, e2, e3;
+    float s = ff_two_sum(px, -py, &e1);
+    float t = ff_two_sum(s, cx.hi, &e2);
+    float e = ex - ey;
+    e = e + e1;
+    e = e + e2;
+    e = e + cx.lo;
+    ff_t xn = ff_fast_two_sum(t, e);
+    float u = ff_two_sum(pxy + pxy, cy.hi, &e3);
+    float f = fmaf(2.f, exy, e3) + cy.lo;
+    *y = ff_fast_two_sum(u, f);
+    *x = xn;
 }
 
 static uint32_t esc_ff(uint32_t max_iter, ff_t cx, ff_t cy, float *r2_exit)
@@ -1117,12 +1132,7 @@ static uint32_t esc_ff(uint32_t max_iter, ff_t cx, ff_t cy, float *r2_exit)
     for (;;) {
         r2 = fmaf(x.hi, x.hi, y.hi * y.hi);
         if (!(i < max_iter && r2 < 4.0f)) break;
-        ff_t xx = ff_sqr(x), yy = ff_sqr(y), xy = ff_mul(x, y);
-        ff_t nyy = {-yy.hi, -yy.lo};
-        ff_t xn = ff_add(ff_add(xx, nyy), cx);
-        ff_t xy2 = {xy.hi + xy.hi, xy.lo + xy.lo};
-        y = ff_add(xy2, cy);
-        x = xn;
+        ff_step(&x, &y, cx, cy);
         ++i;
     }
     *r2_exit = r2;
