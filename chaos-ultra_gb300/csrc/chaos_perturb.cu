@@ -27,7 +27,10 @@
 // alone (escape only where binary32 |Z|^2 >= 4, the glitch test only where it
 // is below 2^-100, the orbit's end), so the orbit carries, per index, the next
 // index where one of them can fire, and steps up to it run as a block of
-// 4 FFMA each on a stored 2Z.
+// 4 FFMA each on a stored 2Z.  Binary64 differences get the same treatment
+// while |d| and |dc| stay below 2^-120 and both components of Z above 2^-20:
+// then 2Z + d rounds to 2Z and Z + d' to Z, so d' = 2Z d + dc (4 DFMA) is the
+// full step bit for bit, and its tests depend on the orbit index alone.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -60,6 +63,8 @@ template <class D> struct PerturbArgs {
     const double2 *orbit64;                // the same orbit in binary64 (rescaled glitch test)
     const float2 *orbit2;                  // 2 Z_m in binary32 (rescaled linear steps)
     const uint32_t *next_event;            // first index >= m where a rescaled step's test can fire
+    const double2 *orbit2_64;              // 2 Z_m in binary64 (binary64 linear steps)
+    const uint32_t *next_event64;          // first index >= m where a binary64 linear step may not be exact
     uint32_t orbit_last;
     uint32_t *counts;
     float *smooth;
@@ -299,6 +304,42 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                     }
                     continue;
                 }
+                if constexpr (!S && sizeof(D) == 8) {
+                    // binary64 differences far below the orbit (|d|, |dc| < 2^-120 while
+                    // both components of Z stay above 2^-20): 2Z + d rounds to 2Z and
+                    // Z + d' to Z, so the step is d' = 2Z d + dc bit for bit and its tests
+                    // depend on the orbit index alone; run up to 16 such steps, stopping
+                    // before the next index where that fails (next_event64)
+                    const uint32_t big = max(max((uint32_t)__double2hiint(dx) & 0x7ff00000u,
+                                                 (uint32_t)__double2hiint(dy) & 0x7ff00000u),
+                                             max((uint32_t)__double2hiint(dcx) & 0x7ff00000u,
+                                                 (uint32_t)__double2hiint(dcy) & 0x7ff00000u));
+                    if (big < (903u << 20)) {
+                        const uint32_t ev = a.next_event64[m];
+                        const uint32_t n = min(min(16u, ev > m ? ev - m - 1u : 0u), a.max_iter - 1u - i);
+                        if (n > 0) {
+                            double wx = dx, wy = dy;
+#pragma unroll
+                            for (uint32_t j = 0; j < 16; j++) {
+                                if (j < n) {
+                                    const double2 Z2 = a.orbit2_64[m + j];
+                                    const double nx = __fma_rn(Z2.x, wx, __fma_rn(-Z2.y, wy, (double)dcx));
+                                    const double ny = __fma_rn(Z2.x, wy, __fma_rn(Z2.y, wx, (double)dcy));
+                                    wx = nx;
+                                    wy = ny;
+                                }
+                            }
+                            m += n;
+                            i += n;
+                            const typename Vec2T<D>::type Z = a.orbit[m];
+                            Zx = Z.x;
+                            Zy = Z.y;
+                            dx = wx;
+                            dy = wy;
+                            continue;
+                        }
+                    }
+                }
                 // d' = (2Z + d) d + dc
                 D wx = O::fma(D(2), Zx, dx), wy = O::fma(D(2), Zy, dy);
                 D ndx = O::fma(wx, dx, O::fma(-wy, dy, dcx));
@@ -416,8 +457,10 @@ struct chaos_orbit {
     double center_x = 0, center_y = 0;  // rounded centre, for reporting
     float2 *z32 = nullptr;
     double2 *z64 = nullptr;
-    float2 *z2 = nullptr;            // 2 Z in binary32
-    uint32_t *next_event = nullptr;  // see the rescaled linear steps of k_perturb
+    float2 *z2 = nullptr;              // 2 Z in binary32
+    uint32_t *next_event = nullptr;    // see the rescaled linear steps of k_perturb
+    double2 *z2_64 = nullptr;          // 2 Z in binary64
+    uint32_t *next_event64 = nullptr;  // see the binary64 linear steps of k_perturb
 };
 
 static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t max_iterations, chaos_orbit **out);
@@ -489,6 +532,23 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
             next_event[j] = next;
         }
     }
+    // next_event64[m]: first index j >= m where a binary64 linear step from or to
+    // j may differ from the full step: the orbit's end, |Z|^2 >= 4 (as the
+    // kernel's escape test computes it), or a component of Z below 2^-20
+    std::vector<double2> z2_64(z64.size());
+    std::vector<uint32_t> next_event64(z64.size());
+    {
+        const size_t last = z64.size() - 1;
+        uint32_t next = (uint32_t)last;
+        for (size_t j = last + 1; j-- > 0;) {
+            const double zx = z64[j].x, zy = z64[j].y;
+            z2_64[j] = make_double2(2.0 * zx, 2.0 * zy);
+            const double r2 = std::fma(zx, zx, zy * zy);
+            if (j == last || !(r2 < 4.0) || !(std::fabs(zx) >= 0x1p-20) || !(std::fabs(zy) >= 0x1p-20))
+                next = (uint32_t)j;
+            next_event64[j] = next;
+        }
+    }
 
     chaos_orbit *o = new (std::nothrow) chaos_orbit();
     if (!o) return api_fail(CHAOS_ERR_OUT_OF_MEMORY, "out of host memory");
@@ -508,11 +568,20 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
     if (e == cudaSuccess) e = cudaMalloc(&o->next_event, next_event.size() * sizeof(uint32_t));
     if (e == cudaSuccess)
         e = cudaMemcpy(o->next_event, next_event.data(), next_event.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&o->z2_64, z2_64.size() * sizeof(double2));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(o->z2_64, z2_64.data(), z2_64.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&o->next_event64, next_event64.size() * sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(o->next_event64, next_event64.data(), next_event64.size() * sizeof(uint32_t),
+                       cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         if (o->z64) cudaFree(o->z64);
         if (o->z32) cudaFree(o->z32);
         if (o->z2) cudaFree(o->z2);
         if (o->next_event) cudaFree(o->next_event);
+        if (o->z2_64) cudaFree(o->z2_64);
+        if (o->next_event64) cudaFree(o->next_event64);
         delete o;
         return api_fail(CHAOS_ERR_CUDA, "reference orbit upload: %s", cudaGetErrorString(e));
     }
@@ -536,6 +605,8 @@ int chaos_orbit_destroy(chaos_orbit *o)
     if (o->z32) cudaFree(o->z32);
     if (o->z2) cudaFree(o->z2);
     if (o->next_event) cudaFree(o->next_event);
+    if (o->z2_64) cudaFree(o->z2_64);
+    if (o->next_event64) cudaFree(o->next_event64);
     delete o;
     return CHAOS_OK;
 }
@@ -565,6 +636,8 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
     a.orbit64 = orb->z64;
     a.orbit2 = orb->z2;
     a.next_event = orb->next_event;
+    a.orbit2_64 = orb->z2_64;
+    a.next_event64 = orb->next_event64;
     a.counts = o->counts;
     a.smooth = o->smooth;
     a.pixels = reinterpret_cast<PixelInfo *>(o->pixels);
