@@ -210,7 +210,7 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
             for (int k = 0; k < K && !done; k++) {
                 if constexpr (S) if (scaled && e < -126) {
                     // linear steps up to (not onto) the next index whose tests can fire
-                    constexpr uint32_t B = 8;
+                    constexpr uint32_t B = 16;  // |w| <= 2^24 grows at most 4^16-fold: below 2^56
                     const uint32_t ev = a.next_event[m + 1];
                     const uint32_t n = min(min(B, ev - (m + 1)), a.max_iter - 1u - i);
                     if (n > 0) {
