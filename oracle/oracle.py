@@ -338,8 +338,9 @@ class Reference:
 
 
 def c1_grid():
-    """BASELINE workload C1 as a point grid: 1024x1024 pixel centres of the plane
-    [-2, 1] x [-1.5, 1.5], maxIter 1000 -> (w, h, x0, y0, dx, dy, max_iter)."""
+    """The plain binary32 workload (C1) as a point grid: 1024x1024 pixel centres
+    of the plane [-2, 1] x [-1.5, 1.5], maxIter 1000 -> (w, h, x0, y0, dx, dy,
+    max_iter)."""
     w = h = 1024
     dx = 3.0 / 1024
     return w, h, -2.0 + dx / 2, 1.5 - dx / 2, dx, dx, 1000
