@@ -41,7 +41,7 @@ extern "C" {
 #define CHAOS_ERR_STATE 5            /* renderer not initialised / already initialised */
 #define CHAOS_ERR_OUT_OF_MEMORY 6    /* allocation or HBM budget refused */
 #define CHAOS_ERR_TIMEOUT 7          /* a bounded device wait gave up */
-#define CHAOS_ERR_UNSUPPORTED 8      /* valid request this build does not implement */
+#define CHAOS_ERR_UNSUPPORTED 8      /* valid request this library does not implement */
 
 /* Message of the last failing call on this thread ("" if none). */
 const char *chaos_last_error(void);

@@ -1,7 +1,7 @@
 /*
  * chaos_oracle.c -- CPU restatement of the reference's fractal-kernel path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: the parity tests, the
  * smoke check and the CPU-baseline leg of bench.py call it to produce the
  * expected answer.  Nothing in the product (the CUDA library, the drop-in
  * module, the Python host layer) links, loads or calls it.

@@ -4,7 +4,7 @@
 reference's fractal-kernel path (oracle/chaos_oracle.c).  `Reference` wraps
 oracle/_ref/libchaos_ref.so, the reference's own computeFractal/colorize built
 for the host by oracle/build_ref.sh.  Only tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline / reference legs use this module, as the checker.
+bench.py's CPU-baseline / reference legs use this module, as the oracle.
 """
 import ctypes as C
 import os
