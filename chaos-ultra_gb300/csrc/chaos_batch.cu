@@ -283,10 +283,12 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
     for (int o = 16; o > 0; o >>= 1) iters += __shfl_down_sync(FULLM, iters, o);
     if (lane == 0 && iters && a.total) atomicAdd(a.total, iters);
     // when launched after a kernel that is still running (programmatic dependent
-    // launch), end only after it has completed, so that the stream's later work
-    // sees both; without such a predecessor this returns at once.  The
-    // predecessor never waits on this kernel, so the wait always ends.
-    asm volatile("griddepcontrol.wait;" ::: "memory");
+    // launch), the kernel ends only after that one has completed, so that the
+    // stream's later work sees both.  Block 0 alone waits: the other blocks
+    // leave at once and free their SM for what is queued behind them.  Without
+    // such a predecessor this returns at once; the predecessor never waits on
+    // this kernel, so the wait always ends.
+    if (blockIdx.x == 0) asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
 // blocks_per_sm > 0 caps the persistent grid at that many blocks per SM (the
@@ -462,10 +464,9 @@ static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s
     // co-residency: with a binary64 tier and a binary32-pipe tier present, the
     // binary64 grid is capped at fp64_warps warps per SM and launched first; the
     // binary32-pipe kernels follow in the same stream as programmatic dependent
-    // launches, so they start once every binary64 block is resident and fill
-    // the rest of each SM.  Their grids keep their full size: blocks that do
-    // not fit beside the binary64 ones wait and take their place when the
-    // binary64 work runs out.
+    // launches, so they start once every binary64 block is resident, with their
+    // grids capped at what fits beside it.  A binary64 tail grid follows (see
+    // below) to widen the binary64 tier when the others finish first.
     int per_sm[kTiers] = {0, 0, 0};
     bool shared = false;
     if (b->n_jobs[2] && (b->n_jobs[0] || b->n_jobs[1])) {
@@ -488,10 +489,11 @@ static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s
             if (n < 1) fits = false;
             per_sm[t] = n;
         }
-        per_sm[0] = per_sm[1] = 0;
         if (fits) {
             per_sm[2] = b64;
             shared = true;
+        } else {
+            per_sm[0] = per_sm[1] = 0;
         }
     }
     for (int oi = 0; oi < kTiers && e == cudaSuccess; oi++) {
@@ -512,6 +514,23 @@ static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s
         if (t == 0) e = launch_batch<float>(a, b->threads[t], b->k[t], b->sms, per_sm[t], after, s);
         if (t == 1) e = launch_batch<FF>(a, b->threads[t], b->k[t], b->sms, per_sm[t], after, s);
         if (t == 2) e = launch_batch<double>(a, b->threads[t], b->k[t], b->sms, per_sm[t], after, s);
+    }
+    if (shared && e == cudaSuccess) {
+        // the binary64 tail: a second, full-size grid on the same job counter.
+        // It starts once every binary32-pipe block has started, and its blocks
+        // take the room those blocks leave when their tier runs out of work, so
+        // a binary64 tier that outlasts the others widens to whole SMs.
+        BatchArgs a{};
+        a.vps = b->d_vps[2];
+        a.n_vp = b->n_vp[2];
+        a.n_jobs = b->n_jobs[2];
+        a.counter = b->d_counters + 2;
+        a.chunk = (uint32_t)b->chunk[2];
+        a.total = b->d_total;
+        a.palette = b->palette;
+        a.palette_len = b->palette_len;
+        a.interior_rgba = b->interior;
+        e = launch_batch<double>(a, b->threads[2], b->k[2], b->sms, 0, true, s0);
     }
     if (e == cudaSuccess) e = cudaEventRecord(j1, s1);
     if (e == cudaSuccess) e = cudaEventRecord(j2, s2);
