@@ -880,6 +880,71 @@ def run_deep(args):
     orbit.close()
 
 
+def run_compose(args):
+    """The compose kernel (gen.cu:455-475) alone: an 8K pixel_info_t frame
+    (7680x4320 records of 16 B, pitched) through a 1536-entry palette into
+    RGBA8.  Algorithmic traffic 20 B per pixel (16 B read, 4 B written); the
+    palette sits in shared memory.  Bound: HBM."""
+    import numpy as np
+    import torch
+
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import default_palette
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    w, h = 7680, 4320
+    pitch = ((16 * w + 511) // 512) * 512
+    out_pitch = ((4 * w + 511) // 512) * 512
+    rng = np.random.default_rng(9)
+    vals = torch.from_numpy(rng.uniform(0, 5000, size=(h, pitch // 4)).astype(np.float32)).to(dev)
+    vals.view(h, pitch // 16, 4)[:, :, 1] = 4.0  # weight
+    out = torch.zeros((h, out_pitch // 4), dtype=torch.int32, device=dev)
+    pal = default_palette()
+    dpal = torch.from_numpy(np.ascontiguousarray(pal, dtype=np.uint32).view(np.int32)).to(dev)
+    m = cg.Module("mandelbrot")
+    stream = torch.cuda.current_stream()
+    flush = _l2_flush(torch, dev)
+
+    def go():
+        m.compose(vals.data_ptr(), pitch, out.data_ptr(), out_pitch, w, h, dpal.data_ptr(), len(pal), 4.0,
+                  stream=stream)
+
+    for _ in range(args.warmup):
+        go()
+    torch.cuda.synchronize()
+    ms = []
+    clocks = ClockSampler(0)
+    clocks.start()
+    for k in range(args.steps):
+        flush(k)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        go()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    per = statistics.median(ms)
+    algo = 20.0 * w * h
+    peak = None
+    try:
+        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+        src = "MEASURED_PEAKS.json hbm_gbs (torch copy, read + write)"
+    except (OSError, KeyError, ValueError):
+        peak, src = 6800.0, "fallback 6.8 TB/s"
+    gbs = algo / (per / 1e3) / 1e9
+    line = {"metric": "GB/s (compose, algorithmic bytes)", "value": gbs, "unit": "GB/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 in, u8x4 out",
+            "data": "synthetic: seeded values, the default 1536-entry palette",
+            "config": {"workload": f"compose {w}x{h} pixel_info_t -> RGBA8", "l2": "flushed between steps"},
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "traffic": None, "peak_source": src, "bytes_per_pixel": 20},
+            "gpu_launches": args.steps, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def run_serve(args):
     """C5: 16 zoom sessions (720p..2160p), 1.02x zoom per frame toward seeded
     boundary points, Poisson arrivals at 60 Hz per session, HBM-budget admission,
@@ -974,7 +1039,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["c1", "c2", "c2-crop", "c3", "c4", "c4-crop", "c5"], default="c2",
+    ap.add_argument("--workload", choices=["c1", "c2", "c2-crop", "c3", "c4", "c4-crop", "c5", "compose"],
+                    default="c2",
                     help="c2-crop / c4-crop: the central 480x270 pixels of the frame / 256x256 of each viewport "
                          "(for profiler captures)")
     args = ap.parse_args()
@@ -985,6 +1051,8 @@ def main():
         run_reference(args)
     elif args.workload == "c1":
         run_c1(args)
+    elif args.workload == "compose":
+        run_compose(args)
     elif args.workload == "c3":
         run_deep(args)
     elif args.workload in ("c4", "c4-crop"):

@@ -295,22 +295,30 @@ __global__ void __launch_bounds__(256) k_compose(ComposeArgs a)
         pal = s_pal;
     }
     __syncthreads();
-    const uint32_t wq = (a.w + 3u) / 4u;
-    const size_t n = (size_t)wq * a.h;
-    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
-        uint32_t y = (uint32_t)(q / wq), x = 4u * (uint32_t)(q % wq);
-        uint32_t c[4] = {0, 0, 0, 0};
+    // A warp takes a run of 128 pixels of one row; lane l handles pixels
+    // x0 + 32k + l (k = 0..3), so every load instruction reads 32 consecutive
+    // 16-byte records (512 B) and every store writes 32 consecutive words.  The
+    // four records are loaded before any is composed, four loads in flight
+    // (eight measured the same and cost 57 registers instead of 32).
+    constexpr int R = 4;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t runs = (a.w + 32u * R - 1u) / (32u * R);
+    const size_t n = (size_t)runs * a.h;
+    const size_t warps = (size_t)gridDim.x * (blockDim.x / 32u);
+    for (size_t c = (size_t)blockIdx.x * (blockDim.x / 32u) + (threadIdx.x >> 5); c < n; c += warps) {
+        const uint32_t y = (uint32_t)(c / runs), x0 = 32u * R * (uint32_t)(c % runs);
+        PixelInfo p[R];
 #pragma unroll
-        for (int k = 0; k < 4; k++)
-            if (x + k < a.w)
-                c[k] = compose_pixel(load_pixel(pixel_ptr(a.in, a.pitch, x + k, y)), pal, a.palette_len, a.max_ss,
-                                     a.visualize, a.color_mode, a.magnifier);
+        for (int k = 0; k < R; k++) {
+            const uint32_t x = x0 + 32u * k + lane;
+            if (x < a.w) p[k] = load_pixel(pixel_ptr(a.in, a.pitch, x, y));
+        }
         uint32_t *row = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(a.out) + (size_t)y * (size_t)a.out_pitch);
-        if (x + 3u < a.w && (reinterpret_cast<uintptr_t>(row + x) & 15u) == 0) {
-            *reinterpret_cast<uint4 *>(row + x) = make_uint4(c[0], c[1], c[2], c[3]);
-        } else {
-            for (int k = 0; k < 4; k++)
-                if (x + k < a.w) row[x + k] = c[k];
+#pragma unroll
+        for (int k = 0; k < R; k++) {
+            const uint32_t x = x0 + 32u * k + lane;
+            if (x < a.w)
+                row[x] = compose_pixel(p[k], pal, a.palette_len, a.max_ss, a.visualize, a.color_mode, a.magnifier);
         }
     }
 }
@@ -389,8 +397,8 @@ cudaError_t launch_frame(const FrameArgs<R> &a, int arith, int fractal, int sms,
 
 cudaError_t launch_compose(const ComposeArgs &a, cudaStream_t s)
 {
-    unsigned long long quads = (unsigned long long)((a.w + 3u) / 4u) * a.h;
-    unsigned long long blocks = (quads + 255ull) / 256ull;
+    unsigned long long runs = (unsigned long long)((a.w + 127u) / 128u) * a.h;  // one warp each
+    unsigned long long blocks = (runs + 7ull) / 8ull;
     if (blocks > 152ull * 16ull) blocks = 152ull * 16ull;
     if (blocks < 1) blocks = 1;
     k_compose<<<(unsigned)blocks, 256, 0, s>>>(a);
