@@ -945,6 +945,71 @@ def run_compose(args):
     print(json.dumps(line), flush=True)
 
 
+def run_reuse(args):
+    """Sample reuse (fractalRenderAdvanced, gen.cu:307-368) alone: an 8K frame
+    whose previous frame covers the same plane rectangle, so every pixel but
+    the 2-pixel border takes its value and weight from the previous frame by
+    bilinear filtering and computes no new sample.  Algorithmic traffic 32 B
+    per pixel (16 B of the previous frame, 16 B written).  Bound: HBM."""
+    import numpy as np
+    import torch
+
+    import chaos_gb300 as cg
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    w, h = 7680, 4320
+    pitch = ((16 * w + 511) // 512) * 512
+    rng = np.random.default_rng(10)
+    prev = torch.from_numpy(rng.uniform(0, 5000, size=(h, pitch // 4)).astype(np.float32)).to(dev)
+    prev.view(h, pitch // 16, 4)[:, :, 1] = 4.0  # weight
+    prev.view(h, pitch // 16, 4)[:, :, 2] = 0.0  # isReused + padding
+    out = torch.zeros_like(prev)
+    m = cg.Module("mandelbrot")
+    stream = torch.cuda.current_stream()
+    flush = _l2_flush(torch, dev)
+    rect = (-2.0, -1.5, 1.0, 1.5)
+
+    def go():
+        m.render_advanced(out.data_ptr(), pitch, w, h, rect, 100, 4.0, cg.FLAG_SAMPLE_REUSE, rect, prev.data_ptr(),
+                          pitch, (w // 2, h // 2), stream=stream)
+
+    for _ in range(args.warmup):
+        go()
+    torch.cuda.synchronize()
+    ms = []
+    clocks = ClockSampler(0)
+    clocks.start()
+    for k in range(args.steps):
+        flush(k)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        go()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    per = statistics.median(ms)
+    reused = float((out.view(h, pitch // 16, 4)[:, :w, 2].view(torch.int32) & 0xFF).ne(0).float().mean().item())
+    algo = 32.0 * w * h
+    try:
+        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+        src = "MEASURED_PEAKS.json hbm_gbs (torch copy, read + write)"
+    except (OSError, KeyError, ValueError):
+        peak, src = 6800.0, "fallback 6.8 TB/s"
+    gbs = algo / (per / 1e3) / 1e9
+    line = {"metric": "GB/s (sample reuse, algorithmic bytes)", "value": gbs, "unit": "GB/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded previous frame (weight 4)",
+            "config": {"workload": f"fractalRenderAdvanced {w}x{h}, previous frame on the same rectangle, "
+                                   "reuse only", "l2": "flushed between steps", "reused_fraction": reused},
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "traffic": None, "peak_source": src, "bytes_per_pixel": 32},
+            "gpu_launches": args.steps, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def run_serve(args):
     """C5: 16 zoom sessions (720p..2160p), 1.02x zoom per frame toward seeded
     boundary points, Poisson arrivals at 60 Hz per session, HBM-budget admission,
@@ -1039,7 +1104,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["c1", "c2", "c2-crop", "c3", "c4", "c4-crop", "c5", "compose"],
+    ap.add_argument("--workload", choices=["c1", "c2", "c2-crop", "c3", "c4", "c4-crop", "c5", "compose", "reuse"],
                     default="c2",
                     help="c2-crop / c4-crop: the central 480x270 pixels of the frame / 256x256 of each viewport "
                          "(for profiler captures)")
@@ -1053,6 +1118,8 @@ def main():
         run_c1(args)
     elif args.workload == "compose":
         run_compose(args)
+    elif args.workload == "reuse":
+        run_reuse(args)
     elif args.workload == "c3":
         run_deep(args)
     elif args.workload in ("c4", "c4-crop"):

@@ -39,6 +39,7 @@ template <class R> struct MainArgs {
     uint32_t *counter;
     unsigned long long *total;  // optional: pixel-iterations of the samples taken
     NewtonParams newton;        // Newton modules only
+    uint32_t tile_chunk;        // tiles per claim (set by the launcher)
 };
 
 template <class R> struct AdvancedArgs {
