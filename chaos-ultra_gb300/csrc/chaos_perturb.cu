@@ -59,6 +59,7 @@ template <class D> struct PerturbArgs {
     uint32_t w, h, spp, mode, max_iter, n_pix;
     uint64_t seed;
     double ps, half_w, half_h;
+    double off_x, off_y;                   // frame centre - orbit centre (plane units)
     const typename Vec2T<D>::type *orbit;  // Z_0 .. Z_{orbit_last}
     const double2 *orbit64;                // the same orbit in binary64 (rescaled glitch test)
     const float2 *orbit2;                  // 2 Z_m in binary32 (rescaled linear steps)
@@ -181,8 +182,8 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                     ox = unit53(sample_hash(a.seed, pix, s, 0));
                     oy = unit53(sample_hash(a.seed, pix, s, 1));
                 }
-                double ddx = __dmul_rn(__dsub_rn(__dadd_rn((double)px, ox), a.half_w), a.ps);
-                double ddy = __dmul_rn(-__dsub_rn(__dadd_rn((double)py, oy), a.half_h), a.ps);
+                double ddx = __fma_rn(__dsub_rn(__dadd_rn((double)px, ox), a.half_w), a.ps, a.off_x);
+                double ddy = __fma_rn(-__dsub_rn(__dadd_rn((double)py, oy), a.half_h), a.ps, a.off_y);
                 dcx = (D)ddx;
                 dcy = (D)ddy;
                 scaled = false;
@@ -627,6 +628,8 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
     a.seed = d->seed;
     a.ps = d->pixel_size;
     a.half_w = 0.5 * d->width;
+    a.off_x = d->center_x;
+    a.off_y = d->center_y;
     a.half_h = 0.5 * d->height;
     if (std::is_same<D, float>::value)
         a.orbit = reinterpret_cast<const typename Vec2T<D>::type *>(orb->z32);

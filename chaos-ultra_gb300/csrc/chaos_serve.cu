@@ -31,6 +31,10 @@
 
 namespace chaos {
 int api_fail(int code, const char *fmt, ...);  // chaos_api.cu
+int api_orbit_create_d(double center_x, double center_y, uint32_t bits, uint32_t max_iterations,
+                       chaos_orbit **out);  // chaos_perturb.cu
+int api_perturb_enqueue(const chaos_frame_desc *desc, const chaos_orbit *orbit, const chaos_frame_out *out,
+                        cudaStream_t stream, uint32_t *counter);  // chaos_perturb.cu
 }
 using namespace chaos;
 
@@ -60,6 +64,9 @@ struct Session {
     bool has_prev = false;
     double prev_rect[4] = {0, 0, 0, 0};
     double cx = 0, cy = 0, span = 0;
+    double off_x = 0, off_y = 0;  // frame centre - target, zoomed alongside (deep frames)
+    chaos_orbit *orbit = nullptr;  // reference orbit of the target, once frames go past binary64
+    uint32_t orbit_bits = 0;
     uint32_t frames = 0;
 };
 
@@ -87,6 +94,7 @@ void free_session(Session &s)
     if (s.rgba) cudaFree(s.rgba);
     if (s.counter) cudaFree(s.counter);
     if (s.iters) cudaFree(s.iters);
+    if (s.orbit) chaos_orbit_destroy(s.orbit);
     if (s.stream) cudaStreamDestroy(s.stream);
     s = Session();
 }
@@ -176,6 +184,8 @@ int chaos_server_open(chaos_server *s, const chaos_session_desc *d, uint32_t *se
     ss.cx = d->center_x;
     ss.cy = d->center_y;
     ss.span = d->span;
+    ss.off_x = d->center_x - d->target_x;
+    ss.off_y = d->center_y - d->target_y;
     s->used += bytes;
     uint32_t id = 0;
     while (id < s->sessions.size() && s->sessions[id].open) id++;
@@ -240,6 +250,77 @@ static cudaError_t enqueue_frame(chaos_server *srv, Session &s, const double rec
     return e;
 }
 
+// A frame past binary64 (the reference stops there): perturbation around the
+// session's target with binary64 differences, one sample per pixel centre, into
+// the session's pixel buffer, then compose.  The target's reference orbit is
+// computed once (again only when the zoom needs more bits) and stays resident
+// with the session.  The frame centre sits at off from the target, which keeps
+// its place on screen as the zoom goes on.
+static int submit_deep_locked(chaos_server *srv, Session &s, uint32_t session, double arrival)
+{
+    const chaos_session_desc &d = s.d;
+    const double ps = s.span / d.width;
+    const uint32_t need = (uint32_t)std::min(1536.0, std::max(128.0, std::ceil((-std::log2(ps) + 96.0) / 64.0) * 64.0));
+    if (!s.orbit || s.orbit_bits < need) {
+        if (s.orbit) {
+            cudaStreamSynchronize(s.stream);  // frames in flight still read it
+            chaos_orbit_destroy(s.orbit);
+            s.orbit = nullptr;
+        }
+        int rc = api_orbit_create_d(d.target_x, d.target_y, need, d.max_iterations, &s.orbit);
+        if (rc != CHAOS_OK) return rc;
+        s.orbit_bits = need;
+    }
+    srv->records.emplace_back();
+    FrameRecord &r = srv->records.back();
+    r.session = session;
+    r.frame = s.frames;
+    r.arrival = arrival;
+    r.start = srv->now();
+    r.precision = CHAOS_PRECISION_TOO_BIG;
+    r.server = srv;
+    chaos_frame_desc fd{};
+    fd.width = d.width;
+    fd.height = d.height;
+    fd.max_iterations = d.max_iterations;
+    fd.samples_per_pixel = 1;
+    fd.sample_mode = CHAOS_SAMPLES_CENTER;
+    fd.tier = CHAOS_TIER_PERTURB_F64;
+    fd.center_x = s.off_x;
+    fd.center_y = s.off_y;
+    fd.pixel_size = ps;
+    chaos_frame_out fo{};
+    fo.pixels = reinterpret_cast<chaos_pixel_info *>(s.buf[0]);
+    fo.pixels_pitch = (long)s.pitch[0];
+    fo.total_iterations = s.iters;
+    int rc = api_perturb_enqueue(&fd, s.orbit, &fo, s.stream, nullptr);
+    if (rc != CHAOS_OK) {
+        r.done.store(-2.0);
+        return rc;
+    }
+    ComposeArgs c{};
+    c.in = s.buf[0];
+    c.pitch = (long)s.pitch[0];
+    c.out = s.rgba;
+    c.out_pitch = (long)s.rgba_pitch;
+    c.w = d.width;
+    c.h = d.height;
+    c.palette = srv->palette;
+    c.palette_len = srv->palette_len;
+    c.max_ss = 1.f;
+    c.visualize = false;
+    cudaError_t e = launch_compose(c, s.stream);
+    if (e == cudaSuccess) e = cudaLaunchHostFunc(s.stream, frame_done, &r);
+    if (e != cudaSuccess) {
+        r.done.store(-2.0);
+        return api_fail(CHAOS_ERR_CUDA, "frame enqueue: %s", cudaGetErrorString(e));
+    }
+    rect_of(s, s.prev_rect);
+    s.has_prev = true;
+    s.frames++;
+    return CHAOS_OK;
+}
+
 static int submit_locked(chaos_server *srv, uint32_t session, double arrival)
 {
     if (session >= srv->sessions.size() || !srv->sessions[session].open)
@@ -251,11 +332,15 @@ static int submit_locked(chaos_server *srv, uint32_t session, double arrival)
         double z = d.zoom_per_frame;
         s.cx = d.target_x + (s.cx - d.target_x) / z;
         s.cy = d.target_y + (s.cy - d.target_y) / z;
+        s.off_x /= z;
+        s.off_y /= z;
         s.span /= z;
     }
     double rect[4];
     rect_of(s, rect);
     int prec = chaos_select_precision(rect, d.width, d.height);
+    if (prec == CHAOS_PRECISION_TOO_BIG && d.fractal == 0 && s.span / d.width >= 1e-290)
+        return submit_deep_locked(srv, s, session, arrival);
     srv->records.emplace_back();
     FrameRecord &r = srv->records.back();
     r.session = session;

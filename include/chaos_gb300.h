@@ -391,7 +391,12 @@ int chaos_server_session_bytes(const chaos_session_desc *desc, size_t *bytes);
 int chaos_server_open(chaos_server *server, const chaos_session_desc *desc, uint32_t *session);
 int chaos_server_close(chaos_server *server, uint32_t session);
 /* Enqueue the session's next frame and return at once (arrival_s is recorded
- * as the request's arrival time). */
+ * as the request's arrival time).  A Mandelbrot frame past binary64
+ * (chaos_select_precision says CHAOS_PRECISION_TOO_BIG, where the reference's
+ * renderer stops) is rendered by perturbation around the session's target
+ * with binary64 differences, one sample per pixel centre; the target's
+ * reference orbit is computed at the first such frame (again when the zoom
+ * needs more bits) and held by the session until it closes. */
 int chaos_server_submit(chaos_server *server, uint32_t session, double arrival_s);
 /* Wait until every submitted frame has finished. */
 int chaos_server_drain(chaos_server *server);
@@ -426,8 +431,9 @@ int chaos_orbit_info(const chaos_orbit *orbit, uint32_t *stored, uint32_t *escap
 int chaos_orbit_destroy(chaos_orbit *orbit);
 
 /* A frame by perturbation (tier CHAOS_TIER_PERTURB_F32 or _F64, Mandelbrot).
- * Sample positions as in chaos_render_frame with the orbit's centre as centre
- * (desc->center_x/y are not used): each sample iterates its difference from the
+ * Sample positions as in chaos_render_frame, with desc->center_x/y read as the
+ * frame centre's offset from the orbit's centre in plane units (0, 0: the
+ * frame is centred on the orbit): each sample iterates its difference from the
  * reference orbit and restarts from the orbit's start (rebasing) when
  * |z| < |difference| or when the orbit ends.  Outputs as chaos_render_frame. */
 int chaos_render_frame_perturb_async(const chaos_frame_desc *desc, const chaos_orbit *orbit,

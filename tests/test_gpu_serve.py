@@ -126,3 +126,56 @@ def test_trace_replay_records_latency(cuda):
         assert [r[1] for r in mine] == list(range(len(mine)))
         assert all(r[4] >= r[2] >= 0 for r in mine)
     srv.close()
+
+
+def test_deep_session_goes_on_by_perturbation(cuda):
+    """A session zooming past binary64 (where the reference's renderer stops)
+    renders by perturbation around its target with the target's orbit held by
+    the session: the served image equals a perturbation frame rendered
+    directly at the same offset, pixel size and orbit precision, composed with
+    the same palette."""
+    import math
+
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import default_palette
+    from chaos_gb300.workloads import boundary_point
+    torch = cuda
+    w, h, mi, z, frames = 320, 180, 3000, 4.0, 9
+    target = boundary_point(21, 3000)
+    center = (target[0] + 2e-13, target[1] - 1e-13)
+    pal = default_palette()
+    srv = cg.Server(1 << 28, pal)
+    d = cg.SessionDesc(width=w, height=h, max_iterations=mi, max_super_sampling=2.0, flags=FLAGS_REUSE,
+                       fractal=cg.MANDELBROT, arith=cg.ARITH_FMA, center_x=center[0], center_y=center[1],
+                       span=4e-12, target_x=target[0], target_y=target[1], zoom_per_frame=z)
+    sid = srv.open(d)
+    for _ in range(frames):
+        srv.submit(sid)
+    srv.drain()
+    recs = srv.records()
+    precs = [r[5] for r in recs]
+    assert precs[0] == cg.PRECISION_DOUBLE and precs[-1] == cg.PRECISION_TOO_BIG, precs
+    img, iters = srv.read(sid)
+    # the same frame, rendered directly: the server's offset and span after `frames` frames
+    off_x, off_y, span = center[0] - target[0], center[1] - target[1], 4e-12
+    for _ in range(frames - 1):
+        off_x, off_y, span = off_x / z, off_y / z, span / z
+    ps = span / w
+    bits = int(min(1536, max(128, math.ceil((-math.log2(ps) + 96) / 64) * 64)))
+    orbit = cg.Orbit(cg.to_hex_fixed(target[0], bits), cg.to_hex_fixed(target[1], bits), bits, mi)
+    pitch = 16 * w
+    pix = torch.zeros((h, pitch), dtype=torch.uint8, device="cuda:0")
+    desc_ = cg.FrameDesc(width=w, height=h, max_iterations=mi, samples_per_pixel=1, sample_mode=cg.SAMPLES_CENTER,
+                         tier=cg.TIER_PERTURB_F64, fractal=cg.MANDELBROT, seed=0, center_x=off_x, center_y=off_y,
+                         pixel_size=ps)
+    cg.render_frame_perturb(desc_, orbit, cg.FrameOut(pixels=pix.data_ptr(), pixels_pitch=pitch))
+    dpal = torch.from_numpy(np.ascontiguousarray(pal, dtype=np.uint32).view(np.int32)).to("cuda:0")
+    rgba = torch.zeros((h, w), dtype=torch.int32, device="cuda:0")
+    with cg.Module("mandelbrot") as m:
+        m.compose(pix.data_ptr(), pitch, rgba.data_ptr(), 4 * w, w, h, dpal.data_ptr(), len(pal), 1.0)
+    torch.cuda.synchronize()
+    want = rgba.cpu().numpy().view(np.uint32).reshape(-1)
+    assert np.array_equal(img.reshape(-1), want)
+    assert len(np.unique(want)) > 8  # the view shows structure
+    orbit.close()
+    srv.close()
