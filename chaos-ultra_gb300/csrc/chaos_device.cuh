@@ -16,6 +16,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "chaos_intarith.cuh"
+
 namespace chaos {
 
 // 16-byte per-pixel record, identical in layout to pixel_info_t
@@ -154,6 +156,25 @@ template <class R> __device__ __forceinline__ void step_rounded6(R &x, R &y, R c
     y = O::fma(R(2), p, cy);
     x = xn;
     emin = min(emin, exponent_bits(p));
+}
+
+// Binary64: the same step with x*x - y*y formed on the integer units
+// (sub_nonneg_bits, exactly the rounded difference), which leaves five
+// operations per step on the binary64 pipe.  A difference the integer
+// routine hands back (a subnormal operand or result) sets emin to 0, so the
+// block is redone with step<double, ARITH_PARITY> like a small product.
+template <> __device__ __forceinline__ void step_rounded6<double>(double &x, double &y, double cx, double cy,
+                                                                  uint32_t &emin)
+{
+    const double xx = __dmul_rn(x, x), yy = __dmul_rn(y, y);
+    bool exact;
+    const double t = __longlong_as_double((long long)sub_nonneg_bits((uint64_t)__double_as_longlong(xx),
+                                                                     (uint64_t)__double_as_longlong(yy), exact));
+    const double xn = __dadd_rn(t, cx);
+    const double p = __dmul_rn(x, y);
+    y = __fma_rn(2.0, p, cy);
+    x = xn;
+    emin = min(emin, exact ? exponent_bits(p) : 0u);
 }
 
 // The binary64 fused step with 2x formed on the integer pipe: adding 1 to the

@@ -85,12 +85,14 @@ class Driver:
         self._check(self.cu.cuMemcpyHtoD_v2(C.c_uint64(ptr), buf, C.c_size_t(size)), "cuMemcpyHtoD")
         return size
 
-    def launch(self, fn, grid, block, params):
-        """params: list of ctypes objects; kernelParams[i] = &params[i] (Pointer.to(...) in JCuda)."""
+    def launch(self, fn, grid, block, params, sync=True):
+        """params: list of ctypes objects; kernelParams[i] = &params[i] (Pointer.to(...) in JCuda).
+        The launch goes to the legacy default stream, like JCuda's."""
         arr = (C.c_void_p * len(params))(*[C.cast(C.pointer(p), C.c_void_p) for p in params])
         self._check(self.cu.cuLaunchKernel(fn, grid[0], grid[1], 1, block[0], block[1], 1, 0, None, arr, None),
                     "cuLaunchKernel")
-        self._check(self.cu.cuCtxSynchronize(), "cuCtxSynchronize")
+        if sync:
+            self._check(self.cu.cuCtxSynchronize(), "cuCtxSynchronize")
 
 
 # Parameter arrays exactly as the Java kernels build them (CudaHelpers.pointerTo).

@@ -1,0 +1,142 @@
+"""The drop-in module against the reference's own kernels on the same GPU:
+same inputs, same launch shape (32x32 blocks on the default stream, as the
+Java host launches), identical pixel records, and the time of each launch.
+
+oracle/build_ref.sh builds the reference's mandelbrot module from its source
+for sm_103a twice: with nvcc's default contraction (the build the Java
+application loads) and with --fmad=false (the rounding the oracle and the
+parity module follow).  Workloads, both in the reference's own sampling
+(fractalRenderMain: sample 0 at the pixel corner, then the diagonal / grid
+pattern with warp votes):
+
+* C2 view: binary64, pixel 1e-10/3840 around the seeded boundary centre of
+  the 3840x2160 workload (bisection along the ray of seed 2), maxIter 20000,
+  maxSS 4, adaptive sampling on; the central 1920x1080 of the frame;
+* C1 view: binary32, 1024x1024 over [-2, 1] x [-1.5, 1.5], maxIter 1000,
+  maxSS 1.
+
+The same frames also go through the C ABI (chaos_render_main_f64/_f32).
+Each kernel runs once untimed, then once between CUDA events.  The times are
+printed as one JSON line per view (run pytest with -s to see them)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+from tests.gpu_util import Driver, java_grid, main_params, pitched, read_pixels, same_pixels  # noqa: E402
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF_DIR = os.path.join(ROOT, "oracle", "_ref")
+
+C2_FULL_W, C2_SPAN, C2_MAX_ITER, C2_SEED = 3840, 1e-10, 20000, 2
+C2_W, C2_H = 1920, 1080
+
+
+@pytest.fixture(scope="module")
+def drv(cuda, native):
+    return Driver()
+
+
+def _cubin(name):
+    p = os.path.join(REF_DIR, name)
+    if not os.path.exists(p):
+        pytest.skip(f"reference cubin not built ({p})")
+    return p
+
+
+def _ours(parity):
+    import chaos_gb300 as cg
+    return os.path.join(cg.DROPIN_PARITY_DIR if parity else cg.DROPIN_DIR, "mandelbrot.ptx")
+
+
+def _timed_main(drv, cuda, path, w, h, rect, max_iter, max_ss, flags, dbl):
+    """One untimed and one timed launch of fractalRenderMain{Float,Double}; (pixels, ms)."""
+    mod = drv.load(path)
+    try:
+        drv.write_constant(mod, "VISUALIZE_SAMPLE_COUNT", b"\0")
+        fn = drv.function(mod, "fractalRenderMainDouble" if dbl else "fractalRenderMainFloat")
+        buf, pitch = pitched(cuda, w, h)
+        grid, block = java_grid(w, h)
+        params = main_params(buf.data_ptr(), pitch, w, h, rect, max_iter, max_ss, flags, dbl)
+        drv.launch(fn, grid, block, params)
+        buf.zero_()
+        e0, e1 = cuda.cuda.Event(enable_timing=True), cuda.cuda.Event(enable_timing=True)
+        cuda.cuda.synchronize()
+        e0.record()
+        drv.launch(fn, grid, block, params, sync=False)
+        e1.record()
+        cuda.cuda.synchronize()
+        return read_pixels(buf, w), e0.elapsed_time(e1)
+    finally:
+        drv.unload(mod)
+
+
+def _timed_library(cuda, w, h, rect, max_iter, max_ss, flags, dbl):
+    """The same render through the C ABI (chaos_render_main_f64/_f32, parity
+    arithmetic) on the current stream; (pixels, ms)."""
+    import chaos_gb300 as cg
+    module = cg.Module("mandelbrot")
+    buf, pitch = pitched(cuda, w, h)
+    stream = cuda.cuda.current_stream()
+
+    def run():
+        module.render_main(buf.data_ptr(), pitch, w, h, rect, max_iter, max_ss, flags, double=dbl,
+                           arith=cg.ARITH_PARITY, stream=stream)
+
+    run()
+    buf.zero_()
+    e0, e1 = cuda.cuda.Event(enable_timing=True), cuda.cuda.Event(enable_timing=True)
+    cuda.cuda.synchronize()
+    e0.record(stream)
+    run()
+    e1.record(stream)
+    cuda.cuda.synchronize()
+    return read_pixels(buf, w), e0.elapsed_time(e1)
+
+
+def _compare(drv, cuda, name, w, h, rect, max_iter, max_ss, flags, dbl):
+    ref_nofma, t_ref_nofma = _timed_main(drv, cuda, _cubin("ref_mandelbrot_nofma.cubin"), w, h, rect, max_iter,
+                                         max_ss, flags, dbl)
+    ref_fma, t_ref_fma = _timed_main(drv, cuda, _cubin("ref_mandelbrot.cubin"), w, h, rect, max_iter, max_ss, flags,
+                                     dbl)
+    ours_par, t_par = _timed_main(drv, cuda, _ours(True), w, h, rect, max_iter, max_ss, flags, dbl)
+    ours_fma, t_fma = _timed_main(drv, cuda, _ours(False), w, h, rect, max_iter, max_ss, flags, dbl)
+    lib_par, t_lib = _timed_library(cuda, w, h, rect, max_iter, max_ss, flags, dbl)
+    line = {"view": name, "width": w, "height": h, "max_iter": max_iter, "max_ss": max_ss,
+            "ms": {"reference_nofma": t_ref_nofma, "dropin_parity": t_par, "reference_default": t_ref_fma,
+                   "dropin_fma": t_fma,
+                   "library_parity": t_lib},
+            "speedup": {"parity_vs_reference_nofma": t_ref_nofma / t_par,
+                        "fma_vs_reference_default": t_ref_fma / t_fma,
+                        "library_parity_vs_reference_nofma": t_ref_nofma / t_lib},
+            "records_differing": {"parity_vs_reference_nofma": float(same_pixels(ours_par, ref_nofma).mean()),
+                                  "fma_vs_reference_default": float(same_pixels(ours_fma, ref_fma).mean()),
+                                  "library_parity_vs_reference_nofma": float(same_pixels(lib_par, ref_nofma).mean())}}
+    print(json.dumps(line), flush=True)
+    return line
+
+
+def test_c2_view_dropin_vs_reference_kernel(drv, cuda):
+    """The parity module equals the reference built with --fmad=false record for
+    record and is faster than it on the deep binary64 view."""
+    import chaos_gb300 as cg
+    from chaos_gb300.workloads import boundary_point
+    cx, cy = boundary_point(C2_SEED, max_iter=C2_MAX_ITER)
+    ps = C2_SPAN / C2_FULL_W
+    rect = (cx - C2_W / 2 * ps, cy - C2_H / 2 * ps, cx + C2_W / 2 * ps, cy + C2_H / 2 * ps)
+    line = _compare(drv, cuda, "C2 central 1920x1080, reference sampling", C2_W, C2_H, rect, C2_MAX_ITER, 4.0,
+                    cg.FLAG_ADAPTIVE_SS, True)
+    assert line["records_differing"]["parity_vs_reference_nofma"] == 0.0
+    assert line["records_differing"]["library_parity_vs_reference_nofma"] == 0.0
+    assert line["speedup"]["parity_vs_reference_nofma"] > 1.0
+    assert line["speedup"]["fma_vs_reference_default"] > 1.0
+
+
+def test_c1_view_dropin_vs_reference_kernel(drv, cuda):
+    line = _compare(drv, cuda, "C1 1024x1024 binary32, reference sampling", 1024, 1024, (-2.0, -1.5, 1.0, 1.5), 1000,
+                    1.0, 0, False)
+    assert line["records_differing"]["parity_vs_reference_nofma"] == 0.0
+    assert line["speedup"]["parity_vs_reference_nofma"] > 1.0
