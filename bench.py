@@ -136,8 +136,8 @@ class ClockSampler:
 # CPU leg: the reference's per-sample function (or the oracle port) on the host
 # ---------------------------------------------------------------------------
 
-def _cpu_impl():
-    """(kind, runner): runner(xs, ys) -> (total pixel-iterations, counts)."""
+def _cpu_impl(max_iter=MAX_ITER):
+    """(kind, threads, runner): runner(xs, ys[, max_iter]) -> (total pixel-iterations, counts)."""
     from oracle import build_oracle
     from oracle.oracle import REF_LIB, Oracle, Reference
     build_oracle.build_oracle()
@@ -148,12 +148,12 @@ def _cpu_impl():
     if os.path.exists(REF_LIB):
         try:
             ref = Reference()
-            return "reference", ref.max_threads(), lambda xs, ys: ref.points_d(xs, ys, MAX_ITER)
+            return "reference", ref.max_threads(), lambda xs, ys, mi=max_iter: ref.points_d(xs, ys, mi)
         except OSError:
             pass
     o = Oracle()
     # the oracle's restatement of computeFractal<double> (rounded arithmetic), OpenMP over points
-    return "port", o.max_threads(), lambda xs, ys: o.mandelbrot_points_d(xs, ys, MAX_ITER)
+    return "port", o.max_threads(), lambda xs, ys, mi=max_iter: o.mandelbrot_points_d(xs, ys, mi)
 
 
 def cpu_sample_points(wl, n_pixels, seed=11):
@@ -411,7 +411,14 @@ def _l2_flush(torch, dev):
 
 def run_batch(args):
     """C4: 64 viewports (side 256..2048, span 1e-12..1e-3, maxIter 500..50000,
-    seeded boundary centres) in one CUDA-graph launch, tier per viewport."""
+    seeded boundary centres) in one CUDA-graph launch, tier per viewport.
+
+    Beside the tiered value: the same batch in binary64 rounded as the
+    reference's computeFractal<double> (tier F64_ROUNDED, the FP64 oracle's
+    counts bit for bit), whose counts give every other form's mismatch against
+    the FP64 oracle over all pixels; and a CPU leg that runs the reference's own
+    host-built computeFractal<double> at seeded pixels of every viewport (the
+    CPU baseline, and the oracle those counts are checked on)."""
     import numpy as np
     import torch
 
@@ -522,9 +529,33 @@ def run_batch(args):
         deep_ms.append(e0.elapsed_time(e1))
     deep_value = deep.read_total() / (min(deep_ms) / 1e3) / 1e9
     deep_tiers = deep.tiers()
-    deep_diff = sum(int((c.cpu().numpy() != a).sum()) for (c, _), a in zip(dbufs, plain_counts))
+    deep_counts = [c.cpu().numpy() for c, _ in dbufs]
+    deep_diff = sum(int((c != a).sum()) for c, a in zip(deep_counts, plain_counts))
     deep.close()
-    del deep, dbufs, plain_counts
+    del deep, dbufs
+
+    # binary64 rounded as the reference's computeFractal<double> (tier
+    # F64_ROUNDED): the FP64 oracle's escape counts, bit for bit, for every pixel
+    rounded, rbufs = make(cg.TIER_F64_ROUNDED, tuned)
+    rounded.launch(stream)
+    torch.cuda.synchronize()
+    r_ms = []
+    for k in range(2):
+        flush(k)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rounded.launch(stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        r_ms.append(e0.elapsed_time(e1))
+    rounded_iters = rounded.read_total()
+    rounded_value = rounded_iters / (min(r_ms) / 1e3) / 1e9
+    rounded_counts = [c.cpu().numpy() for c, _ in rbufs]
+    rounded.close()
+    del rounded, rbufs
+
+    def vs_oracle(counts):
+        return sum(int((c != r).sum()) for c, r in zip(counts, rounded_counts)) / total
 
     # time per tier: the same batch restricted to one tier's viewports
     per_tier = {}
@@ -576,6 +607,35 @@ def run_batch(args):
         vals = out.view(torch.float32).reshape(h_, w_, 4)[:, :, 0].cpu().numpy()
         dm_iters += int(np.where(vals == 0, sp["max_iter"], vals).astype(np.int64).sum())
     dropin_value = dm_iters / (dm_ms / 1e3) / 1e9
+
+    # CPU leg: the reference's own computeFractal<double> (host build, all host
+    # threads) at seeded pixels of every viewport, the same binary64 sample
+    # points: the CPU baseline, and the FP64 oracle the GPU counts are checked on
+    from oracle.oracle import Oracle
+    kind, cpu_threads, cpu_run = _cpu_impl()
+    orc = Oracle()
+    rng = np.random.default_rng(44)
+    cpu_iters, cpu_s, cpu_n, cpu_bad = 0, 0.0, 0, {"rounded": 0, "tiered": 0, "tiered_deep": 0, "f64_fma": 0}
+    per_vp = 1024 if args.workload == "c4" else 256
+    for k, sp in enumerate(specs):
+        n_pix = sp["width"] * sp["height"]
+        pix = np.sort(rng.choice(n_pix, size=min(per_vp, n_pix), replace=False))
+        pts = [orc.frame_points(sp["width"], sp["height"], 1, 0, sp["seed"], sp["center"], sp["span"] / sp["width"],
+                                int(q), 1) for q in pix]
+        xs = np.concatenate([a for a, _ in pts])
+        ys = np.concatenate([b for _, b in pts])
+        t0 = time.perf_counter()
+        it, ref_counts = cpu_run(xs, ys, sp["max_iter"])
+        cpu_s += time.perf_counter() - t0
+        cpu_iters += it
+        cpu_n += len(pix)
+        for name, arr in (("rounded", rounded_counts), ("tiered", tiered_counts), ("tiered_deep", deep_counts),
+                          ("f64_fma", plain_counts)):
+            cpu_bad[name] += int((arr[k].view(np.uint32)[pix] != ref_counts).sum())
+    cpu_base = {"value": cpu_iters / cpu_s / 1e9, "unit": "Gpixel-iter/s", "cores": cpu_threads, "kind": kind,
+                "sample": f"{cpu_n} seeded pixels ({per_vp} per viewport) at the batch's sample points, "
+                          f"FP64 computeFractal, {cpu_iters} pixel-iterations in {cpu_s:.2f} s"}
+    oracle_mismatch = {name: bad / cpu_n for name, bad in cpu_bad.items()}
     line = {"metric": "Gpixel-iter/s (batched uneven launch)", "value": value, "unit": "Gpixel-iter/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(ms) / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/ff/f64 per viewport",
@@ -605,6 +665,18 @@ def run_batch(args):
                                     "(orbits computed at batch creation, outside the timed launch)"},
             "per_tier": per_tier,
             "escape_count_mismatch_vs_f64_batch": diff / total,
+            "rounded_f64_batch": {
+                "value": rounded_value, "ms": min(r_ms), "pixel_iterations": rounded_iters,
+                "speedup_of_plain_f64_dropin": rounded_value / dropin_value,
+                "escape_count_mismatch_vs_fp64_oracle_cpu_sample": oracle_mismatch["rounded"],
+                "what": "all 64 viewports in binary64 rounded as the reference's computeFractal<double> "
+                        "(tier F64_ROUNDED, one graph launch): the form within 0.1% of the FP64 oracle"},
+            "escape_count_mismatch_vs_fp64_oracle": {
+                "all_pixels_vs_rounded_batch": {"tiered": vs_oracle(tiered_counts),
+                                                "tiered_deep": vs_oracle(deep_counts),
+                                                "f64_fma_batch": vs_oracle(plain_counts)},
+                "cpu_sample_vs_reference": oracle_mismatch},
+            "cpu_baseline": cpu_base,
             "gpu_launches": args.steps * sum(1 for t in (0, 1, 2) if t in tiers),
             "gpu_launches_note": "one persistent kernel per tier present per graph launch", "clocks": clk}
     print(json.dumps(line), flush=True)

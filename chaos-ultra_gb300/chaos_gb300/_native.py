@@ -44,6 +44,7 @@ TIER_F64 = 1
 TIER_FLOATFLOAT = 2
 TIER_PERTURB_F32 = 3
 TIER_PERTURB_F64 = 4
+TIER_F64_ROUNDED = 5  # batches: binary64 rounded as the reference's computeFractal<double>
 
 MANDELBROT = 0
 JULIA = 1

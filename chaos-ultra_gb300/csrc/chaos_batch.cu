@@ -78,6 +78,23 @@ template <> struct Num<FF> {
     static __device__ __forceinline__ bool blockable(T cx, T cy) { return blockable_c(cx.hi, cy.hi); }
 };
 
+// Binary64 with the reference's rounding (tier CHAOS_TIER_F64_ROUNDED): the
+// rounded step of the frame path, five binary64 operations with x*x - y*y on
+// the integer units, redone with the literal step when its checks ask for it.
+struct R64 {};
+template <> struct Num<R64> {
+    using T = double;
+    static __device__ __forceinline__ T from(double d) { return d; }
+    static __device__ __forceinline__ T zero() { return 0.0; }
+    static __device__ __forceinline__ void step(T &x, T &y, T cx, T cy)
+    {
+        chaos::step<double, ARITH_PARITY>(x, y, cx, cy);
+    }
+    static __device__ __forceinline__ double r2(T x, T y) { return radius2<double, ARITH_PARITY>(x, y); }
+    static __device__ __forceinline__ bool blockable(T cx, T cy) { return blockable_c(cx, cy); }
+};
+template <class N> constexpr bool is_binary64() { return std::is_same<N, double>::value || std::is_same<N, R64>::value; }
+
 constexpr uint32_t BATCH_MAX_VIEWPORTS = 1024;
 
 template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchArgs a)
@@ -168,7 +185,7 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
                 i = 0;
                 window = 0;
                 if (max_iter == 0) done = true;
-                if constexpr (std::is_same<N, double>::value) {
+                if constexpr (is_binary64<N>()) {
                     // start at z = c, the first step's result (+0 for -0), so that no
                     // block begins with x = 0 (which the integer doubling redoes)
                     if (max_iter > 0) {
@@ -223,6 +240,16 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
                 uint32_t emin = 0xffffffffu;
                 run_block([&](T &u, T &v) { step_fma3(u, v, cx, cy, emin); });
                 if (emin == 0u) {
+                    x = sx;
+                    y = sy;
+                    run_block([&](T &u, T &v) { P::step(u, v, cx, cy); });
+                }
+            } else if constexpr (std::is_same<N, R64>::value) {
+                // x*x - y*y on the integer units, fma(2, x*y, cy); a block with a
+                // product or difference near the subnormal range is redone literally
+                uint32_t emin = 0xffffffffu;
+                run_block([&](T &u, T &v) { step_rounded6<double>(u, v, cx, cy, emin); });
+                if (emin < exponent_bits_two<double>()) {
                     x = sx;
                     y = sy;
                     run_block([&](T &u, T &v) { P::step(u, v, cx, cy); });
@@ -345,6 +372,7 @@ static void prepare_batch_kernels()
         set_carveout<float, 8>(), set_carveout<float, 16>(), set_carveout<float, 32>();
         set_carveout<FF, 8>(), set_carveout<FF, 16>(), set_carveout<FF, 32>();
         set_carveout<double, 8>(), set_carveout<double, 16>(), set_carveout<double, 32>();
+        set_carveout<R64, 8>(), set_carveout<R64, 16>(), set_carveout<R64, 32>();
         return true;
     }();
     (void)done;
@@ -386,7 +414,7 @@ using namespace chaos;
 
 namespace {
 constexpr int kTiers = 3;  // 0 binary32, 1 float-float, 2 binary64
-int tier_slot(uint32_t tier) { return tier == CHAOS_TIER_F32 ? 0 : tier == CHAOS_TIER_FLOATFLOAT ? 1 : 2; }
+int tier_slot(uint32_t tier) { return tier == CHAOS_TIER_F32 ? 0 : tier == CHAOS_TIER_FLOATFLOAT ? 1 : 2; }  // F64 or F64_ROUNDED: 2
 }  // namespace
 
 // A viewport of the batch rendered by perturbation (its own reference orbit).
@@ -408,6 +436,7 @@ struct chaos_batch {
     uint32_t palette_len = 0, interior = 0;
     int threads[kTiers] = {256, 256, 256}, k[kTiers] = {16, 16, 16}, chunk[kTiers] = {1, 1, 1};
     int fp64_warps = 8;  // binary64 warps per SM when it shares the SMs
+    bool rounded64 = false;  // the binary64 slot runs CHAOS_TIER_F64_ROUNDED
     int sms = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -470,7 +499,7 @@ static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s
     int per_sm[kTiers] = {0, 0, 0};
     bool shared = false;
     if (b->n_jobs[2] && (b->n_jobs[0] || b->n_jobs[1])) {
-        Footprint f64 = footprint<double>(b->threads[2], b->k[2]);
+        Footprint f64 = b->rounded64 ? footprint<R64>(b->threads[2], b->k[2]) : footprint<double>(b->threads[2], b->k[2]);
         int b64 = std::max(1, std::min(f64.alone, b->fp64_warps / std::max(1, f64.warps)));
         int dev = 0, smem_sm = 0;
         cudaGetDevice(&dev);
@@ -513,7 +542,9 @@ static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s
         const bool after = shared && t != 2;
         if (t == 0) e = launch_batch<float>(a, b->threads[t], b->k[t], b->sms, per_sm[t], after, s);
         if (t == 1) e = launch_batch<FF>(a, b->threads[t], b->k[t], b->sms, per_sm[t], after, s);
-        if (t == 2) e = launch_batch<double>(a, b->threads[t], b->k[t], b->sms, per_sm[t], after, s);
+        if (t == 2)
+            e = b->rounded64 ? launch_batch<R64>(a, b->threads[t], b->k[t], b->sms, per_sm[t], after, s)
+                             : launch_batch<double>(a, b->threads[t], b->k[t], b->sms, per_sm[t], after, s);
     }
     if (shared && e == cudaSuccess) {
         // the binary64 tail: a second, full-size grid on the same job counter.
@@ -530,7 +561,8 @@ static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s
         a.palette = b->palette;
         a.palette_len = b->palette_len;
         a.interior_rgba = b->interior;
-        e = launch_batch<double>(a, b->threads[2], b->k[2], b->sms, 0, true, s0);
+        e = b->rounded64 ? launch_batch<R64>(a, b->threads[2], b->k[2], b->sms, 0, true, s0)
+                         : launch_batch<double>(a, b->threads[2], b->k[2], b->sms, 0, true, s0);
     }
     if (e == cudaSuccess) e = cudaEventRecord(j1, s1);
     if (e == cudaSuccess) e = cudaEventRecord(j2, s2);
@@ -549,7 +581,7 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
     std::vector<BatchViewport> per[kTiers];
     std::vector<uint32_t> tiers(n);
     uint64_t jobs[kTiers] = {0, 0, 0};
-    bool any_rgba = false;
+    bool any_rgba = false, any_f64 = false, any_rounded = false;
     for (uint32_t k = 0; k < n; k++) {
         const chaos_viewport &v = vps[k];
         if (v.width == 0 || v.height == 0 || (uint64_t)v.width * v.height > (1ull << 31))
@@ -566,9 +598,14 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
                         : v.tier == CHAOS_TIER_AUTO_DEEP ? auto_deep_tier(v.center_x, v.center_y, v.pixel_size)
                                                          : v.tier;
         if (tier != CHAOS_TIER_F32 && tier != CHAOS_TIER_FLOATFLOAT && tier != CHAOS_TIER_F64 &&
-            tier != CHAOS_TIER_PERTURB_F32 && tier != CHAOS_TIER_PERTURB_F64)
+            tier != CHAOS_TIER_F64_ROUNDED && tier != CHAOS_TIER_PERTURB_F32 && tier != CHAOS_TIER_PERTURB_F64)
             return api_fail(CHAOS_ERR_UNSUPPORTED, "viewport %u: tier %u not batchable", k, tier);
         tiers[k] = tier;
+        any_f64 |= tier == CHAOS_TIER_F64;
+        any_rounded |= tier == CHAOS_TIER_F64_ROUNDED;
+        if (any_f64 && any_rounded)
+            return api_fail(CHAOS_ERR_INVALID_ARGUMENT,
+                            "viewport %u: binary64 viewports of one batch must all be fused or all rounded", k);
         if (tier == CHAOS_TIER_PERTURB_F32 || tier == CHAOS_TIER_PERTURB_F64) {
             if (!(v.pixel_size >= 1e-290))
                 return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "viewport %u: perturbation needs pixel >= 1e-290", k);
@@ -604,6 +641,7 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
     cudaGetDevice(&b->device);
     cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
     b->tiers = tiers;
+    b->rounded64 = any_rounded;
     b->palette = palette;
     b->palette_len = palette_len;
     b->interior = interior_rgba;
@@ -844,7 +882,9 @@ int chaos_batch_autotune(const chaos_viewport *vps, uint32_t n, const char *cach
         uint32_t tier = v.tier == CHAOS_TIER_AUTO        ? chaos_batch_auto_tier(v.center_x, v.center_y, v.pixel_size)
                         : v.tier == CHAOS_TIER_AUTO_DEEP ? auto_deep_tier(v.center_x, v.center_y, v.pixel_size)
                                                          : v.tier;
-        if (tier != CHAOS_TIER_F32 && tier != CHAOS_TIER_FLOATFLOAT && tier != CHAOS_TIER_F64) continue;
+        if (tier != CHAOS_TIER_F32 && tier != CHAOS_TIER_FLOATFLOAT && tier != CHAOS_TIER_F64 &&
+            tier != CHAOS_TIER_F64_ROUNDED)
+            continue;
         const int t = tier_slot(tier);
         chaos_viewport c = v;
         c.tier = tier;
@@ -855,7 +895,7 @@ int chaos_batch_autotune(const chaos_viewport *vps, uint32_t n, const char *cach
         c.counts = nullptr;
         c.smooth = nullptr;
         c.rgba = nullptr;
-        const uint32_t fields[5] = {c.width, c.height, c.samples_per_pixel, c.sample_mode, c.max_iterations};
+        const uint32_t fields[6] = {c.width, c.height, c.samples_per_pixel, c.sample_mode, c.max_iterations, c.tier};
         sig[t] = fnv1a(sig[t], fields, sizeof(fields));
         const double geo[3] = {c.center_x, c.center_y, c.pixel_size};
         sig[t] = fnv1a(sig[t], geo, sizeof(geo));
@@ -947,7 +987,9 @@ int chaos_batch_autotune(const chaos_viewport *vps, uint32_t n, const char *cach
                                 : v.tier == CHAOS_TIER_AUTO_DEEP
                                     ? auto_deep_tier(v.center_x, v.center_y, v.pixel_size)
                                     : v.tier;
-                if (tier != CHAOS_TIER_F32 && tier != CHAOS_TIER_FLOATFLOAT && tier != CHAOS_TIER_F64) continue;
+                if (tier != CHAOS_TIER_F32 && tier != CHAOS_TIER_FLOATFLOAT && tier != CHAOS_TIER_F64 &&
+            tier != CHAOS_TIER_F64_ROUNDED)
+            continue;
                 chaos_viewport c = v;
                 c.tier = tier;
                 c.width = std::min<uint32_t>(v.width, std::max<uint32_t>(64, v.width / 4));

@@ -277,6 +277,13 @@ int chaos_render_frame_host(const chaos_frame_desc *desc, const uint32_t *palett
 
 #define CHAOS_TIER_AUTO 255      /* binary32 / float-float / binary64 by pixel size */
 #define CHAOS_TIER_AUTO_DEEP 254 /* binary32 / float-float / perturbation where AUTO would pick binary64 */
+/* Batched binary64 with every operation rounded as the reference's
+ * computeFractal<double> rounds it (no contraction): the escape counts of the
+ * FP64 oracle, bit for bit.  The binary64 viewports of one batch are all
+ * CHAOS_TIER_F64 (fused) or all CHAOS_TIER_F64_ROUNDED; mixing the two fails
+ * with CHAOS_ERR_INVALID_ARGUMENT.  Launch shape: the binary64 entries of
+ * chaos_batch_config. */
+#define CHAOS_TIER_F64_ROUNDED 5
 
 /* One viewport of a batch.  Samples as in chaos_frame_desc (the plane point is
  * computed in binary64, then rounded to the viewport's tier).  Outputs are
@@ -287,7 +294,7 @@ typedef struct chaos_viewport {
     uint32_t max_iterations;
     uint32_t samples_per_pixel;
     uint32_t sample_mode;
-    uint32_t tier; /* CHAOS_TIER_F32, _FLOATFLOAT, _F64, _PERTURB_F32, _PERTURB_F64, _AUTO or _AUTO_DEEP */
+    uint32_t tier; /* CHAOS_TIER_F32, _FLOATFLOAT, _F64, _F64_ROUNDED, _PERTURB_F32, _PERTURB_F64, _AUTO or _AUTO_DEEP */
     uint64_t seed;
     double center_x, center_y, pixel_size;
     uint32_t *counts;

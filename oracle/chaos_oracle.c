@@ -1140,14 +1140,15 @@ static uint32_t esc_ff(uint32_t max_iter, ff_t cx, ff_t cy, float *r2_exit)
 }
 
 typedef struct {
-    uint32_t w, h, spp, mode, max_iter, tier; /* tier: 0 binary32, 1 binary64, 2 float-float */
+    uint32_t w, h, spp, mode, max_iter, tier; /* tier: 0 binary32, 1 binary64, 2 float-float, 5 binary64 rounded */
     uint64_t seed;
     double cx, cy, ps;
 } orc_viewport;
 
 /* One viewport of a batch: sample point in binary64 (fma), rounded to the
- * tier, Mandelbrot with fused multiply-adds (binary32/64) or float-float;
- * outputs as orc_frame.  Returns the pixel-iterations. */
+ * tier, Mandelbrot with fused multiply-adds (binary32/64), float-float, or
+ * the reference's rounded binary64 loop (mandelbrot.cu:16-21); outputs as
+ * orc_frame.  Returns the pixel-iterations. */
 uint64_t orc_batch_viewport(const orc_viewport *v, uint32_t *counts, float *smooth, uint32_t *rgba,
                             const uint32_t *palette, uint32_t palette_len, uint32_t interior_rgba)
 {
@@ -1172,6 +1173,10 @@ uint64_t orc_batch_viewport(const orc_viewport *v, uint32_t *counts, float *smoo
             } else if (v->tier == 1) {
                 double r2;
                 i = esc_fma_d(v->max_iter, 0.0, 0.0, cxd, cyd, &r2);
+                r2f = (float)r2;
+            } else if (v->tier == 5) { /* binary64 rounded as computeFractal<double> */
+                double r2;
+                i = esc_parity_d(v->max_iter, 0.0, 0.0, cxd, cyd, &r2);
                 r2f = (float)r2;
             } else {
                 i = esc_ff(v->max_iter, ff_from_double(cxd), ff_from_double(cyd), &r2f);

@@ -94,6 +94,46 @@ def test_batch_rejects_bad_config(cuda):
         build(cuda, VIEWS[:2], seeded_palette(16), cg.BatchConfig((0, 0, 0), (0, 0, 0), (0, 65, 0)))
 
 
+# binary64 rounded as the reference's computeFractal<double> (tier 5), beside a
+# binary32 viewport; the 31x31 view has a sample row on the real axis (y = 0,
+# products 0: the literal-step redo)
+ROUNDED_VIEWS = [
+    (80, 40, 1, 1, 3000, 5, (-0.74364388703715, 0.13182590420531), 8e-12),
+    (64, 48, 2, 1, 2500, 5, (-0.748, 0.1), 1.4e-5),
+    (40, 30, 1, 0, 1500, 5, (-0.925, 0.266), 3e-3),
+    (31, 31, 1, 0, 800, 5, (-0.5, 0.0), 2.5),
+    (1, 1, 4, 1, 100, 5, (-1.95, 0.0), 1e-3),
+    (33, 17, 3, 1, 1200, 0, (-0.235125, 0.827215), 4e-4),
+]
+
+
+def test_batch_rounded_binary64_matches_oracle(cuda, oracle):
+    """Tier F64_ROUNDED gives the FP64 oracle's escape counts bit for bit."""
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import seeded_palette
+    pal = seeded_palette(256, seed=3)
+    b, bufs, _ = build(cuda, ROUNDED_VIEWS, pal)
+    assert b.tiers() == [cg.TIER_F64_ROUNDED] * 5 + [cg.TIER_F32]
+    got = run(cuda, b, bufs)
+    for k, ((w, h, spp, mode, mi, tier, c, span), (counts, smooth, rgba)) in enumerate(zip(ROUNDED_VIEWS, got)):
+        o = oracle.batch_viewport(w, h, spp, mode, mi, tier, 17 + w, c, span / w, palette=pal)
+        assert np.array_equal(counts, o["counts"]), (k, int((counts != o["counts"]).sum()))
+        tol = 2 * np.spacing(np.abs(o["smooth"])) + 2e-6
+        assert (np.abs(smooth - o["smooth"]) <= tol).all(), k
+        d = np.abs(rgba.view(np.uint8).astype(int) - o["rgba"].view(np.uint8).astype(int))
+        assert d.max() <= 1, k
+    assert b.read_total() == sum(int(c.astype(np.int64).sum()) for c, _, _ in got)
+    b.close()
+
+
+def test_batch_rejects_mixed_binary64_arithmetic(cuda):
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import seeded_palette
+    views = [(8, 8, 1, 0, 100, cg.TIER_F64, (0.3, 0.02), 0.5), (8, 8, 1, 0, 100, cg.TIER_F64_ROUNDED, (0.3, 0.02), 0.5)]
+    with pytest.raises(cg.ChaosError):
+        build(cuda, views, seeded_palette(16))
+
+
 def test_autotune_picks_a_shape_and_caches_it(cuda, tmp_path):
     """The autotuner returns a shape from its search space for each tier slot
     present, the batch built with it gives the default shape's bits, and a

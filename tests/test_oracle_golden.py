@@ -143,3 +143,20 @@ def test_rounded_step_doubling_identity():
         assert libm.fma(2.0, p, cy) == (2.0 * x) * y + cy, (x, y, cy)
         checked += 1
     assert checked > 4000
+
+
+def test_rounded_batch_tier_is_the_reference_loop(oracle, reference):
+    """The oracle's batch viewport in the rounded binary64 tier (5) gives the
+    reference's computeFractal<double> counts at the same sample points.  The
+    view is dyadic (pixel 2^-9, centre (-0.75, 0.09375)), so each sample point
+    is one rounded add whether formed with an fma or not."""
+    w = h = 48
+    ps, cx, cy, mi = 2.0 ** -9, -0.75, 0.09375, 3000
+    o = oracle.batch_viewport(w, h, 1, 0, mi, 5, 1, (cx, cy), ps)
+    q = np.arange(w * h)
+    xs = cx + ((q % w) + 0.5 - w / 2) * ps
+    ys = cy - ((q // w) + 0.5 - h / 2) * ps
+    total, want = reference.points_d(xs, ys, mi)
+    assert np.array_equal(o["counts"], want)
+    assert o["total"] == total
+    assert 0 < (want == mi).sum() < len(want)  # interior and exterior both present
