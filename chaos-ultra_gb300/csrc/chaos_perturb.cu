@@ -217,10 +217,20 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                     if (n > 0) {
                         float wx = (float)dx, wy = (float)dy;
                         const float ux = (float)dcx, uy = (float)dcy;
+                        const float2 *Z2p = a.orbit2 + m;
+                        if (n == B) {
+                            // the usual case: a whole block, no per-step bound
 #pragma unroll
-                        for (uint32_t j = 0; j < B; j++) {
-                            if (j < n) {
-                                const float2 Z2 = a.orbit2[m + j];
+                            for (uint32_t j = 0; j < B; j++) {
+                                const float2 Z2 = Z2p[j];
+                                const float nx = __fmaf_rn(Z2.x, wx, __fmaf_rn(-Z2.y, wy, ux));
+                                const float ny = __fmaf_rn(Z2.x, wy, __fmaf_rn(Z2.y, wx, uy));
+                                wx = nx;
+                                wy = ny;
+                            }
+                        } else {
+                            for (uint32_t j = 0; j < n; j++) {
+                                const float2 Z2 = Z2p[j];
                                 const float nx = __fmaf_rn(Z2.x, wx, __fmaf_rn(-Z2.y, wy, ux));
                                 const float ny = __fmaf_rn(Z2.x, wy, __fmaf_rn(Z2.y, wx, uy));
                                 wx = nx;
@@ -320,10 +330,19 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                         const uint32_t n = min(min(16u, ev > m ? ev - m - 1u : 0u), a.max_iter - 1u - i);
                         if (n > 0) {
                             double wx = dx, wy = dy;
+                            const double2 *Z2p = a.orbit2_64 + m;
+                            if (n == 16) {
 #pragma unroll
-                            for (uint32_t j = 0; j < 16; j++) {
-                                if (j < n) {
-                                    const double2 Z2 = a.orbit2_64[m + j];
+                                for (uint32_t j = 0; j < 16; j++) {
+                                    const double2 Z2 = Z2p[j];
+                                    const double nx = __fma_rn(Z2.x, wx, __fma_rn(-Z2.y, wy, (double)dcx));
+                                    const double ny = __fma_rn(Z2.x, wy, __fma_rn(Z2.y, wx, (double)dcy));
+                                    wx = nx;
+                                    wy = ny;
+                                }
+                            } else {
+                                for (uint32_t j = 0; j < n; j++) {
+                                    const double2 Z2 = Z2p[j];
                                     const double nx = __fma_rn(Z2.x, wx, __fma_rn(-Z2.y, wy, (double)dcx));
                                     const double ny = __fma_rn(Z2.x, wy, __fma_rn(Z2.y, wx, (double)dcy));
                                     wx = nx;
