@@ -207,7 +207,7 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                 i = 0;
                 if (a.max_iter == 0) done = true;
             }
-#pragma unroll 4
+#pragma unroll 1
             for (int k = 0; k < K && !done; k++) {
                 if constexpr (S) if (scaled && e < -126) {
                     // linear steps up to (not onto) the next index whose tests can fire
