@@ -758,7 +758,7 @@ def run_c1(args):
     roof = {"bound": "fp32-pipe", "achieved": achieved / 1e12, "peak": peak / 2 / 1e12, "unit": "Top/s",
             "frac": achieved / (peak / 2), "traffic": None, "ops_per_iteration": ops,
             "peak_source": "measured in this run: chaos_measure_fma_peak (full-occupancy FFMA chains)",
-            "kernel": "k_frame<float,PARITY,mandelbrot,32>"}
+            "kernel": "k_frame<float,PARITY,mandelbrot,64>"}
 
     # CPU leg: the reference's computeFractal<float> over the whole frame, all host threads
     cpu = None
