@@ -200,6 +200,28 @@ __device__ __forceinline__ void step_fma3(double &x, double &y, double cx, doubl
     x = xn;
 }
 
+// Up to K steps of the reference loop, each with its own test (binary32
+// frames): stops at a state that tests >= 4 (esc, r2 = its test value) or
+// after `lim` steps when BOUNDED.  Returns the steps taken.  In rounded
+// arithmetic the test's products are the step's own, so a test costs one add,
+// a compare and a branch; a lane that stops waits for its warp at the end of
+// the block.  Exact for every c, with no roll-back or search.
+template <class R, int A, int K, bool BOUNDED>
+__device__ __forceinline__ uint32_t tested_block(R &x, R &y, R cx, R cy, uint32_t lim, R &r2, bool &esc)
+{
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        if (BOUNDED && (uint32_t)k == lim) return lim;
+        r2 = radius2<R, A>(x, y);
+        if (!(r2 < R(4))) {
+            esc = true;
+            return (uint32_t)k;
+        }
+        step<R, A>(x, y, cx, cy);
+    }
+    return (uint32_t)K;
+}
+
 // Escape loop with the reference's semantics:
 //     i = 0; while (i < max_iter && r2(z) < 4) { z = z^2 + c; ++i; }  return i
 // run as blocks of ESCAPE_BLOCK untested steps.  A block is kept when its last
@@ -210,7 +232,10 @@ __device__ __forceinline__ void step_fma3(double &x, double &y, double cx, doubl
 // binary32), and |z| keeps growing until it overflows to inf/NaN; neither
 // tests below 4, so a block whose last state tests below 4 contains no
 // escape.  Otherwise `blockable` is false and every step is tested.
-// r2_exit is r2 of the final state.
+// r2_exit is r2 of the final state.  (Tested blocks, which the binary32
+// frame kernel uses, were slower here: a tile's lanes run in lock step, so
+// every lane pays the per-step test for as long as the tile's slowest lane
+// runs, while a roll-back costs only the lane that escaped.)
 // Binary64 blocks run step_rounded6 / step_fma3 (the same values as step<>)
 // and are redone with step<> when the integer checks ask for it.  i0 is the
 // iteration count of the state passed in (1 when a Mandelbrot caller starts

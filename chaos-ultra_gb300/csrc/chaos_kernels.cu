@@ -93,28 +93,6 @@ __device__ __forceinline__ uint32_t pack_mean_rgba(const float acc[4], uint32_t 
     return out;
 }
 
-// Up to K steps of the reference loop, each with its own test (binary32
-// frames): stops at a state that tests >= 4 (esc, r2 = its test value) or
-// after `lim` steps when BOUNDED.  Returns the steps taken.  In rounded
-// arithmetic the test's products are the step's own, so a test costs one add,
-// a compare and a branch; a lane that stops waits for its warp at the end of
-// the block.  Exact for every c, with no roll-back or search.
-template <class R, int A, int K, bool BOUNDED>
-__device__ __forceinline__ uint32_t tested_block(R &x, R &y, R cx, R cy, uint32_t lim, R &r2, bool &esc)
-{
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-        if (BOUNDED && (uint32_t)k == lim) return lim;
-        r2 = radius2<R, A>(x, y);
-        if (!(r2 < R(4))) {
-            esc = true;
-            return (uint32_t)k;
-        }
-        step<R, A>(x, y, cx, cy);
-    }
-    return (uint32_t)K;
-}
-
 template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIST_THREADS) k_frame(FrameArgs<R> a)
 {
     __shared__ uint32_t s_pal[PALETTE_SMEM];
