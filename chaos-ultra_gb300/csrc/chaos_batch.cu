@@ -635,6 +635,19 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
     }
     if (any_rgba && (!palette || palette_len == 0 || palette_len > 4096))
         return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "rgba outputs need a device palette of 1..4096 entries");
+    // Costly viewports first: lanes claim a tier's job space in order, so the
+    // pixels with the highest maxIter x samples start first and the end of the
+    // launch, where lanes run out of work, is made of short ones.
+    for (int t = 0; t < kTiers; t++) {
+        std::stable_sort(per[t].begin(), per[t].end(), [](const BatchViewport &p, const BatchViewport &q) {
+            return (uint64_t)p.max_iter * p.spp > (uint64_t)q.max_iter * q.spp;
+        });
+        uint32_t base = 0;
+        for (BatchViewport &bv : per[t]) {
+            bv.job_base = base;
+            base += bv.w * bv.h;
+        }
+    }
 
     chaos_batch *b = new (std::nothrow) chaos_batch();
     if (!b) return api_fail(CHAOS_ERR_OUT_OF_MEMORY, "out of host memory");

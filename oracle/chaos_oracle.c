@@ -828,7 +828,7 @@ uint64_t orc_mandelbrot_points_d(long n, const double *xs, const double *ys, uin
                                  uint32_t *counts)
 {
     uint64_t total = 0;
-#pragma omp parallel for schedule(dynamic, 256) reduction(+ : total)
+#pragma omp parallel for schedule(dynamic, 8) reduction(+ : total)
     for (long k = 0; k < n; k++) {
         double r2;
         uint32_t i = arith == ORC_ARITH_FMA ? esc_fma_d(max_iter, 0.0, 0.0, xs[k], ys[k], &r2)

@@ -107,7 +107,7 @@ unsigned long long ref_mandelbrot_points_d(size_t n, const double *x, const doub
 {
     unsigned long long total = 0;
     if (n_threads > 0) omp_set_num_threads(n_threads);
-#pragma omp parallel for schedule(dynamic, 256) reduction(+ : total)
+#pragma omp parallel for schedule(dynamic, 8) reduction(+ : total)
     for (long k = 0; k < (long)n; k++) {
         unsigned e = (unsigned)ref_mandelbrot_d(max_iter, x[k], y[k]);
         if (e == 0) e = max_iter;
