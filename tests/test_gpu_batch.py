@@ -126,6 +126,33 @@ def test_batch_rounded_binary64_matches_oracle(cuda, oracle):
     b.close()
 
 
+def test_floatfloat_tier_accuracy_against_rounded_binary64(cuda):
+    """Float-float (about 48 bits) on views where that is ample: its escape
+    counts differ from the FP64 oracle's (the rounded binary64 tier) on few
+    pixels, no more than the fused binary64 tier's do plus a small margin.  A
+    broken double-word step (one that drops its normalisation, for instance)
+    shows up here even though it would still match its own restatement."""
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import seeded_palette
+    views = [(128, 96, 1, 0, 2000, (-0.748, 0.1), 1.4e-5),
+             (96, 96, 1, 0, 3000, (-0.925, 0.266), 3e-4),
+             (128, 64, 1, 0, 3000, (-0.74364388703715, 0.13182590420531), 1e-9)]
+    pal = seeded_palette(16)
+    counts = {}
+    for tier in (cg.TIER_FLOATFLOAT, cg.TIER_F64, cg.TIER_F64_ROUNDED):
+        b, bufs, _ = build(cuda, [(w, h, spp, m, mi, tier, c, sp) for w, h, spp, m, mi, c, sp in views], pal)
+        counts[tier] = [c for c, _, _ in run(cuda, b, bufs)]
+        b.close()
+    n = sum(len(c) for c in counts[cg.TIER_F64_ROUNDED])
+
+    def mismatch(t):
+        return sum(int((a != r).sum()) for a, r in zip(counts[t], counts[cg.TIER_F64_ROUNDED])) / n
+
+    ff, fused = mismatch(cg.TIER_FLOATFLOAT), mismatch(cg.TIER_F64)
+    print("float-float / fused binary64 mismatch vs rounded binary64:", ff, fused)
+    assert ff <= 2 * fused + 0.01, (ff, fused)
+
+
 def test_batch_rejects_mixed_binary64_arithmetic(cuda):
     import chaos_gb300 as cg
     from chaos_gb300.palette import seeded_palette
