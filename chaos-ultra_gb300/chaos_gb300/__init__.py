@@ -9,7 +9,7 @@ zoom sessions, `Orbit` / `render_frame_perturb` are the deep-zoom tier.
 Device buffers are passed as raw device pointers (e.g. torch tensor
 data_ptr()).
 """
-from ._native import (ARITH_FMA, ARITH_PARITY, DROPIN_DIR, DROPIN_PARITY_DIR, FLAG_ADAPTIVE_SS, FLAG_FOVEATION,
+from ._native import (ARITH_CONTRACTED, ARITH_FMA, ARITH_PARITY, DROPIN_DIR, DROPIN_PARITY_DIR, FLAG_ADAPTIVE_SS, FLAG_FOVEATION,
                       FLAG_IS_ZOOMING, FLAG_SAMPLE_REUSE, FLAG_VISUALIZE_SAMPLE_COUNT, FLAG_ZOOMING_IN, JULIA,
                       LIB_PATH, MANDELBROT, PRECISION_DOUBLE, PRECISION_SINGLE, PRECISION_TOO_BIG, SAMPLES_CENTER,
                       SAMPLES_JITTER, TIER_AUTO, TIER_AUTO_DEEP, TIER_F32, TIER_F64, TIER_F64_ROUNDED, TIER_FLOATFLOAT,
@@ -20,7 +20,7 @@ from .api import (Batch, Module, Orbit, Renderer, Server, auto_tier, autotune_ba
                   to_hex_fixed, version)
 
 __all__ = [
-    "ARITH_FMA", "ARITH_PARITY", "DROPIN_DIR", "DROPIN_PARITY_DIR", "FLAG_ADAPTIVE_SS", "FLAG_FOVEATION",
+    "ARITH_CONTRACTED", "ARITH_FMA", "ARITH_PARITY", "DROPIN_DIR", "DROPIN_PARITY_DIR", "FLAG_ADAPTIVE_SS", "FLAG_FOVEATION",
     "FLAG_IS_ZOOMING", "FLAG_SAMPLE_REUSE", "FLAG_VISUALIZE_SAMPLE_COUNT", "FLAG_ZOOMING_IN", "JULIA", "LIB_PATH",
     "MANDELBROT", "PRECISION_DOUBLE", "PRECISION_SINGLE", "PRECISION_TOO_BIG", "SAMPLES_CENTER", "SAMPLES_JITTER",
     "TIER_AUTO", "TIER_AUTO_DEEP", "TIER_F32", "TIER_F64", "TIER_F64_ROUNDED", "TIER_FLOATFLOAT", "TIER_PERTURB_F32", "TIER_PERTURB_F64",

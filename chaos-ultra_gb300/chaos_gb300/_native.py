@@ -32,6 +32,7 @@ FLAG_ZOOMING_IN = 1 << 5
 
 ARITH_FMA = 0
 ARITH_PARITY = 1
+ARITH_CONTRACTED = 2  # the reference module as nvcc builds it by default (reference-mode calls)
 
 PRECISION_SINGLE = 0
 PRECISION_DOUBLE = 1

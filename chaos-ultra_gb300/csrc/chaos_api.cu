@@ -237,7 +237,7 @@ const JsonValue *json_member(const JsonValue &o, const char *key)
 
 int arith_of(int arith)
 {
-    return arith == CHAOS_ARITH_PARITY ? ARITH_PARITY : ARITH_FMA;
+    return arith == CHAOS_ARITH_PARITY ? ARITH_PARITY : arith == CHAOS_ARITH_CONTRACTED ? ARITH_CONTRACTED : ARITH_FMA;
 }
 
 double float_ulp(float f)  // java.lang.Math.ulp(float)
@@ -690,6 +690,8 @@ static int frame_entry(const chaos_frame_desc *dsc, const chaos_frame_out *o, cu
     if (o->pixels && (rc = check_pitched(o->pixels, o->pixels_pitch, dsc->width, "pixels"))) return rc;
     if (o->rgba && (!o->palette || o->palette_len == 0))
         return fail(CHAOS_ERR_INVALID_ARGUMENT, "rgba output needs a palette");
+    if (dsc->arith != CHAOS_ARITH_FMA && dsc->arith != CHAOS_ARITH_PARITY)
+        return fail(CHAOS_ERR_UNSUPPORTED, "frames take CHAOS_ARITH_FMA or CHAOS_ARITH_PARITY");
     if (dsc->tier == CHAOS_TIER_F32) return frame_impl<float>(dsc, o, s, sync);
     if (dsc->tier == CHAOS_TIER_F64) return frame_impl<double>(dsc, o, s, sync);
     return fail(CHAOS_ERR_UNSUPPORTED, "unknown tier %u", dsc->tier);

@@ -31,7 +31,14 @@ struct PixelInfo {
 };
 static_assert(sizeof(PixelInfo) == 16, "pixel_info_t is 16 bytes");
 
-enum Arith { ARITH_PARITY = 0, ARITH_FMA = 1 };
+// ARITH_CONTRACTED: the reference modules as nvcc builds them by default
+// (contraction on).  Established against the reference's own default build:
+// every product and sum is rounded except where nvcc fuses a product that has
+// no other use into the add after it -- the escape step's y' = fma(2x, y, cy),
+// the sample's x coordinate fma(px + dx, psx, lbx), and in the reuse path
+// oy = fma(-ry, h, h), the filter's chain of products and the blend.  The
+// squares x*x and y*y feed both the test and x' and stay rounded.
+enum Arith { ARITH_PARITY = 0, ARITH_FMA = 1, ARITH_CONTRACTED = 2 };
 enum FractalKind {
     FRACTAL_MANDELBROT = 0,
     FRACTAL_JULIA = 1,
@@ -111,13 +118,14 @@ template <> struct Op<double> {
 template <class R, int A> __device__ __forceinline__ R radius2(R x, R y)
 {
     using O = Op<R>;
-    if (A == ARITH_PARITY) return O::add(O::mul(x, x), O::mul(y, y));
+    if (A == ARITH_PARITY || A == ARITH_CONTRACTED) return O::add(O::mul(x, x), O::mul(y, y));
     return O::fma(x, x, O::mul(y, y));
 }
 
 // One step of z <- z^2 + c.
-//   parity: x' = (x*x - y*y) + cx, y' = (2*x)*y + cy  (mandelbrot.cu:17-18 order)
-//   fma:    x' = fma(x, x, fma(-y, y, cx)), y' = fma(x + x, y, cy)  (4 FP32-pipe ops)
+//   parity:     x' = (x*x - y*y) + cx, y' = (2*x)*y + cy  (mandelbrot.cu:17-18 order)
+//   contracted: x' as parity, y' = fma(x + x, y, cy)
+//   fma:        x' = fma(x, x, fma(-y, y, cx)), y' = fma(x + x, y, cy)  (4 FP32-pipe ops)
 template <class R, int A> __device__ __forceinline__ void step(R &x, R &y, R cx, R cy)
 {
     using O = Op<R>;
@@ -125,6 +133,11 @@ template <class R, int A> __device__ __forceinline__ void step(R &x, R &y, R cx,
         R xx = O::mul(x, x), yy = O::mul(y, y);
         R xn = O::add(O::sub(xx, yy), cx);
         y = O::add(O::mul(O::mul(R(2), x), y), cy);
+        x = xn;
+    } else if (A == ARITH_CONTRACTED) {
+        R xx = O::mul(x, x), yy = O::mul(y, y);
+        R xn = O::add(O::sub(xx, yy), cx);
+        y = O::fma(O::add(x, x), y, cy);
         x = xn;
     } else {
         R t = O::fma(-y, y, cx);
@@ -200,6 +213,22 @@ __device__ __forceinline__ void step_fma3(double &x, double &y, double cx, doubl
     x = xn;
 }
 
+// step<double, ARITH_CONTRACTED> in four binary64 operations: x*x - y*y on the
+// integer units (sub_nonneg_bits) and 2x by the exponent field.  A block that
+// met x = 0, a subnormal x or a difference the integer routine hands back
+// (emin = 0) is redone with the literal step.
+__device__ __forceinline__ void step_contracted4(double &x, double &y, double cx, double cy, uint32_t &emin)
+{
+    const double xx = __dmul_rn(x, x), yy = __dmul_rn(y, y);
+    bool exact;
+    const double t = __longlong_as_double((long long)sub_nonneg_bits((uint64_t)__double_as_longlong(xx),
+                                                                     (uint64_t)__double_as_longlong(yy), exact));
+    const double xn = __dadd_rn(t, cx);
+    y = __fma_rn(twice_on_int(x, emin), y, cy);
+    x = xn;
+    emin = exact ? emin : 0u;
+}
+
 // Up to K steps of the reference loop, each with its own test (binary32
 // frames): stops at a state that tests >= 4 (esc, r2 = its test value) or
 // after `lim` steps when BOUNDED.  Returns the steps taken.  In rounded
@@ -259,6 +288,11 @@ __device__ __forceinline__ uint32_t escape(uint32_t max_iter, R x, R y, R cx, R 
 #pragma unroll
                 for (int k = 0; k < ESCAPE_BLOCK; k++) step_rounded6<R>(x, y, cx, cy, emin);
                 redo = emin < exponent_bits_two<R>();
+            } else if constexpr (sizeof(R) == 8 && A == ARITH_CONTRACTED) {
+                uint32_t emin = 0xffffffffu;
+#pragma unroll
+                for (int k = 0; k < ESCAPE_BLOCK; k++) step_contracted4(x, y, cx, cy, emin);
+                redo = emin == 0u;
             } else if constexpr (sizeof(R) == 8) {
                 uint32_t emin = 0xffffffffu;
 #pragma unroll
@@ -361,9 +395,11 @@ __device__ __forceinline__ SampleGeometry<R> make_geometry(const Rect<R> &r, UIn
     return g;
 }
 
-// Sample offset i (gen.cu:104-117) and plane point (gen.cu:119-124).
-template <class R> __device__ __forceinline__ void sample_point(const SampleGeometry<R> &g, uint32_t px, uint32_t py,
-                                                                uint32_t i, float sample_count_f, R &cx, R &cy)
+// Sample offset i (gen.cu:104-117) and plane point (gen.cu:119-124).  The
+// contracted build fuses the x coordinate's product into its add.
+template <class R, int A = ARITH_PARITY>
+__device__ __forceinline__ void sample_point(const SampleGeometry<R> &g, uint32_t px, uint32_t py, uint32_t i,
+                                             float sample_count_f, R &cx, R &cy)
 {
     using O = Op<R>;
     const uint32_t skip_first = 2;
@@ -376,7 +412,10 @@ template <class R> __device__ __forceinline__ void sample_point(const SampleGeom
         dx = (R)__fdiv_rn((float)((i - skip_first) % spr), spr_f);
         dy = (R)__fdiv_rn((float)((i - skip_first) / spr), spr_f);
     }
-    cx = O::add(g.lbx, O::mul(O::add((R)px, dx), g.psx));
+    if (A == ARITH_CONTRACTED)
+        cx = O::fma(O::add((R)px, dx), g.psx, g.lbx);
+    else
+        cx = O::add(g.lbx, O::mul(O::add((R)px, dx), g.psx));
     cy = O::add(g.rty, O::mul(-O::add((R)py, dy), g.psy));
 }
 
@@ -416,7 +455,7 @@ __device__ uint32_t sample_the_fractal(const SampleGeometry<R> &g, uint32_t px, 
         uint32_t e = 0;
         if (valid) {
             R cx, cy;
-            sample_point(g, px, py, i, sample_count_f, cx, cy);
+            sample_point<R, A>(g, px, py, i, sample_count_f, cx, cy);
             e = compute_fractal_g<R, A, F>(g, cx, cy);
             // pixel-iterations (escape-time modules; the Newton modules return a root index)
             if (F < FRACTAL_NEWTON_WIRED) iters += (F == FRACTAL_MANDELBROT && e == 0u) ? g.max_iter : e;
@@ -522,8 +561,9 @@ __device__ __forceinline__ void render_main_tile(const SampleGeometry<R> &g, voi
 // Sample reuse and foveation (fractalRenderAdvanced, gen.cu:194-368)
 // ---------------------------------------------------------------------------
 
-// getWarpingOriginOfSampleReuse, gen.cu:194-203
-template <class R>
+// getWarpingOriginOfSampleReuse, gen.cu:194-203 (contracted: the y flip is
+// one fused multiply-add)
+template <class R, int A = ARITH_PARITY>
 __device__ __forceinline__ void warping_origin(UInt2 p, UInt2 grid, const Rect<R> &cur, const Rect<R> &old, float &ox,
                                                float &oy)
 {
@@ -534,11 +574,18 @@ __device__ __forceinline__ void warping_origin(UInt2 p, UInt2 grid, const Rect<R
     R rx = O::div(O::sub(ppx, old.lbx), O::sub(old.rtx, old.lbx));
     R ry = O::div(O::sub(ppy, old.lby), O::sub(old.rty, old.lby));
     ox = __fmul_rn((float)rx, (float)grid.x);
-    float oyv = __fmul_rn((float)ry, (float)grid.y);
-    oy = __fsub_rn((float)grid.y, oyv);
+    if (A == ARITH_CONTRACTED) {
+        oy = __fmaf_rn(-(float)ry, (float)grid.y, (float)grid.y);
+    } else {
+        float oyv = __fmul_rn((float)ry, (float)grid.y);
+        oy = __fsub_rn((float)grid.y, oyv);
+    }
 }
 
-// readFromArrayUsingFiltering<float>, gen.cu:259-302
+// readFromArrayUsingFiltering<float>, gen.cu:259-302 (contracted: each term
+// after the first is a fused multiply-add onto the sum so far, the first two
+// as fma(w00, T00, w10*T10))
+template <int A = ARITH_PARITY>
 __device__ __forceinline__ void read_filtered(const void *in, long pitch, float x, float y, float &value, float &weight)
 {
     uint32_t i = (uint32_t)floorf(x), j = (uint32_t)floorf(y);
@@ -549,18 +596,30 @@ __device__ __forceinline__ void read_filtered(const void *in, long pitch, float 
     PixelInfo d = load_pixel(pixel_ptr(in, pitch, i + 1, j + 1));
     float oa = __fsub_rn(1.f, alpha), ob = __fsub_rn(1.f, beta);
     float w00 = __fmul_rn(oa, ob), w10 = __fmul_rn(alpha, ob), w01 = __fmul_rn(oa, beta), w11 = __fmul_rn(alpha, beta);
-    float r = __fadd_rn(__fmul_rn(w00, a.value), __fmul_rn(w10, b.value));
-    r = __fadd_rn(r, __fmul_rn(w01, c.value));
-    r = __fadd_rn(r, __fmul_rn(w11, d.value));
-    float w = __fadd_rn(__fmul_rn(w00, a.weight), __fmul_rn(w10, b.weight));
-    w = __fadd_rn(w, __fmul_rn(w01, c.weight));
-    w = __fadd_rn(w, __fmul_rn(w11, d.weight));
+    float r, w;
+    if (A == ARITH_CONTRACTED) {
+        r = __fmaf_rn(w00, a.value, __fmul_rn(w10, b.value));
+        r = __fmaf_rn(w01, c.value, r);
+        r = __fmaf_rn(w11, d.value, r);
+        w = __fmaf_rn(w00, a.weight, __fmul_rn(w10, b.weight));
+        w = __fmaf_rn(w01, c.weight, w);
+        w = __fmaf_rn(w11, d.weight, w);
+    } else {
+        r = __fadd_rn(__fmul_rn(w00, a.value), __fmul_rn(w10, b.value));
+        r = __fadd_rn(r, __fmul_rn(w01, c.value));
+        r = __fadd_rn(r, __fmul_rn(w11, d.value));
+        w = __fadd_rn(__fmul_rn(w00, a.weight), __fmul_rn(w10, b.weight));
+        w = __fadd_rn(w, __fmul_rn(w01, c.weight));
+        w = __fadd_rn(w, __fmul_rn(w11, d.weight));
+    }
     value = r;
     weight = w;
 }
 
 // getFoveationAdvisedSampleCount + linearMapping<float>, gen.cu:209-257.
 // Uniform over the 8x4 warp tile (the pixel is snapped to the tile corner).
+// Contracted: the distance's sum of squares and k*x + q are fused.
+template <int A = ARITH_PARITY>
 __device__ __forceinline__ void foveation(UInt2 p, UInt2 focus, float max_ss, float &advised, bool &inside)
 {
     const float pi_f = 3.14159265358979f;
@@ -569,11 +628,13 @@ __device__ __forceinline__ void foveation(UInt2 p, UInt2 focus, float max_ss, fl
     float foveal = max_ss >= 1.f ? 5.5f : (float)__dmul_rn(5.5, (double)max_ss);
     float peripheral = 60.f;
     float ddx = __fsub_rn((float)focus.x, (float)nx), ddy = __fsub_rn((float)focus.y, (float)ny);
-    float dist = __fmul_rn(__fsqrt_rn(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy))), pixel_cm);
+    float sq = A == ARITH_CONTRACTED ? __fmaf_rn(ddx, ddx, __fmul_rn(ddy, ddy))
+                                     : __fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy));
+    float dist = __fmul_rn(__fsqrt_rn(sq), pixel_cm);
     float angle = __fdiv_rn(__fmul_rn(atanf(__fdiv_rn(dist, screen_distance)), 180.f), pi_f);
     float k = __fdiv_rn(__fsub_rn(0.f, 1.f), __fsub_rn(peripheral, foveal));
     float q = __fdiv_rn(__fsub_rn(__fmul_rn(peripheral, 1.f), __fmul_rn(0.f, foveal)), __fsub_rn(peripheral, foveal));
-    float lin = __fadd_rn(__fmul_rn(k, angle), q);
+    float lin = A == ARITH_CONTRACTED ? __fmaf_rn(k, angle, q) : __fadd_rn(__fmul_rn(k, angle), q);
     float rel = (float)fmin(1.0, (double)lin);
     float adv = __fmul_rn(max_ss, rel);
     inside = false;
@@ -601,13 +662,13 @@ __device__ __forceinline__ void render_advanced_tile(const SampleGeometry<R> &g,
     float reused_v = 0.f, reused_w = 0.f;
     if (valid) {
         if ((flags & FLAG_FOVEATION) && (flags & FLAG_IS_ZOOMING) && (flags & FLAG_ZOOMING_IN))
-            foveation(p, focus, max_ss, advised, inside);
+            foveation<A>(p, focus, max_ss, advised, inside);
         if (flags & FLAG_SAMPLE_REUSE) {
             float ox, oy;
-            warping_origin(p, size, image, image_reused, ox, oy);
+            warping_origin<R, A>(p, size, image, image_reused, ox, oy);
             int oix = (int)roundf(ox), oiy = (int)roundf(oy);
             if (!(oix < 2 || (uint32_t)oix >= size.x - 2 || oiy < 2 || (uint32_t)oiy >= size.y - 2)) {
-                read_filtered(in, in_pitch, ox, oy, reused_v, reused_w);
+                read_filtered<A>(in, in_pitch, ox, oy, reused_v, reused_w);
                 reusing = !(reused_w < 0.1f);
             }
         }
@@ -629,7 +690,9 @@ __device__ __forceinline__ void render_advanced_tile(const SampleGeometry<R> &g,
         float rw = __fmul_rn(reused_w, 0.75f);
         res.weight_of_new_samples = sc;
         res.weight = __fadd_rn(rw, sc);
-        res.value = __fdiv_rn(__fadd_rn(__fmul_rn(reused_v, rw), __fmul_rn(samples, sc)), res.weight);
+        const float num = A == ARITH_CONTRACTED ? __fmaf_rn(reused_v, rw, __fmul_rn(samples, sc))
+                                                : __fadd_rn(__fmul_rn(reused_v, rw), __fmul_rn(samples, sc));
+        res.value = __fdiv_rn(num, res.weight);
     }
     if (group_b) {
         float sc = advised < 1.f ? 1.f : advised;

@@ -368,6 +368,9 @@ cudaError_t launch_main(const MainArgs<R> &a, int arith, int fractal, int sms, c
     if (arith == ARITH_PARITY)
         return fractal == FRACTAL_JULIA ? launch_main_t<R, ARITH_PARITY, FRACTAL_JULIA>(a, sms, s)
                                         : launch_main_t<R, ARITH_PARITY, FRACTAL_MANDELBROT>(a, sms, s);
+    if (arith == ARITH_CONTRACTED)
+        return fractal == FRACTAL_JULIA ? launch_main_t<R, ARITH_CONTRACTED, FRACTAL_JULIA>(a, sms, s)
+                                        : launch_main_t<R, ARITH_CONTRACTED, FRACTAL_MANDELBROT>(a, sms, s);
     return fractal == FRACTAL_JULIA ? launch_main_t<R, ARITH_FMA, FRACTAL_JULIA>(a, sms, s)
                                     : launch_main_t<R, ARITH_FMA, FRACTAL_MANDELBROT>(a, sms, s);
 }
@@ -380,6 +383,9 @@ cudaError_t launch_advanced(const AdvancedArgs<R> &a, int arith, int fractal, in
     if (arith == ARITH_PARITY)
         return fractal == FRACTAL_JULIA ? launch_advanced_t<R, ARITH_PARITY, FRACTAL_JULIA>(a, sms, s)
                                         : launch_advanced_t<R, ARITH_PARITY, FRACTAL_MANDELBROT>(a, sms, s);
+    if (arith == ARITH_CONTRACTED)
+        return fractal == FRACTAL_JULIA ? launch_advanced_t<R, ARITH_CONTRACTED, FRACTAL_JULIA>(a, sms, s)
+                                        : launch_advanced_t<R, ARITH_CONTRACTED, FRACTAL_MANDELBROT>(a, sms, s);
     return fractal == FRACTAL_JULIA ? launch_advanced_t<R, ARITH_FMA, FRACTAL_JULIA>(a, sms, s)
                                     : launch_advanced_t<R, ARITH_FMA, FRACTAL_MANDELBROT>(a, sms, s);
 }

@@ -1,7 +1,8 @@
 // dropin_module.cu -- the CUDA module the Java host loads by file path.
 //
 // Built once per fractal (-DCHAOS_DROPIN_FRACTAL=0 mandelbrot, 1 julia) and per
-// arithmetic (-DCHAOS_DROPIN_ARITH=ARITH_FMA | ARITH_PARITY) into a cubin that
+// arithmetic (-DCHAOS_DROPIN_ARITH=ARITH_CONTRACTED | ARITH_PARITY | ARITH_FMA)
+// into a cubin that
 // J/cudarenderer/FractalRenderingModule.java:73-100 opens with cuModuleLoad and
 // resolves with cuModuleGetFunction.  It exports the seven entry points
 // FractalRenderingModule.initialize requires, with the parameter order and

@@ -71,11 +71,17 @@ typedef struct chaos_pixel_info {
 /* Arithmetic of the escape loop.
  * CHAOS_ARITH_PARITY rounds every product and sum (the reference kernel built
  * with nvcc --fmad=false): escape counts are bit-identical to it.
+ * CHAOS_ARITH_CONTRACTED is the reference module as nvcc builds it by default
+ * (contraction on, the build the Java application loads): y' = fma(2x, y, cy),
+ * the sample's x coordinate and parts of the reuse path fused, everything
+ * else rounded; pixel records are bit-identical to that build.  Reference-mode
+ * calls (render_main / render_advanced, the renderer) only.
  * CHAOS_ARITH_FMA uses fused multiply-adds, 4 FP ops per iteration; counts are
  * bit-identical to the oracle's fma restatement and differ from PARITY only
  * where rounding decides an escape. */
 #define CHAOS_ARITH_FMA 0
 #define CHAOS_ARITH_PARITY 1
+#define CHAOS_ARITH_CONTRACTED 2
 
 /* ---- module level: FractalRenderingModule + its seven kernels ----------- */
 

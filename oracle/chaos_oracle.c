@@ -48,7 +48,7 @@ void orc_set_newton(const double roots[6], const double coeffs[4], int magnifier
 float orc_newton_compute_f(int fractal, uint32_t max_iter, float x, float y, const double *roots, const double *coeffs);
 float orc_newton_compute_d(int fractal, uint32_t max_iter, double x, double y, const double *roots,
                            const double *coeffs);
-enum { ORC_ARITH_FMA = 0, ORC_ARITH_PARITY = 1 }; /* same numbering as CHAOS_ARITH_* */
+enum { ORC_ARITH_FMA = 0, ORC_ARITH_PARITY = 1, ORC_ARITH_CONTRACTED = 2 }; /* same numbering as CHAOS_ARITH_* */
 
 /* kernel flag bits, gen.cu:157-161 */
 #define ORC_FLAG_ADAPTIVE_SS (1u << 0)
@@ -134,6 +134,61 @@ static uint32_t esc_fma_d(uint32_t max_iter, double x, double y, double cx, doub
     return i;
 }
 
+/* The reference loop as nvcc compiles it with contraction on (its default):
+ * the squares feed both the test and x', so they stay rounded products, and
+ * only y' = 2*x*y + cy becomes one fused multiply-add.  Established by
+ * comparing the reference's default sm_103a build with candidate roundings on
+ * the same points. */
+static uint32_t esc_contracted_f(uint32_t max_iter, float x, float y, float cx, float cy, float *r2_exit)
+{
+    uint32_t i = 0;
+    float r2;
+    for (;;) {
+        float xx = x * x, yy = y * y;
+        r2 = xx + yy;
+        if (!(i < max_iter && r2 < 4.0f)) break;
+        float xn = (xx - yy) + cx;
+        float yn = fmaf(x + x, y, cy);
+        x = xn;
+        y = yn;
+        ++i;
+    }
+    *r2_exit = r2;
+    return i;
+}
+
+static uint32_t esc_contracted_d(uint32_t max_iter, double x, double y, double cx, double cy, double *r2_exit)
+{
+    uint32_t i = 0;
+    double r2;
+    for (;;) {
+        double xx = x * x, yy = y * y;
+        r2 = xx + yy;
+        if (!(i < max_iter && r2 < 4.0)) break;
+        double xn = (xx - yy) + cx;
+        double yn = fma(x + x, y, cy);
+        x = xn;
+        y = yn;
+        ++i;
+    }
+    *r2_exit = r2;
+    return i;
+}
+
+static uint32_t esc_any_f(int arith, uint32_t max_iter, float x, float y, float cx, float cy, float *r2)
+{
+    return arith == ORC_ARITH_FMA          ? esc_fma_f(max_iter, x, y, cx, cy, r2)
+           : arith == ORC_ARITH_CONTRACTED ? esc_contracted_f(max_iter, x, y, cx, cy, r2)
+                                           : esc_parity_f(max_iter, x, y, cx, cy, r2);
+}
+
+static uint32_t esc_any_d(int arith, uint32_t max_iter, double x, double y, double cx, double cy, double *r2)
+{
+    return arith == ORC_ARITH_FMA          ? esc_fma_d(max_iter, x, y, cx, cy, r2)
+           : arith == ORC_ARITH_CONTRACTED ? esc_contracted_d(max_iter, x, y, cx, cy, r2)
+                                           : esc_parity_d(max_iter, x, y, cx, cy, r2);
+}
+
 /* computeFractal<float>: Mandelbrot starts at z=0 with c=point and maps an
  * interior point (i == maxIterations) to 0 (mandelbrot.cu:11-25); Julia starts
  * at z=point with c=(Real)julia_c and returns i unchanged (julia.cu:5-17). */
@@ -143,14 +198,12 @@ float orc_compute_fractal_f(int fractal, int arith, uint32_t max_iter, float px,
     uint32_t i;
     if (fractal >= 2) return orc_newton_compute_f(fractal, max_iter, px, py, g_newton_roots, g_newton_coeffs);
     if (fractal == ORC_MANDELBROT) {
-        i = arith == ORC_ARITH_FMA ? esc_fma_f(max_iter, 0.f, 0.f, px, py, &r2)
-                                   : esc_parity_f(max_iter, 0.f, 0.f, px, py, &r2);
+        i = esc_any_f(arith, max_iter, 0.f, 0.f, px, py, &r2);
         if (i == max_iter) return 0;
         return (float)i;
     }
     float cx = (float)jcx, cy = (float)jcy;
-    i = arith == ORC_ARITH_FMA ? esc_fma_f(max_iter, px, py, cx, cy, &r2)
-                               : esc_parity_f(max_iter, px, py, cx, cy, &r2);
+    i = esc_any_f(arith, max_iter, px, py, cx, cy, &r2);
     return (float)i;
 }
 
@@ -160,13 +213,11 @@ float orc_compute_fractal_d(int fractal, int arith, uint32_t max_iter, double px
     uint32_t i;
     if (fractal >= 2) return orc_newton_compute_d(fractal, max_iter, px, py, g_newton_roots, g_newton_coeffs);
     if (fractal == ORC_MANDELBROT) {
-        i = arith == ORC_ARITH_FMA ? esc_fma_d(max_iter, 0.0, 0.0, px, py, &r2)
-                                   : esc_parity_d(max_iter, 0.0, 0.0, px, py, &r2);
+        i = esc_any_d(arith, max_iter, 0.0, 0.0, px, py, &r2);
         if (i == max_iter) return 0;
         return (float)i;
     }
-    i = arith == ORC_ARITH_FMA ? esc_fma_d(max_iter, px, py, jcx, jcy, &r2)
-                               : esc_parity_d(max_iter, px, py, jcx, jcy, &r2);
+    i = esc_any_d(arith, max_iter, px, py, jcx, jcy, &r2);
     return (float)i;
 }
 
@@ -205,7 +256,9 @@ static uint32_t sample_escape(const orc_view *v, uint32_t px, uint32_t py, uint3
         }
         double psx = (v->rd[2] - v->rd[0]) / (double)v->w;
         double psy = (v->rd[3] - v->rd[1]) / (double)v->h;
-        double cx = v->rd[0] + ((double)px + dx) * psx;
+        /* the contracted build fuses the x coordinate's product into its add */
+        double cx = v->arith == ORC_ARITH_CONTRACTED ? fma((double)px + dx, psx, v->rd[0])
+                                                     : v->rd[0] + ((double)px + dx) * psx;
         double cy = v->rd[3] + (-((double)py + dy)) * psy;
         return (uint32_t)orc_compute_fractal_d(v->fractal, v->arith, v->max_iter, cx, cy, v->jcx, v->jcy);
     } else {
@@ -220,7 +273,8 @@ static uint32_t sample_escape(const orc_view *v, uint32_t px, uint32_t py, uint3
         }
         float psx = (v->rf[2] - v->rf[0]) / (float)v->w;
         float psy = (v->rf[3] - v->rf[1]) / (float)v->h;
-        float cx = v->rf[0] + ((float)px + dx) * psx;
+        float cx = v->arith == ORC_ARITH_CONTRACTED ? fmaf((float)px + dx, psx, v->rf[0])
+                                                    : v->rf[0] + ((float)px + dx) * psx;
         float cy = v->rf[3] + (-((float)py + dy)) * psy;
         return (uint32_t)orc_compute_fractal_f(v->fractal, v->arith, v->max_iter, cx, cy, v->jcx, v->jcy);
     }
@@ -403,11 +457,13 @@ static void warping_origin(const orc_view *v, const double old_rect[4], uint32_t
     }
     *ox = rx * (float)v->w;
     float oyv = ry * (float)v->h;
-    *oy = (float)v->h - oyv;
+    *oy = v->arith == ORC_ARITH_CONTRACTED ? fmaf(-ry, (float)v->h, (float)v->h) : (float)v->h - oyv;
 }
 
-/* readFromArrayUsingFiltering<float>, gen.cu:259-302 */
-static void read_filtered(const void *in, long pitch, float x, float y, float *value, float *weight)
+/* readFromArrayUsingFiltering<float>, gen.cu:259-302.  Contracted: every
+ * term after the first is fused onto the sum so far, the first pair as
+ * fma(w00, T00, w10 * T10). */
+static void read_filtered(int arith, const void *in, long pitch, float x, float y, float *value, float *weight)
 {
     uint32_t i = (uint32_t)floorf(x), j = (uint32_t)floorf(y);
     float alpha = x - (float)i, beta = y - (float)j;
@@ -416,12 +472,22 @@ static void read_filtered(const void *in, long pitch, float x, float y, float *v
     const orc_pixel_info *c = pixel_at((void *)in, pitch, i, j + 1);
     const orc_pixel_info *d = pixel_at((void *)in, pitch, i + 1, j + 1);
     float w00 = (1 - alpha) * (1 - beta), w10 = alpha * (1 - beta), w01 = (1 - alpha) * beta, w11 = alpha * beta;
-    float r = w00 * a->value + w10 * b->value;
-    r = r + w01 * c->value;
-    r = r + w11 * d->value;
-    float ww = w00 * a->weight + w10 * b->weight;
-    ww = ww + w01 * c->weight;
-    ww = ww + w11 * d->weight;
+    float r, ww;
+    if (arith == ORC_ARITH_CONTRACTED) {
+        r = fmaf(w00, a->value, w10 * b->value);
+        r = fmaf(w01, c->value, r);
+        r = fmaf(w11, d->value, r);
+        ww = fmaf(w00, a->weight, w10 * b->weight);
+        ww = fmaf(w01, c->weight, ww);
+        ww = fmaf(w11, d->weight, ww);
+    } else {
+        r = w00 * a->value + w10 * b->value;
+        r = r + w01 * c->value;
+        r = r + w11 * d->value;
+        ww = w00 * a->weight + w10 * b->weight;
+        ww = ww + w01 * c->weight;
+        ww = ww + w11 * d->weight;
+    }
     *value = r;
     *weight = ww;
 }
@@ -429,7 +495,8 @@ static void read_filtered(const void *in, long pitch, float x, float y, float *v
 /* getFoveationAdvisedSampleCount + linearMapping, gen.cu:209-257.
  * atanf here is the C library's; CUDA's atanf may differ in the last place,
  * which can move a pixel across a foveation threshold. */
-static void foveation(uint32_t px, uint32_t py, uint32_t fx, uint32_t fy, float max_ss, float *advised, int *inside)
+static void foveation(int arith, uint32_t px, uint32_t py, uint32_t fx, uint32_t fy, float max_ss, float *advised,
+                      int *inside)
 {
     const float pi_f = 3.14159265358979f;
     const float screen_distance = 60.0f, pixel_cm = 0.02652f;
@@ -437,12 +504,14 @@ static void foveation(uint32_t px, uint32_t py, uint32_t fx, uint32_t fy, float 
     float foveal = max_ss >= 1 ? 5.5f : (float)(5.5 * (double)max_ss);
     float peripheral = 60;
     float ddx = (float)fx - (float)nx, ddy = (float)fy - (float)ny;
-    float dist = sqrtf(ddx * ddx + ddy * ddy) * pixel_cm;
+    /* contracted: the sum of squares and k*x + q are fused */
+    float sq = arith == ORC_ARITH_CONTRACTED ? fmaf(ddx, ddx, ddy * ddy) : ddx * ddx + ddy * ddy;
+    float dist = sqrtf(sq) * pixel_cm;
     float angle = atanf(dist / screen_distance) * 180 / pi_f;
     /* linearMapping<float>(angle, foveal, peripheral, 1, 0) */
     float k = (0.0f - 1.0f) / (peripheral - foveal);
     float q = (peripheral * 1.0f - 0.0f * foveal) / (peripheral - foveal);
-    float lin = k * angle + q;
+    float lin = arith == ORC_ARITH_CONTRACTED ? fmaf(k, angle, q) : k * angle + q;
     float rel = (float)fmin(1.0, (double)lin);
     float adv = max_ss * rel;
     int in = 0;
@@ -479,7 +548,7 @@ void orc_render_advanced(int fractal, int dbl, int arith, void *out, long pitch,
             adv[l] = max_ss;
             inside[l] = 0;
             if ((flags & ORC_FLAG_FOVEATION) && (flags & ORC_FLAG_IS_ZOOMING) && (flags & ORC_FLAG_ZOOMING_IN))
-                foveation(lx[l], ly[l], focus_x, focus_y, max_ss, &adv[l], &inside[l]);
+                foveation(arith, lx[l], ly[l], focus_x, focus_y, max_ss, &adv[l], &inside[l]);
             reusing[l] = 0;
             if (flags & ORC_FLAG_SAMPLE_REUSE) {
                 float ox, oy;
@@ -488,7 +557,7 @@ void orc_render_advanced(int fractal, int dbl, int arith, void *out, long pitch,
                 if (oix < 2 || (uint32_t)oix >= w - 2 || oiy < 2 || (uint32_t)oiy >= h - 2) {
                     reusing[l] = 0;
                 } else {
-                    read_filtered(in, in_pitch, ox, oy, &reused_v[l], &reused_w[l]);
+                    read_filtered(arith, in, in_pitch, ox, oy, &reused_v[l], &reused_w[l]);
                     reusing[l] = !(reused_w[l] < 0.1);
                 }
             }
@@ -535,9 +604,8 @@ void orc_render_advanced(int fractal, int dbl, int arith, void *out, long pitch,
                 float rw = reused_w[l] * 0.75f;
                 res[l].weight_of_new_samples = sc;
                 res[l].weight = rw + sc;
-                float num = reused_v[l] * rw;
                 float add = samples * sc;
-                num = num + add;
+                float num = arith == ORC_ARITH_CONTRACTED ? fmaf(reused_v[l], rw, add) : reused_v[l] * rw + add;
                 res[l].value = num / res[l].weight;
             }
         }

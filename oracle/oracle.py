@@ -16,7 +16,7 @@ ORACLE_LIB = os.path.join(HERE, "_build", "libchaos_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libchaos_ref.so")
 
 MANDELBROT, JULIA = 0, 1
-ARITH_FMA, ARITH_PARITY = 0, 1  # same numbering as CHAOS_ARITH_* in include/chaos_gb300.h
+ARITH_FMA, ARITH_PARITY, ARITH_CONTRACTED = 0, 1, 2  # same numbering as CHAOS_ARITH_* in include/chaos_gb300.h
 
 PIXEL_DTYPE = np.dtype([("value", "<f4"), ("weight", "<f4"), ("is_reused", "u1"), ("pad", "u1", 3),
                         ("weight_of_new_samples", "<f4")])

@@ -6,7 +6,10 @@ cuModuleGetGlobal + memcpy for the __constant__ symbols, cuLaunchKernel with a
 void** parameter array and the 32x32 block shape.  Results are compared with
 the oracle; where the reference's own kernels were built for sm_103a
 (oracle/_ref/ref_<fractal>[_nofma].cubin) they are run the same way, which pins
-the oracle's lock-step restatement to the reference itself."""
+the oracle's lock-step restatement to the reference itself.  The modules in
+cudaKernels_parity match the reference built with --fmad=false, the
+escape-time modules in cudaKernels the reference as nvcc builds it by default
+(contraction on), record for record."""
 import os
 
 import numpy as np
@@ -113,7 +116,7 @@ def test_dropin_main_matches_oracle(drv, cuda, oracle, w, h, max_ss, flags, dbl,
     import chaos_gb300 as cg
     rect = rect_for(M1[:2], M1[2], w, h)
     got = replay_main(drv, cuda, module_path("mandelbrot", parity), w, h, rect, 600, max_ss, flags, dbl)
-    arith = cg.ARITH_PARITY if parity else cg.ARITH_FMA
+    arith = cg.ARITH_PARITY if parity else cg.ARITH_CONTRACTED
     want = oracle.render_main(MANDELBROT, dbl, arith, w, h, rect, 600, max_ss, flags)
     assert not same_pixels(got, want).any()
 
@@ -200,3 +203,94 @@ def test_reference_julia_pins_oracle(drv, cuda, oracle):
     ref = replay_main(drv, cuda, ref_cubin("julia"), w, h, rect, 900, 4.0, 1, True, julia_c=(-0.4, 0.6))
     want = oracle.render_main(JULIA, True, cg.ARITH_PARITY, w, h, rect, 900, 4.0, 1, julia_c=(-0.4, 0.6))
     assert not same_pixels(ref, want).any()
+
+
+CONTRACTED_ADV_FLAGS = [8 | 16 | 32 | 1, 8 | 1, 4 | 8 | 16 | 32 | 1, 4 | 16 | 32 | 1]
+
+
+@pytest.mark.parametrize("w,h,max_ss,flags", MAIN_CASES + [(48, 40, 12.0, 1), (33, 29, 17.0, 1), (257, 131, 4.6, 1)])
+@pytest.mark.parametrize("dbl", [False, True])
+def test_contracted_module_is_the_reference_default_build_main(drv, cuda, oracle, w, h, max_ss, flags, dbl):
+    """cudaKernels/mandelbrot = the reference's module as nvcc builds it by
+    default (ref_mandelbrot.cubin), record for record; the oracle's contracted
+    restatement gives the same records."""
+    import chaos_gb300 as cg
+    rect = rect_for(M1[:2], M1[2], w, h)
+    ref = replay_main(drv, cuda, ref_cubin("mandelbrot", nofma=False), w, h, rect, 600, max_ss, flags, dbl)
+    ours = replay_main(drv, cuda, module_path("mandelbrot", False), w, h, rect, 600, max_ss, flags, dbl)
+    bad = same_pixels(ours, ref)
+    assert not bad.any(), (int(bad.sum()), ours[bad][:3], ref[bad][:3])
+    want = oracle.render_main(MANDELBROT, dbl, cg.ARITH_CONTRACTED, w, h, rect, 600, max_ss, flags)
+    assert not same_pixels(ref, want).any()
+
+
+@pytest.mark.parametrize("flags", CONTRACTED_ADV_FLAGS)
+@pytest.mark.parametrize("dbl", [False, True])
+def test_contracted_module_is_the_reference_default_build_advanced(drv, cuda, oracle, flags, dbl):
+    """Sample reuse, the blend near the zoom centre and foveation as the
+    reference's default build computes them (the same CUDA atanf on both
+    sides, so foveated tiles agree exactly as well)."""
+    import chaos_gb300 as cg
+    w, h, focus = 128, 80, (40, 50)
+    old = rect_for(M1[:2], M1[2], w, h)
+    new = zoom_at(old, focus, w, h)
+    prev = replay_main(drv, cuda, ref_cubin("mandelbrot", nofma=False), w, h, old, 600, 3.0, 1, dbl)
+    ref = replay_advanced(drv, cuda, ref_cubin("mandelbrot", nofma=False), w, h, new, 600, 3.0, flags, old, prev, focus,
+                          dbl)
+    ours = replay_advanced(drv, cuda, module_path("mandelbrot", False), w, h, new, 600, 3.0, flags, old, prev, focus,
+                           dbl)
+    bad = same_pixels(ours, ref)
+    assert not bad.any(), (int(bad.sum()), ours[bad][:3], ref[bad][:3])
+    want = oracle.render_advanced(MANDELBROT, dbl, cg.ARITH_CONTRACTED, w, h, new, 600, 3.0, flags, old, prev, focus)
+    assert same_pixels(ref, want).mean() < (0.02 if flags & 4 else 1e-9)  # CUDA vs C-library atanf
+
+
+@pytest.mark.parametrize("dbl", [False, True])
+def test_contracted_julia_module_is_the_reference_default_build(drv, cuda, dbl):
+    w, h = 90, 60
+    rect = rect_for((0.0, 0.0), 2.0, w, h)
+    ref = replay_main(drv, cuda, ref_cubin("julia", nofma=False), w, h, rect, 900, 4.0, 1, dbl, julia_c=(-0.4, 0.6))
+    ours = replay_main(drv, cuda, module_path("julia", False), w, h, rect, 900, 4.0, 1, dbl, julia_c=(-0.4, 0.6))
+    assert not same_pixels(ours, ref).any()
+
+
+def test_contracted_library_call_matches_the_default_build(drv, cuda):
+    """The C ABI's render_main with CHAOS_ARITH_CONTRACTED = the reference's
+    default build (binary64, adaptive super-sampling)."""
+    import chaos_gb300 as cg
+    from tests.gpu_util import pitched, read_pixels
+    w, h = 100, 37
+    rect = rect_for(M1[:2], M1[2], w, h)
+    ref = replay_main(drv, cuda, ref_cubin("mandelbrot", nofma=False), w, h, rect, 600, 4.6, 1, True)
+    buf, pitch = pitched(cuda, w, h)
+    cg.Module("mandelbrot").render_main(buf.data_ptr(), pitch, w, h, rect, 600, 4.6, 1, double=True,
+                                        arith=cg.ARITH_CONTRACTED)
+    cuda.cuda.synchronize()
+    assert not same_pixels(read_pixels(buf, w), ref).any()
+
+
+def replay_under_sampled(drv, cuda, path, w, h, rect, max_iter, level):
+    import ctypes as C
+    mod = drv.load(path)
+    try:
+        fn = drv.function(mod, "fractalRenderUnderSampled")
+        buf, pitch = pitched(cuda, w, h)
+        params = [C.c_uint64(buf.data_ptr()), C.c_int64(pitch), C.c_uint32(w), C.c_uint32(h)] + \
+                 [C.c_float(v) for v in rect] + [C.c_uint32(max_iter), C.c_uint32(level)]
+        grid, block = java_grid((w + level - 1) // level, (h + level - 1) // level)
+        drv.launch(fn, grid, block, params)
+        return read_pixels(buf, w)
+    finally:
+        drv.unload(mod)
+
+
+@pytest.mark.parametrize("parity", [True, False])
+def test_under_sampled_is_the_reference_build(drv, cuda, parity):
+    """fractalRenderUnderSampled of each drop-in module against the reference
+    built the same way (--fmad=false / default contraction)."""
+    w, h, level = 150, 97, 3
+    rect = tuple(float(v) for v in np.float32(rect_for(M1[:2], M1[2], w, h)))
+    ref = replay_under_sampled(drv, cuda, ref_cubin("mandelbrot", nofma=parity), w, h, rect, 700, level)
+    ours = replay_under_sampled(drv, cuda, module_path("mandelbrot", parity), w, h, rect, 700, level)
+    bad = same_pixels(ours, ref)
+    assert not bad.any(), (int(bad.sum()), ours[bad][:3], ref[bad][:3])
