@@ -36,7 +36,7 @@ static_assert(sizeof(PixelInfo) == 16, "pixel_info_t is 16 bytes");
 // every product and sum is rounded except where nvcc fuses a product that has
 // no other use into the add after it -- the escape step's y' = fma(2x, y, cy),
 // the sample's x coordinate fma(px + dx, psx, lbx), and in the reuse path
-// oy = fma(-ry, h, h), the filter's chain of products and the blend.  The
+// the warp to the old frame, the filter's chain of products and the blend.  The
 // squares x*x and y*y feed both the test and x' and stay rounded.
 enum Arith { ARITH_PARITY = 0, ARITH_FMA = 1, ARITH_CONTRACTED = 2 };
 enum FractalKind {
@@ -561,16 +561,22 @@ __device__ __forceinline__ void render_main_tile(const SampleGeometry<R> &g, voi
 // Sample reuse and foveation (fractalRenderAdvanced, gen.cu:194-368)
 // ---------------------------------------------------------------------------
 
-// getWarpingOriginOfSampleReuse, gen.cu:194-203 (contracted: the y flip is
-// one fused multiply-add)
+// getWarpingOriginOfSampleReuse, gen.cu:194-203 (contracted: the pixel's
+// position in the plane and the y flip are fused multiply-adds)
 template <class R, int A = ARITH_PARITY>
 __device__ __forceinline__ void warping_origin(UInt2 p, UInt2 grid, const Rect<R> &cur, const Rect<R> &old, float &ox,
                                                float &oy)
 {
     using O = Op<R>;
     uint32_t qy = grid.y - p.y;
-    R ppx = O::add(O::mul(O::div((R)p.x, (R)grid.x), O::sub(cur.rtx, cur.lbx)), cur.lbx);
-    R ppy = O::add(O::mul(O::div((R)qy, (R)grid.y), O::sub(cur.rty, cur.lby)), cur.lby);
+    R ppx, ppy;
+    if (A == ARITH_CONTRACTED) {
+        ppx = O::fma(O::div((R)p.x, (R)grid.x), O::sub(cur.rtx, cur.lbx), cur.lbx);
+        ppy = O::fma(O::div((R)qy, (R)grid.y), O::sub(cur.rty, cur.lby), cur.lby);
+    } else {
+        ppx = O::add(O::mul(O::div((R)p.x, (R)grid.x), O::sub(cur.rtx, cur.lbx)), cur.lbx);
+        ppy = O::add(O::mul(O::div((R)qy, (R)grid.y), O::sub(cur.rty, cur.lby)), cur.lby);
+    }
     R rx = O::div(O::sub(ppx, old.lbx), O::sub(old.rtx, old.lbx));
     R ry = O::div(O::sub(ppy, old.lby), O::sub(old.rty, old.lby));
     ox = __fmul_rn((float)rx, (float)grid.x);

@@ -442,16 +442,19 @@ static void warping_origin(const orc_view *v, const double old_rect[4], uint32_t
     float rx, ry;
     if (v->dbl) {
         double sx = v->rd[2] - v->rd[0], sy = v->rd[3] - v->rd[1];
-        double ppx = (double)px / (double)v->w * sx + v->rd[0];
-        double ppy = (double)qy / (double)v->h * sy + v->rd[1];
+        /* contracted: the position in the plane is one fused multiply-add */
+        int fz = v->arith == ORC_ARITH_CONTRACTED;
+        double ppx = fz ? fma((double)px / (double)v->w, sx, v->rd[0]) : (double)px / (double)v->w * sx + v->rd[0];
+        double ppy = fz ? fma((double)qy / (double)v->h, sy, v->rd[1]) : (double)qy / (double)v->h * sy + v->rd[1];
         double osx = old_rect[2] - old_rect[0], osy = old_rect[3] - old_rect[1];
         rx = (float)((ppx - old_rect[0]) / osx);
         ry = (float)((ppy - old_rect[1]) / osy);
     } else {
         float o0 = (float)old_rect[0], o1 = (float)old_rect[1], o2 = (float)old_rect[2], o3 = (float)old_rect[3];
         float sx = v->rf[2] - v->rf[0], sy = v->rf[3] - v->rf[1];
-        float ppx = (float)px / (float)v->w * sx + v->rf[0];
-        float ppy = (float)qy / (float)v->h * sy + v->rf[1];
+        int fz = v->arith == ORC_ARITH_CONTRACTED;
+        float ppx = fz ? fmaf((float)px / (float)v->w, sx, v->rf[0]) : (float)px / (float)v->w * sx + v->rf[0];
+        float ppy = fz ? fmaf((float)qy / (float)v->h, sy, v->rf[1]) : (float)qy / (float)v->h * sy + v->rf[1];
         rx = (ppx - o0) / (o2 - o0);
         ry = (ppy - o1) / (o3 - o1);
     }

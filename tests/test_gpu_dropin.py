@@ -294,3 +294,59 @@ def test_under_sampled_is_the_reference_build(drv, cuda, parity):
     ours = replay_under_sampled(drv, cuda, module_path("mandelbrot", parity), w, h, rect, 700, level)
     bad = same_pixels(ours, ref)
     assert not bad.any(), (int(bad.sum()), ours[bad][:3], ref[bad][:3])
+
+
+def _random_view(rng, dbl):
+    """A seeded view near the set's boundary: centre from a short list of
+    boundary regions, plane height log-uniform (down to 1e-12 in binary64,
+    1e-5 in binary32), frame 8..96 pixels a side, maxIter 50..3000, maxSS
+    1..20, adaptive sampling on or off."""
+    centres = [(-0.748, 0.1), (-0.74364388703715, 0.13182590420531), (0.3004395381261789, -0.5705143370804123),
+               (-1.25066, 0.02012), (-0.1011, 0.9563), (0.285, 0.01)]
+    c = centres[rng.integers(len(centres))]
+    zoom = 10 ** rng.uniform(-12 if dbl else -5, -1)
+    w, h = int(rng.integers(8, 97)), int(rng.integers(8, 97))
+    return (c, zoom, w, h, int(rng.integers(50, 3001)), float(rng.uniform(1.0, 20.0)), int(rng.integers(0, 2)))
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_random_main_views_against_both_reference_builds(drv, cuda, seed):
+    """Seeded random views: cudaKernels = the reference's default build and
+    cudaKernels_parity = its --fmad=false build, record for record."""
+    rng = np.random.default_rng(1000 + seed)
+    for dbl in (False, True):
+        c, zoom, w, h, mi, mss, flags = _random_view(rng, dbl)
+        rect = rect_for(c, zoom, w, h)
+        if not dbl:
+            rect = tuple(float(v) for v in np.float32(rect))
+        for parity in (False, True):
+            ref = replay_main(drv, cuda, ref_cubin("mandelbrot", nofma=parity), w, h, rect, mi, mss, flags, dbl)
+            ours = replay_main(drv, cuda, module_path("mandelbrot", parity), w, h, rect, mi, mss, flags, dbl)
+            bad = same_pixels(ours, ref)
+            assert not bad.any(), (seed, dbl, parity, (c, zoom, w, h, mi, mss, flags), int(bad.sum()))
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_random_advanced_frames_against_both_reference_builds(drv, cuda, seed):
+    """Seeded zoom steps with random flags (reuse, zooming in or out,
+    foveation, adaptive) and focus, previous frame from the same build."""
+    rng = np.random.default_rng(2000 + seed)
+    for dbl in (False, True):
+        c, zoom, w, h, mi, mss, _ = _random_view(rng, dbl)
+        w, h = max(w, 24), max(h, 16)
+        focus = (int(rng.integers(0, w)), int(rng.integers(0, h)))
+        old = rect_for(c, zoom, w, h)
+        into = bool(rng.integers(0, 2))
+        new = zoom_at(old, focus, w, h, into=into)
+        flags = 8 | 16 | (32 if into else 0) | int(rng.integers(0, 2)) | (4 if rng.integers(0, 2) else 0)
+        if not dbl:
+            old = tuple(float(v) for v in np.float32(old))
+            new = tuple(float(v) for v in np.float32(new))
+        for parity in (False, True):
+            prev = replay_main(drv, cuda, ref_cubin("mandelbrot", nofma=parity), w, h, old, mi, mss, 1, dbl)
+            ref = replay_advanced(drv, cuda, ref_cubin("mandelbrot", nofma=parity), w, h, new, mi, mss, flags, old, prev,
+                                  focus, dbl)
+            ours = replay_advanced(drv, cuda, module_path("mandelbrot", parity), w, h, new, mi, mss, flags, old, prev,
+                                   focus, dbl)
+            bad = same_pixels(ours, ref)
+            assert not bad.any(), (seed, dbl, parity, flags, (c, zoom, w, h, mi, mss), int(bad.sum()))
