@@ -350,3 +350,24 @@ def test_random_advanced_frames_against_both_reference_builds(drv, cuda, seed):
                                    focus, dbl)
             bad = same_pixels(ours, ref)
             assert not bad.any(), (seed, dbl, parity, flags, (c, zoom, w, h, mi, mss), int(bad.sum()))
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_julia_views_against_both_reference_builds(drv, cuda, seed):
+    """Julia modules on seeded views and constants, both builds."""
+    rng = np.random.default_rng(3000 + seed)
+    consts = [(-0.4, 0.6), (0.285, 0.01), (-0.8, 0.156), (-0.7269, 0.1889), (0.355, 0.355)]
+    for dbl in (False, True):
+        jc = consts[rng.integers(len(consts))]
+        c = (float(rng.uniform(-0.8, 0.8)), float(rng.uniform(-0.8, 0.8)))
+        zoom = 10 ** rng.uniform(-9 if dbl else -4, 0.3)
+        w, h = int(rng.integers(8, 97)), int(rng.integers(8, 97))
+        mi, mss, flags = int(rng.integers(50, 2001)), float(rng.uniform(1.0, 12.0)), int(rng.integers(0, 2))
+        rect = rect_for(c, zoom, w, h)
+        if not dbl:
+            rect = tuple(float(v) for v in np.float32(rect))
+        for parity in (False, True):
+            ref = replay_main(drv, cuda, ref_cubin("julia", nofma=parity), w, h, rect, mi, mss, flags, dbl, julia_c=jc)
+            ours = replay_main(drv, cuda, module_path("julia", parity), w, h, rect, mi, mss, flags, dbl, julia_c=jc)
+            bad = same_pixels(ours, ref)
+            assert not bad.any(), (seed, dbl, parity, jc, (c, zoom, w, h, mi, mss, flags), int(bad.sum()))
