@@ -153,6 +153,11 @@ def test_argument_validation_without_gpu(native):
     with pytest.raises(cg.ChaosError) as e:
         cg.render_frame(d, cg.FrameOut())
     assert e.value.code == 8
+    # the contracted arithmetic is for the reference-mode calls only
+    d.tier, d.arith = cg.TIER_F32, cg.ARITH_CONTRACTED
+    with pytest.raises(cg.ChaosError) as e:
+        cg.render_frame(d, cg.FrameOut())
+    assert e.value.code == 8 and "ARITH" in e.value.message
 
 
 def test_renderer_state_machine_without_gpu(native):
