@@ -1019,7 +1019,10 @@ def run_compose(args):
             "data": "synthetic: seeded values, the default 1536-entry palette",
             "config": {"workload": f"compose {w}x{h} pixel_info_t -> RGBA8", "l2": "flushed between steps"},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
-                         "traffic": None, "peak_source": src, "bytes_per_pixel": 20},
+                         # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the same
+                         # 7680x4320 compose, from the committed ncu summary (k_compose_8k)
+                         "traffic": 646.9e6, "traffic_unit": "bytes per launch (ncu capture)",
+                         "peak_source": src, "bytes_per_pixel": 20},
             "gpu_launches": args.steps, "clocks": clk}
     print(json.dumps(line), flush=True)
 
@@ -1084,7 +1087,10 @@ def run_reuse(args):
             "config": {"workload": f"fractalRenderAdvanced {w}x{h}, previous frame on the same rectangle, "
                                    "reuse only", "l2": "flushed between steps", "reused_fraction": reused},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
-                         "traffic": None, "peak_source": src, "bytes_per_pixel": 32},
+                         # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the same
+                         # 7680x4320 reuse frame, from the committed ncu summary (k_advanced_reuse_8k)
+                         "traffic": 1022.0e6, "traffic_unit": "bytes per launch (ncu capture)",
+                         "peak_source": src, "bytes_per_pixel": 32},
             "gpu_launches": args.steps, "clocks": clk}
     print(json.dumps(line), flush=True)
 
