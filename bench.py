@@ -337,6 +337,8 @@ def run_ours(args):
     achieved_ops = rate * ops_per_iter
     roof = {"bound": "fp64-pipe", "achieved": achieved_ops / 1e12, "peak": peak / 2 / 1e12, "unit": "Top/s",
             "frac": achieved_ops / (peak / 2), "traffic": None,
+            "traffic_note": "FP64-pipe bound, state in registers: the ncu capture of the central 480x270 crop "
+                            "read 461 KB and wrote 0 B of DRAM per launch",
             "peak_source": "measured in this run: chaos_measure_fma_peak (full-occupancy DFMA chains)",
             "ops_per_iteration": ops_per_iter, "fp64_pipe_ops_per_iteration": pipe_ops_per_iter,
             "fp64_pipe_frac": rate * pipe_ops_per_iter / (peak / 2),
