@@ -309,7 +309,7 @@ def _random_view(rng, dbl):
     return (c, zoom, w, h, int(rng.integers(50, 3001)), float(rng.uniform(1.0, 20.0)), int(rng.integers(0, 2)))
 
 
-@pytest.mark.parametrize("seed", range(16))
+@pytest.mark.parametrize("seed", range(40))
 def test_random_main_views_against_both_reference_builds(drv, cuda, seed):
     """Seeded random views: cudaKernels = the reference's default build and
     cudaKernels_parity = its --fmad=false build, record for record."""
@@ -326,7 +326,7 @@ def test_random_main_views_against_both_reference_builds(drv, cuda, seed):
             assert not bad.any(), (seed, dbl, parity, (c, zoom, w, h, mi, mss, flags), int(bad.sum()))
 
 
-@pytest.mark.parametrize("seed", range(16))
+@pytest.mark.parametrize("seed", range(40))
 def test_random_advanced_frames_against_both_reference_builds(drv, cuda, seed):
     """Seeded zoom steps with random flags (reuse, zooming in or out,
     foveation, adaptive) and focus, previous frame from the same build."""
@@ -352,7 +352,7 @@ def test_random_advanced_frames_against_both_reference_builds(drv, cuda, seed):
             assert not bad.any(), (seed, dbl, parity, flags, (c, zoom, w, h, mi, mss), int(bad.sum()))
 
 
-@pytest.mark.parametrize("seed", range(8))
+@pytest.mark.parametrize("seed", range(20))
 def test_random_julia_views_against_both_reference_builds(drv, cuda, seed):
     """Julia modules on seeded views and constants, both builds."""
     rng = np.random.default_rng(3000 + seed)
