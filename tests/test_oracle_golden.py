@@ -160,3 +160,30 @@ def test_rounded_batch_tier_is_the_reference_loop(oracle, reference):
     assert np.array_equal(o["counts"], want)
     assert o["total"] == total
     assert 0 < (want == mi).sum() < len(want)  # interior and exterior both present
+
+
+def test_contracted_oracle_matches_the_reference_default_build(oracle):
+    """The oracle's ARITH_CONTRACTED restatement against pixel records the
+    reference's own default (contraction-on) sm_103a build produced
+    (tests/golden/contracted_golden.npz, tests/golden/make_contracted_golden.py):
+    main frames at maxSS 1..17 and zoom steps with sample reuse, every record
+    bit for bit."""
+    import json
+    import os
+    from oracle.oracle import ARITH_CONTRACTED, MANDELBROT, PIXEL_DTYPE
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "contracted_golden.npz")
+    g = np.load(path)
+    meta = json.loads(g["meta"].tobytes().decode())
+    for m in meta["main"]:
+        got = oracle.render_main(MANDELBROT, m["dbl"], ARITH_CONTRACTED, m["w"], m["h"], tuple(m["rect"]),
+                                 m["max_iter"], m["max_ss"], m["flags"])
+        want = g[m["name"]]
+        bad = (got.view(np.uint8).reshape(m["h"], m["w"], 16) != want).any(axis=2)
+        assert not bad.any(), (m["name"], int(bad.sum()))
+    for m in meta["advanced"]:
+        prev = np.ascontiguousarray(g[m["name"] + "_prev"]).view(PIXEL_DTYPE).reshape(m["h"], m["w"])
+        got = oracle.render_advanced(MANDELBROT, m["dbl"], ARITH_CONTRACTED, m["w"], m["h"], tuple(m["new"]),
+                                     m["max_iter"], m["max_ss"], m["flags"], tuple(m["old"]), prev, tuple(m["focus"]))
+        want = g[m["name"]]
+        bad = (got.view(np.uint8).reshape(m["h"], m["w"], 16) != want).any(axis=2)
+        assert not bad.any(), (m["name"], int(bad.sum()))
