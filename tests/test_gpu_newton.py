@@ -95,12 +95,16 @@ def _replay(drv, cuda, path, kind, w, h, rect, dbl, params):
 
 @pytest.mark.parametrize("kind", [2, 3, 4])
 @pytest.mark.parametrize("dbl", [False, True])
-def test_dropin_newton_matches_reference_and_oracle(drv, cuda, oracle, kind, dbl):
+@pytest.mark.parametrize("parity_dir", [True, False])
+def test_dropin_newton_matches_reference_and_oracle(drv, cuda, oracle, kind, dbl, parity_dir):
+    """The Newton modules of both module directories are rounded operation by
+    operation: the reference built with --fmad=false, bit for bit."""
     import chaos_gb300 as cg
     w, h = 100, 60
     rect = rect_for((0.1, -0.05), 3.0, w, h)
     params = OTHER if kind != 2 else DEFAULT
-    ours = _replay(drv, cuda, os.path.join(cg.DROPIN_PARITY_DIR, NAMES[kind] + ".ptx"), kind, w, h, rect, dbl, params)
+    directory = cg.DROPIN_PARITY_DIR if parity_dir else cg.DROPIN_DIR
+    ours = _replay(drv, cuda, os.path.join(directory, NAMES[kind] + ".ptx"), kind, w, h, rect, dbl, params)
     oracle.set_newton(*params)
     want = oracle.render_main(kind, dbl, 1, w, h, rect, 200, 3.0, 1)
     oracle.set_newton()
