@@ -445,11 +445,16 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
     }
 }
 
+// K = 64 steps (a linear block counts as one) per round between the warp's
+// refill checks: on the C3 frames 16, 32, 64, 128 and 256 gave 1508, 1582,
+// 1635, 1661 and 1688 Gpixel-iter/s, but a long round also keeps a lane that
+// escaped early idle until its warp's round ends, which costs on views whose
+// escape counts vary (batch viewports); 64 gained there too (676 -> 687).
 template <class D, bool S> static cudaError_t launch_perturb(const PerturbArgs<D> &a, int sms, cudaStream_t s)
 {
     static const int occ = [] {
         int n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_perturb<D, 16, S>, 256, 0) != cudaSuccess || n < 1)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_perturb<D, 64, S>, 256, 0) != cudaSuccess || n < 1)
             n = 1;
         return n;
     }();
@@ -458,7 +463,7 @@ template <class D, bool S> static cudaError_t launch_perturb(const PerturbArgs<D
     unsigned long long cap = (unsigned long long)occ * (unsigned long long)sms;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    k_perturb<D, 16, S><<<(unsigned)blocks, 256, 0, s>>>(a);
+    k_perturb<D, 64, S><<<(unsigned)blocks, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
