@@ -111,7 +111,7 @@ def deep_zoom_centre():
     """The perturbation deep-zoom centre (1920x1080, spans 1e-60 and 1e-200,
     maxIter 100000): a seeded Misiurewicz point as 1024-bit "[-]I.hex" strings,
     with its preperiod and period (data/deep_centres.json, written by
-    make_deep_centres.py)."""
+    tests/golden/make_deep_centres.py)."""
     import json
     import os
     with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "deep_centres.json")) as f:

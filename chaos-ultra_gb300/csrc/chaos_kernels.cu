@@ -14,6 +14,7 @@
 //   k_under_sampled       fractalRenderUnderSampled (gen.cu:478-503)
 #include <cstdio>
 
+#include "chaos_frame.cuh"
 #include "chaos_kernels.cuh"
 #include "chaos_refmode.cuh"
 
@@ -25,16 +26,6 @@ constexpr uint32_t PALETTE_SMEM = 4096;
 // Independent-sample frames with per-lane refill
 // ---------------------------------------------------------------------------
 
-template <class R> __device__ __forceinline__ R unit_interval(uint64_t h);
-template <> __device__ __forceinline__ float unit_interval<float>(uint64_t h)
-{
-    return (float)(uint32_t)(h >> 40) * 0x1p-24f;
-}
-template <> __device__ __forceinline__ double unit_interval<double>(uint64_t h)
-{
-    return (double)(h >> 11) * 0x1p-53;
-}
-
 template <class R>
 __device__ __forceinline__ void frame_point(const FrameArgs<R> &a, uint32_t w_magic, uint32_t pix, uint32_t s, R &cx,
                                             R &cy)
@@ -44,53 +35,13 @@ __device__ __forceinline__ void frame_point(const FrameArgs<R> &a, uint32_t w_ma
     divmod_magic(pix, a.w, w_magic, py, px);
     R ox = R(0.5), oy = R(0.5);
     if (a.mode == SAMPLES_JITTER) {
-        ox = unit_interval<R>(sample_hash(a.seed, pix, s, 0));
-        oy = unit_interval<R>(sample_hash(a.seed, pix, s, 1));
+        ox = unit_interval_t<R>(sample_hash(a.seed, pix, s, 0));
+        oy = unit_interval_t<R>(sample_hash(a.seed, pix, s, 1));
     }
     R dxp = O::sub(O::add((R)px, ox), a.half_w);
     R dyp = O::sub(O::add((R)py, oy), a.half_h);
     cx = O::fma(dxp, a.ps, a.center_x);
     cy = O::fma(-dyp, a.ps, a.center_y);
-}
-
-// n + 1 - log2(log2|z_n|) for an escaped sample, max_iter for an interior one.
-__device__ __forceinline__ float smooth_value(uint32_t i, float r2, uint32_t max_iter)
-{
-    if (i >= max_iter) return (float)max_iter;
-    if (!(r2 < 3.0e38f)) return (float)i;
-    float l = __fmul_rn(0.5f, log2f(r2));
-    return __fsub_rn((float)(i + 1u), log2f(l));
-}
-
-// Palette sampled with linear interpolation at t = nu mod len.
-__device__ __forceinline__ void palette_lerp(const uint32_t *pal, uint32_t len, float nu, float ch[4])
-{
-    float fl = (float)len;
-    float t = fmodf(nu, fl);
-    if (t < 0.f) t = __fadd_rn(t, fl);
-    uint32_t i0 = (uint32_t)t;
-    if (i0 >= len) i0 = len - 1u;
-    float f = __fsub_rn(t, (float)i0);
-    uint32_t i1 = i0 + 1u == len ? 0u : i0 + 1u;
-    uint32_t c0 = pal[i0], c1 = pal[i1];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        float a0 = (float)((c0 >> (8 * k)) & 255u), a1 = (float)((c1 >> (8 * k)) & 255u);
-        ch[k] = __fmaf_rn(__fsub_rn(a1, a0), f, a0);
-    }
-}
-
-__device__ __forceinline__ uint32_t pack_mean_rgba(const float acc[4], uint32_t spp)
-{
-    uint32_t out = 0;
-    float n = (float)spp;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        float v = __fadd_rn(__fdiv_rn(acc[k], n), 0.5f);
-        v = v < 255.f ? v : 255.f;
-        out |= ((uint32_t)v & 255u) << (8 * k);
-    }
-    return out;
 }
 
 template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIST_THREADS) k_frame(FrameArgs<R> a)
@@ -256,7 +207,7 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
         }
         if (done) {
             const bool escaped = i < a.max_iter;
-            const float nu = (a.smooth || a.pixels || a.rgba) ? smooth_value(i, (float)r2, a.max_iter) : 0.f;
+            const float nu = (a.smooth || a.pixels || a.rgba) ? frame_smooth(i, (float)r2, a.max_iter) : 0.f;
             const size_t sidx = (size_t)pix * a.spp + s;
             if (a.counts) a.counts[sidx] = i;
             if (a.smooth) a.smooth[sidx] = nu;
@@ -266,7 +217,7 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
             if (a.rgba) {
                 float ch[4];
                 if (escaped) {
-                    palette_lerp(pal, a.palette_len, nu, ch);
+                    frame_palette_lerp(pal, a.palette_len, nu, ch);
                 } else {
 #pragma unroll
                     for (int k = 0; k < 4; k++) ch[k] = (float)((a.interior_rgba >> (8 * k)) & 255u);
@@ -281,7 +232,7 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
                 if (a.pixels)
                     store_pixel(pixel_ptr(a.pixels, a.pixels_pitch, px, py),
                                 make_pixel(__fdiv_rn(acc_v, (float)a.spp), (float)a.spp));
-                if (a.rgba) a.rgba[pix] = pack_mean_rgba(acc, a.spp);
+                if (a.rgba) a.rgba[pix] = frame_pack_rgba(acc, a.spp);
                 need = true;
             } else {
                 begin = true;

@@ -2,11 +2,11 @@
 // memory that allocates no device memory at any point.
 //
 // Who needs it: callers that may not call cudaMalloc -- a host whose GPU
-// memory is budgeted up front and must not grow while it serves frames, code
-// running between a stream-capture begin and end, or a thin JNI/Panama binding
-// that owns no CUDA allocator.  chaos_render_frame_host keeps its device
-// buffers per thread and grows them with cudaMalloc; this entry point puts the
-// same buffers in one fixed array that is part of the library image instead.
+// memory is budgeted up front and must not grow while it serves frames, or a
+// thin JNI/Panama binding that owns no CUDA allocator.  chaos_render_frame_host
+// keeps its device buffers per thread and grows them with cudaMalloc; this
+// entry point puts the same buffers in one fixed array that is part of the
+// library image instead.
 //
 // The array g_noalloc_scratch (64 MiB, 256-byte aligned) is a file-scope
 // __device__ variable: every GPU that loads the library holds it until the
@@ -18,8 +18,11 @@
 // In host code the name g_noalloc_scratch is only a host-side stand-in, not a
 // device address.  The first call on each device (with that device current)
 // asks the runtime for the real address with cudaGetSymbolAddress and keeps
-// it; that first call should come before any stream capture.  All calls share
-// the one array and it keeps the last call's contents: each call clears the
+// it; under lazy module loading (the CUDA default) that is also when the
+// device's copy of the array is reserved, so make one call during set-up,
+// before the GPU's memory is handed out and before any stream capture.  A
+// failed look-up is not kept: the next call tries again.  All calls share the
+// one array and it keeps the last call's contents: each call clears the
 // counter and total itself, and calls whose GPU work overlaps (different
 // streams or threads at once) race on the array.
 #include <cmath>
@@ -52,12 +55,31 @@ constexpr uint64_t kMaxPixels = (kScratchBytes - kImageOffset) / sizeof(uint32_t
 
 constexpr int kMaxDevices = 64;
 struct NoAllocDevice {
-    std::once_flag once;
-    cudaError_t err = cudaSuccess;
-    unsigned char *base = nullptr;  // device address of g_noalloc_scratch
+    std::mutex mu;
+    unsigned char *base = nullptr;  // device address of g_noalloc_scratch, once looked up
     int sms = 0;
 };
 NoAllocDevice g_noalloc[kMaxDevices];
+
+// The device address of this device's copy of the array (with `dev`
+// current).  Only a successful look-up is kept.
+cudaError_t scratch_of(int dev, unsigned char **base, int *sms)
+{
+    NoAllocDevice &nd = g_noalloc[dev];
+    std::lock_guard<std::mutex> g(nd.mu);
+    if (!nd.base) {
+        unsigned char *p = nullptr;
+        int n = 0;
+        cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        nd.sms = n;
+        nd.base = p;
+    }
+    *base = nd.base;
+    *sms = nd.sms;
+    return cudaSuccess;
+}
 
 template <class R>
 cudaError_t launch(const chaos_frame_desc *d, unsigned char *base, uint32_t palette_len, uint32_t interior_rgba,
@@ -123,29 +145,30 @@ int chaos_render_frame_host_noalloc(const chaos_frame_desc *desc, const uint32_t
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return api_fail(CHAOS_ERR_UNSUPPORTED, "device %d out of range", dev);
-    NoAllocDevice &nd = g_noalloc[dev];
-    std::call_once(nd.once, [&]() {
-        // with `dev` current: the device address of this device's copy of the array
-        nd.err = cudaGetSymbolAddress((void **)&nd.base, g_noalloc_scratch);
-        if (nd.err == cudaSuccess) nd.err = cudaDeviceGetAttribute(&nd.sms, cudaDevAttrMultiProcessorCount, dev);
-    });
-    if (nd.err != cudaSuccess)
-        return api_fail(CHAOS_ERR_CUDA, "no-alloc scratch set-up: %s", cudaGetErrorString(nd.err));
+    unsigned char *base = nullptr;
+    int sms = 0;
+    e = scratch_of(dev, &base, &sms);
+    if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "no-alloc scratch set-up: %s", cudaGetErrorString(e));
 
     cudaStream_t s = (cudaStream_t)stream;
-    e = cudaMemsetAsync(nd.base, 0, kHeaderBytes, s);  // work counter and total start at zero
+    e = cudaMemsetAsync(base, 0, kHeaderBytes, s);  // work counter and total start at zero
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(nd.base + kHeaderBytes, palette, palette_len * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                            s);
+        e = cudaMemcpyAsync(base + kHeaderBytes, palette, palette_len * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
-        e = desc->tier == CHAOS_TIER_F64 ? launch<double>(desc, nd.base, palette_len, interior_rgba, nd.sms, s)
-                                         : launch<float>(desc, nd.base, palette_len, interior_rgba, nd.sms, s);
+        e = desc->tier == CHAOS_TIER_F64 ? launch<double>(desc, base, palette_len, interior_rgba, sms, s)
+                                         : launch<float>(desc, base, palette_len, interior_rgba, sms, s);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(rgba_host, nd.base + kImageOffset, pixels * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        e = cudaMemcpyAsync(rgba_host, base + kImageOffset, pixels * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
     unsigned long long total = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&total, nd.base + 8, sizeof total, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&total, base + 8, sizeof total, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "no-alloc frame: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+        // copies queued before the failure may still target rgba_host and the
+        // local total: let the stream finish before returning (its own status
+        // is already the error reported)
+        cudaStreamSynchronize(s);
+        return api_fail(CHAOS_ERR_CUDA, "no-alloc frame: %s", cudaGetErrorString(e));
+    }
     if (total_host) *total_host = total;
     return CHAOS_OK;
 }

@@ -8,8 +8,8 @@
  *      the Java host resolves by name, with the reference's parameter layout and
  *      __constant__ symbols, so FractalRenderingModule loads them unchanged.
  *   2. This library: plain C functions (pointers, sizes, a cudaStream_t passed as
- *      void*), int status returns, no exceptions and no device traps.  A JNI or
- *      Panama shim binds them.
+ *      void*), int status returns, no exceptions and no device traps, for a
+ *      thin JNI or Panama binding on the Java side.
  *
  * Reference paths are relative to the chaos-ultra root; J/ stands for
  * src/main/java/cz/cuni/mff/cgg/teichmaa/chaosultra/ and gen.cu for
@@ -455,16 +455,19 @@ int chaos_render_frame_perturb(const chaos_frame_desc *desc, const chaos_orbit *
                                void *stream);
 
 /* chaos_render_frame_host for callers that must not allocate GPU memory (a
- * host whose GPU memory is fixed before it starts serving frames, code between
- * a stream-capture begin and end, a JNI/Panama binding without a CUDA
- * allocator).  No counterpart in the reference.  The device-side image,
- * palette, work counter and total live in one 64 MiB array that is part of the
- * library (every GPU that loads it holds the array until exit): frames of at
- * most 16,773,056 pixels (3840x2160 fits), palettes of at most 4096 entries,
- * tiers CHAOS_TIER_F32/F64; larger requests fail with
- * CHAOS_ERR_INVALID_ARGUMENT.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) and should come before any stream
- * capture.  All calls share the array: calls whose GPU work overlaps race. */
+ * host whose GPU memory is fixed before it starts serving frames, a JNI/Panama
+ * binding without a CUDA allocator).  No counterpart in the reference.  The
+ * device-side image, palette, work counter and total live in one 64 MiB array
+ * that is part of the library (every GPU that loads it holds the array until
+ * exit): frames of at most 16,773,056 pixels (3840x2160 fits), palettes of at
+ * most 4096 entries, tiers CHAOS_TIER_F32/F64; larger requests fail with
+ * CHAOS_ERR_INVALID_ARGUMENT.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); under lazy module loading
+ * (the CUDA default) the array is reserved on that device at the same moment,
+ * so make one call during set-up, before the GPU's memory is handed out and
+ * before any stream capture.  A failed look-up is retried by the next call.
+ * The call synchronises the stream before it returns.  All calls share the
+ * array: calls whose GPU work overlaps race. */
 int chaos_render_frame_host_noalloc(const chaos_frame_desc *desc, const uint32_t *palette, uint32_t palette_len,
                                     uint32_t interior_rgba, uint32_t *rgba_host, unsigned long long *total_host,
                                     void *stream);

@@ -11,6 +11,7 @@ import shutil
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT_DIR = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 
@@ -67,13 +68,19 @@ def build_oracle():
     return out
 
 
+def reference_root():
+    """Where the reference checkout is read from: $REFERENCE_ROOT, else a
+    chaos-ultra checkout named `reference` beside this repository."""
+    return os.environ.get("REFERENCE_ROOT") or os.path.join(os.path.dirname(ROOT_DIR), "reference")
+
+
 def build_reference():
     """Run oracle/build_ref.sh when the reference sources are reachable.
 
     Returns the path of oracle/_ref/libchaos_ref.so, or None.  The cubins are
     only rebuilt where nvcc exists; the host library is rebuilt when it is
     missing or built for another CPU architecture."""
-    ref_root = os.environ.get("REFERENCE_ROOT", "/root/reference")
+    ref_root = reference_root()
     have_src = os.path.isdir(os.path.join(ref_root, "src", "main", "cuda")) or os.path.exists(
         os.path.join(REF_OUT, "src", "fractalRendererGeneric.cu"))
     if not have_src:
@@ -92,6 +99,7 @@ def build_reference():
             env["NVCC"] = "/usr/local/cuda/bin/nvcc"
         if not need_cubin and not os.path.isdir(os.path.join(ref_root, "src")):
             env["SKIP_CUBIN"] = "1"
+        env["REFERENCE_ROOT"] = ref_root
         _run(["sh", os.path.join(HERE, "build_ref.sh")], env=env)
     return lib if os.path.exists(lib) else None
 

@@ -1,8 +1,9 @@
 #!/bin/sh
 # Builds the reference's own fractal code into oracle/_ref/ (git-ignored).
 #
-# TEST INFRASTRUCTURE ONLY.  Run where the reference checkout exists
-# (REFERENCE_ROOT, default /root/reference).  Steps:
+# TEST INFRASTRUCTURE ONLY.  Run where the reference checkout exists:
+# REFERENCE_ROOT names it (oracle/build_oracle.py sets it: $REFERENCE_ROOT, else
+# a checkout named `reference` beside this repository).  Steps:
 #   1. copy the few CUDA sources the path needs into oracle/_ref/src/ (a
 #      build-directory copy; the checkout is read-only), patching one token in
 #      fractalRendererGeneric.cu:200 that current nvcc rejects
@@ -15,7 +16,7 @@
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
-REF="${REFERENCE_ROOT:-/root/reference}"
+REF="${REFERENCE_ROOT:?REFERENCE_ROOT must name the chaos-ultra checkout}"
 C="$REF/src/main/cuda"
 mkdir -p "$OUT/src/fractals"
 if [ -f "$C/fractalRendererGeneric.cu" ]; then

@@ -1,4 +1,4 @@
-"""Write data/deep_centres.json: the centre of the perturbation deep-zoom
+"""Write chaos-ultra_gb300/chaos_gb300/data/deep_centres.json: the centre of the perturbation deep-zoom
 workload (1920x1080, spans 1e-60 and 1e-200, maxIter 100000), a seeded point
 on the Mandelbrot set boundary as a 1024-bit fixed-point value.
 
@@ -17,7 +17,7 @@ converged below 2^-1080, the preperiod is exactly k (z_{k-1+q} != z_{k-1}) and
 the period exactly q (z_{k+d} != z_k for proper divisors d of q).  Needs
 mpmath; the result is committed so renders do not need it.
 
-    python chaos-ultra_gb300/chaos_gb300/make_deep_centres.py
+    python tests/golden/make_deep_centres.py
 """
 import json
 import os
@@ -25,7 +25,9 @@ import sys
 from fractions import Fraction
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, os.path.dirname(HERE))
+PKG = os.path.join(os.path.dirname(os.path.dirname(HERE)), "chaos-ultra_gb300")
+sys.path.insert(0, PKG)
+DATA = os.path.join(PKG, "chaos_gb300", "data")
 
 SEED, BITS, PREC = 3, 1024, 1150
 
@@ -85,8 +87,8 @@ def main():
     c = r.pop("c")
     r.update({"bits": BITS, "center_x": to_hex(mp, c.real), "center_y": to_hex(mp, c.imag),
               "approx": [float(c.real), float(c.imag)]})
-    os.makedirs(os.path.join(HERE, "data"), exist_ok=True)
-    with open(os.path.join(HERE, "data", "deep_centres.json"), "w") as f:
+    os.makedirs(DATA, exist_ok=True)
+    with open(os.path.join(DATA, "deep_centres.json"), "w") as f:
         json.dump(r, f, indent=1)
         f.write("\n")
     print(r["attempt"], r["preperiod"], r["period"], r["approx"])

@@ -1,6 +1,6 @@
 """chaos_render_frame_host_noalloc: the frame entry point for callers that may
-not allocate GPU memory (fixed GPU memory budgets, code between a stream-capture
-begin and end, bindings without a CUDA allocator).
+not allocate GPU memory (a process whose GPU memory is budgeted before it
+serves frames, a JNI/Panama binding without a CUDA allocator).
 
 It is checked through the C ABI against chaos_render_frame_host, the entry
 point that allocates its device buffers: two different frames in a row must
@@ -69,3 +69,26 @@ def test_noalloc_rejects_frames_beyond_its_scratch(cuda, native):
     assert rc == 1
     rc, got, total = _noalloc(cg, small, default_palette(), 0xFF000000)  # still usable afterwards
     assert rc == 0 and total > 0
+
+
+def test_noalloc_leaves_device_memory_unchanged(cuda, native):
+    """After one call has set the entry point up (address look-up, kernel
+    loaded), further calls -- the same frame again and a larger one on the
+    same kernel -- take no device memory: the device's free bytes
+    (cudaMemGetInfo) are the same before and after."""
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import default_palette
+    torch = cuda
+    small = _desc(cg, 64, 48, 1, cg.SAMPLES_CENTER, cg.TIER_F32, cg.ARITH_FMA, (-0.5, 0.0), 3.0 / 64, 0)
+    large = _desc(cg, 1920, 1080, 1, cg.SAMPLES_CENTER, cg.TIER_F32, cg.ARITH_FMA, (-0.75, 0.1), 0.01 / 1920, 0)
+    pal = default_palette()
+    rc, _, _ = _noalloc(cg, small, pal, 0xFF000000)  # set-up call
+    assert rc == 0, cg.lib().chaos_last_error()
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    for desc in (small, large):
+        rc, _, total = _noalloc(cg, desc, pal, 0xFF000000)
+        assert rc == 0 and total > 0, cg.lib().chaos_last_error()
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
