@@ -43,6 +43,8 @@ W, H, SPAN, MAX_ITER, SPP = 3840, 2160, 1e-10, 20000, 4
 FULL_W = W  # the plane span is defined on the full 3840-pixel width
 METRIC = "Gpixel-iter/s at <=0.1% escape-count mismatch vs FP64 oracle"
 MISMATCH_SAMPLE_PIXELS = 4096
+E2E_FRAMES = 3  # frames timed through the host-buffer call (each ~4.7 s at C2)
+MIN_TIMED_S = 2.5  # shortest timed region of the C1 / C3 lines (clock samples every 200 ms)
 
 
 # ---------------------------------------------------------------------------
@@ -312,9 +314,10 @@ def run_ours(args):
         pass
     cg.render_frame_host(desc, wl["palette"], wl["interior_rgba"], host_rgba)  # warm the workspace
     torch.cuda.synchronize()
+    e2e_frames = min(args.steps, E2E_FRAMES)
     e0 = time.perf_counter()
     e2e_iters = 0
-    for _ in range(args.steps):
+    for _ in range(e2e_frames):
         e2e_iters += cg.render_frame_host(desc, wl["palette"], wl["interior_rgba"], host_rgba)
     e2e_s = time.perf_counter() - e0
     e2e_value = e2e_iters / e2e_s / 1e9
@@ -396,11 +399,20 @@ def run_ours(args):
         "roofline": roof,
         "cpu_baseline": base,
         "e2e": {"value": e2e_value, "unit": "Gpixel-iter/s", "h2d_bytes_per_step": 4 * len(wl["palette"]),
-                "d2h_bytes_per_step": 4 * W * H + 8, "call": "chaos_render_frame_host"},
+                "d2h_bytes_per_step": 4 * W * H + 8, "call": "chaos_render_frame_host", "frames": e2e_frames},
         "gpu_launches": args.steps,
         "clocks": clk,
         "wall_s_timed": wall,
     }
+    if not args.headline_only and W == 3840:
+        # after the headline's timed region: the benchmark spec's other claims, each
+        # with its own clock record (the reference's own GPU kernel on this machine,
+        # the batched C4 forms, the served C5 trace)
+        t_sub = time.perf_counter()
+        line["vs_reference_kernel"] = measure_vs_reference_kernel()
+        line["c4"] = measure_c4("c4", steps=3, warmup=1, compact=True)
+        line["c5"] = measure_c5(seconds=C5_BENCH_SECONDS, compact=True)
+        line["wall_s_sub_objects"] = time.perf_counter() - t_sub
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -411,16 +423,121 @@ def _l2_flush(torch, dev):
     return lambda k: buf.fill_(k & 255)
 
 
-def run_batch(args):
+REF_CUBIN_DIR = os.path.join(ROOT, "oracle", "_ref")
+VS_REF_W, VS_REF_H = 1920, 1080
+
+
+def measure_vs_reference_kernel(launches=3):
+    """The reference's own fractalRenderMainDouble against the drop-in modules
+    on the same GB300, the way the Java host runs them: module loaded by file
+    (cuModuleLoad), 32x32 blocks over ceil(W/32) x ceil(H/32), the legacy
+    default stream (CudaFractalRenderer.java:235-269).
+
+    The reference's mandelbrot module is its own source built for sm_103a
+    twice: as nvcc builds it by default (contraction on: the build the Java
+    application loads) and with --fmad=false (every product and sum rounded,
+    the FP64 oracle's arithmetic).  They are set against cudaKernels/ (the
+    default build's arithmetic reproduced) and cudaKernels_parity/ (rounded).
+    View: the central 1920x1080 of the C2 frame (pixel 1e-10/3840 around the
+    seeded boundary centre), maxIter 20000, maxSS 4, adaptive sampling on, in
+    the reference's own sampling (sample 0 at the pixel corner, diagonal /
+    grid pattern, warp votes).  One untimed launch, then `launches` launches
+    between CUDA events with an L2 flush between them; the records of the last
+    launch are compared field by field."""
+    import torch
+
+    import chaos_gb300 as cg
+    from chaos_gb300.dropin import Driver, java_grid, main_params, pitched, read_pixels, same_pixels
+
+    paths = {"reference_nofma": os.path.join(REF_CUBIN_DIR, "ref_mandelbrot_nofma.cubin"),
+             "dropin_parity": os.path.join(cg.DROPIN_PARITY_DIR, "mandelbrot.ptx"),
+             "reference_default": os.path.join(REF_CUBIN_DIR, "ref_mandelbrot.cubin"),
+             "dropin_contracted": os.path.join(cg.DROPIN_DIR, "mandelbrot.ptx")}
+    missing = [os.path.relpath(p, ROOT) for p in paths.values() if not os.path.exists(p)]
+    if missing:
+        return {"unavailable": "not built: " + ", ".join(missing)}
+    cx, cy = boundary_point(WORKLOAD_SEED)
+    ps = SPAN / FULL_W
+    w, h = VS_REF_W, VS_REF_H
+    rect = (cx - w / 2 * ps, cy - h / 2 * ps, cx + w / 2 * ps, cy + h / 2 * ps)
+    drv = Driver()
+    buf, pitch = pitched(torch, w, h)
+    grid, block = java_grid(w, h)
+    flush = _l2_flush(torch, torch.device("cuda", 0))
+    ms, recs = {}, {}
+    clocks = ClockSampler(0)
+    clocks.start()
+    for name, path in paths.items():
+        mod = drv.load(path)
+        try:
+            drv.write_constant(mod, "VISUALIZE_SAMPLE_COUNT", b"\0")
+            fn = drv.function(mod, "fractalRenderMainDouble")
+            params = main_params(buf.data_ptr(), pitch, w, h, rect, MAX_ITER, 4.0, cg.FLAG_ADAPTIVE_SS, True)
+            drv.launch(fn, grid, block, params)
+            times = []
+            for k in range(launches):
+                flush(k)
+                buf.zero_()
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                drv.launch(fn, grid, block, params, sync=False)
+                e1.record()
+                torch.cuda.synchronize()
+                times.append(e0.elapsed_time(e1))
+            ms[name] = times
+            recs[name] = read_pixels(buf, w)
+        finally:
+            drv.unload(mod)
+    clk = clocks.stop()
+    med = {k: statistics.median(v) for k, v in ms.items()}
+    return {
+        "view": f"C2 central {w}x{h}: pixel {SPAN}/{FULL_W}, maxIter {MAX_ITER}, maxSS 4, adaptive sampling, "
+                "fractalRenderMainDouble in the Java launch shape",
+        "launches": launches, "ms": ms, "ms_median": med,
+        "speedup": {"dropin_parity_vs_reference_nofma": med["reference_nofma"] / med["dropin_parity"],
+                    "dropin_contracted_vs_reference_default": med["reference_default"] / med["dropin_contracted"]},
+        "records_differing": {
+            "dropin_parity_vs_reference_nofma": float(same_pixels(recs["dropin_parity"],
+                                                                  recs["reference_nofma"]).mean()),
+            "dropin_contracted_vs_reference_default": float(same_pixels(recs["dropin_contracted"],
+                                                                        recs["reference_default"]).mean())},
+        "reference_build": "the reference's src/main/cuda mandelbrot module built from source for sm_103a "
+                           "(oracle/build_ref.sh): default nvcc contraction and --fmad=false",
+        "clocks": clk}
+
+
+def _timed_launches(torch, stream, flush, launch, n):
+    """One untimed launch, then n launches between CUDA events on `stream`
+    with an L2 flush before each; returns the list of ms."""
+    launch()
+    torch.cuda.synchronize()
+    ms = []
+    for k in range(n):
+        flush(k)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        launch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return ms
+
+
+def measure_c4(workload="c4", steps=3, warmup=3, compact=False):
     """C4: 64 viewports (side 256..2048, span 1e-12..1e-3, maxIter 500..50000,
     seeded boundary centres) in one CUDA-graph launch, tier per viewport.
 
     Beside the tiered value: the same batch in binary64 rounded as the
     reference's computeFractal<double> (tier F64_ROUNDED, the FP64 oracle's
     counts bit for bit), whose counts give every other form's mismatch against
-    the FP64 oracle over all pixels; and a CPU leg that runs the reference's own
-    host-built computeFractal<double> at seeded pixels of every viewport (the
-    CPU baseline, and the oracle those counts are checked on)."""
+    the FP64 oracle over all pixels; the plain FP64 drop-in viewport by
+    viewport (the library's fractalRenderMainDouble, and the drop-in module
+    and the reference's own module, both built --fmad=false, in the Java launch
+    shape); and a CPU leg that runs the reference's own host-built
+    computeFractal<double> at seeded pixels of every viewport (the CPU
+    baseline, and the oracle those counts are checked on).  `compact` leaves
+    out the untuned shape and the per-tier breakdown."""
     import numpy as np
     import torch
 
@@ -430,7 +547,7 @@ def run_batch(args):
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
     specs = c4_viewports()
-    if args.workload == "c4-crop":
+    if workload == "c4-crop":
         # the central 256 x 256 window of each viewport at the same pixel size (profiler captures)
         for sp in specs:
             side = min(sp["width"], 256)
@@ -465,14 +582,14 @@ def run_batch(args):
     batch, bufs = make(cg.TIER_AUTO, tuned)
     stream = torch.cuda.current_stream()
     flush = _l2_flush(torch, dev)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batch.launch(stream)
     torch.cuda.synchronize()
     per_launch = batch.read_total()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     clocks = ClockSampler(0)
     clocks.start()
-    for k in range(args.steps):
+    for k in range(steps):
         flush(k)
         ev[k][0].record(stream)
         batch.launch(stream)
@@ -480,135 +597,139 @@ def run_batch(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     ms = [a.elapsed_time(b) for a, b in ev]
-    value = per_launch * args.steps / (sum(ms) / 1e3) / 1e9
+    value = per_launch * steps / (sum(ms) / 1e3) / 1e9
     tiers = batch.tiers()
     tiered_counts = [c.cpu().numpy() for c, _ in bufs]
+    batch.close()
+    del batch, bufs
 
-    # the same batch with the default launch shape (256 threads, 16-step blocks, chunk 1)
-    untuned, ubufs = make(cg.TIER_AUTO)
-    untuned.launch(stream)
-    torch.cuda.synchronize()
-    u_ms = []
-    for k in range(2):
-        flush(k)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        untuned.launch(stream)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        u_ms.append(e0.elapsed_time(e1))
-    untuned.close()
-    del untuned, ubufs
+    # binary64 rounded as the reference's computeFractal<double> (tier
+    # F64_ROUNDED): the FP64 oracle's escape counts, bit for bit, for every pixel
+    rounded, rbufs = make(cg.TIER_F64_ROUNDED, tuned)
+    rclocks = ClockSampler(0)
+    rclocks.start()
+    r_ms = _timed_launches(torch, stream, flush, lambda: rounded.launch(stream), steps)
+    rclk = rclocks.stop()
+    rounded_iters = rounded.read_total()
+    rounded_value = rounded_iters * len(r_ms) / (sum(r_ms) / 1e3) / 1e9
+    rounded_counts = [c.cpu().numpy() for c, _ in rbufs]
+    rounded.close()
+    del rounded, rbufs
+    total = sum(len(a) for a in rounded_counts)
+
+    def vs_oracle(counts):
+        return sum(int((c != r).sum()) for c, r in zip(counts, rounded_counts)) / total
+
+    untuned_ms = None
+    if not compact:
+        # the same batch with the default launch shape (256 threads, 16-step blocks, chunk 1)
+        untuned, ubufs = make(cg.TIER_AUTO)
+        untuned_ms = min(_timed_launches(torch, stream, flush, lambda: untuned.launch(stream), 2))
+        untuned.close()
+        del untuned, ubufs
 
     plain, pbufs = make(cg.TIER_F64)
-    plain.launch(stream)
-    torch.cuda.synchronize()
-    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s0.record(stream)
-    plain.launch(stream)
-    s1.record(stream)
-    torch.cuda.synchronize()
-    plain_ms = s0.elapsed_time(s1)
+    plain_ms = _timed_launches(torch, stream, flush, lambda: plain.launch(stream), 1)[0]
     plain_value = plain.read_total() / (plain_ms / 1e3) / 1e9
     plain_counts = [c.cpu().numpy() for c, _ in pbufs]
-    diff = sum(int((a != c).sum()) for a, c in zip(tiered_counts, plain_counts))
-    total = sum(len(a) for a in tiered_counts)
     plain.close()
     del plain, pbufs
 
     # binary32 / float-float / perturbation (the deep viewports on reference orbits)
     deep, dbufs = make(cg.TIER_AUTO_DEEP)
-    deep.launch(stream)
-    torch.cuda.synchronize()
-    deep_ms = []
-    for k in range(2):
-        flush(k)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        deep.launch(stream)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        deep_ms.append(e0.elapsed_time(e1))
+    deep_ms = _timed_launches(torch, stream, flush, lambda: deep.launch(stream), 2)
     deep_value = deep.read_total() / (min(deep_ms) / 1e3) / 1e9
     deep_tiers = deep.tiers()
     deep_counts = [c.cpu().numpy() for c, _ in dbufs]
-    deep_diff = sum(int((c != a).sum()) for c, a in zip(deep_counts, plain_counts))
     deep.close()
     del deep, dbufs
 
-    # binary64 rounded as the reference's computeFractal<double> (tier
-    # F64_ROUNDED): the FP64 oracle's escape counts, bit for bit, for every pixel
-    rounded, rbufs = make(cg.TIER_F64_ROUNDED, tuned)
-    rounded.launch(stream)
-    torch.cuda.synchronize()
-    r_ms = []
-    for k in range(2):
-        flush(k)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        rounded.launch(stream)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        r_ms.append(e0.elapsed_time(e1))
-    rounded_iters = rounded.read_total()
-    rounded_value = rounded_iters / (min(r_ms) / 1e3) / 1e9
-    rounded_counts = [c.cpu().numpy() for c, _ in rbufs]
-    rounded.close()
-    del rounded, rbufs
-
-    def vs_oracle(counts):
-        return sum(int((c != r).sum()) for c, r in zip(counts, rounded_counts)) / total
-
-    # time per tier: the same batch restricted to one tier's viewports
     per_tier = {}
-    for tier_id, name in ((2, "floatfloat"), (1, "f64"), (0, "f32")):
-        idx = [k for k, t in enumerate(tiers) if t == tier_id]
-        if not idx:
-            continue
-        sub_bufs, sub_vps = [], []
-        for k in idx:
-            sp = specs[k]
-            n = sp["width"] * sp["height"]
-            rgba = torch.zeros(n, dtype=torch.int32, device=dev)
-            sub_bufs.append(rgba)
-            sub_vps.append(cg.Viewport(width=sp["width"], height=sp["height"], max_iterations=sp["max_iter"],
-                                       samples_per_pixel=1, sample_mode=cg.SAMPLES_CENTER, tier=tier_id,
-                                       seed=sp["seed"], center_x=sp["center"][0], center_y=sp["center"][1],
-                                       pixel_size=sp["span"] / sp["width"], rgba=rgba.data_ptr()))
-        sb = cg.Batch(sub_vps, dpal.data_ptr(), len(pal), 0xFF000000, tuned)
-        sb.launch(stream)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        sb.launch(stream)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        t_ms = e0.elapsed_time(e1)
-        it = sb.read_total()
-        per_tier[name] = {"viewports": len(idx), "ms": t_ms, "pixel_iterations": it,
-                          "Gpixel_iter_s": it / (t_ms / 1e3) / 1e9}
-        sb.close()
+    if not compact:
+        # time per tier: the same batch restricted to one tier's viewports
+        for tier_id, name in ((2, "floatfloat"), (1, "f64"), (0, "f32")):
+            idx = [k for k, t in enumerate(tiers) if t == tier_id]
+            if not idx:
+                continue
+            sub_bufs, sub_vps = [], []
+            for k in idx:
+                sp = specs[k]
+                n = sp["width"] * sp["height"]
+                rgba = torch.zeros(n, dtype=torch.int32, device=dev)
+                sub_bufs.append(rgba)
+                sub_vps.append(cg.Viewport(width=sp["width"], height=sp["height"], max_iterations=sp["max_iter"],
+                                           samples_per_pixel=1, sample_mode=cg.SAMPLES_CENTER, tier=tier_id,
+                                           seed=sp["seed"], center_x=sp["center"][0], center_y=sp["center"][1],
+                                           pixel_size=sp["span"] / sp["width"], rgba=rgba.data_ptr()))
+            sb = cg.Batch(sub_vps, dpal.data_ptr(), len(pal), 0xFF000000, tuned)
+            t_ms = _timed_launches(torch, stream, flush, lambda: sb.launch(stream), 1)[0]
+            it = sb.read_total()
+            per_tier[name] = {"viewports": len(idx), "ms": t_ms, "pixel_iterations": it,
+                              "Gpixel_iter_s": it / (t_ms / 1e3) / 1e9}
+            sb.close()
 
-    # the plain FP64 drop-in: fractalRenderMainDouble semantics (rounded arithmetic,
-    # one sample at the pixel corner, no adaptive super-sampling), viewport by viewport
+    # the plain FP64 drop-in, viewport by viewport: fractalRenderMainDouble
+    # semantics (rounded arithmetic, one sample at the pixel corner, no
+    # adaptive super-sampling) through (i) the library's C ABI, (ii) the
+    # drop-in module and (iii) the reference's own module (both --fmad=false)
+    # in the Java launch shape.  Each form's pixel-iterations are counted from
+    # its own records (value 0 = interior = maxIter).
+    from chaos_gb300.dropin import Driver, java_grid, main_params, pitched, read_pixels, same_pixels
     module = cg.Module("mandelbrot")
-    dm_ms, dm_iters = 0.0, 0
+    drv = Driver()
+    forms = {"library": None, "dropin_module": os.path.join(cg.DROPIN_PARITY_DIR, "mandelbrot.ptx"),
+             "reference_module": os.path.join(REF_CUBIN_DIR, "ref_mandelbrot_nofma.cubin")}
+    fns, mods = {}, []
+    for name, path in list(forms.items()):
+        if path is None:
+            continue
+        if not os.path.exists(path):
+            forms.pop(name)
+            continue
+        m = drv.load(path)
+        mods.append(m)
+        drv.write_constant(m, "VISUALIZE_SAMPLE_COUNT", b"\0")
+        fns[name] = drv.function(m, "fractalRenderMainDouble")
+    vp_stats = {name: {"ms": 0.0, "iters": 0} for name in forms}
+    records_differ = 0
+    vp_clocks = ClockSampler(0)
+    vp_clocks.start()
     for sp in specs:
         w_, h_ = sp["width"], sp["height"]
-        pitch = 16 * w_
-        out = torch.empty((h_, pitch), dtype=torch.uint8, device=dev)
+        buf, pitch = pitched(torch, w_, h_)
         cx, cy, span = sp["center"][0], sp["center"][1], sp["span"]
         rect = (cx - span / 2, cy - span / 2 * h_ / w_, cx + span / 2, cy + span / 2 * h_ / w_)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        module.render_main(out.data_ptr(), pitch, w_, h_, rect, sp["max_iter"], 1.0, 0, double=True,
-                           arith=cg.ARITH_PARITY, stream=stream)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        dm_ms += e0.elapsed_time(e1)
-        vals = out.view(torch.float32).reshape(h_, w_, 4)[:, :, 0].cpu().numpy()
-        dm_iters += int(np.where(vals == 0, sp["max_iter"], vals).astype(np.int64).sum())
-    dropin_value = dm_iters / (dm_ms / 1e3) / 1e9
+        recs = {}
+        for name in forms:
+            if name == "library":
+                def go():
+                    module.render_main(buf.data_ptr(), pitch, w_, h_, rect, sp["max_iter"], 1.0, 0, double=True,
+                                       arith=cg.ARITH_PARITY, stream=stream)
+            else:
+                params = main_params(buf.data_ptr(), pitch, w_, h_, rect, sp["max_iter"], 1.0, 0, True)
+                grid, block = java_grid(w_, h_)
+
+                def go(fn=fns[name], params=params, grid=grid, block=block):
+                    drv.launch(fn, grid, block, params, sync=False)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            go()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            vp_stats[name]["ms"] += e0.elapsed_time(e1)
+            recs[name] = read_pixels(buf, w_)
+            vals = recs[name]["value"]
+            vp_stats[name]["iters"] += int(np.where(vals == 0, sp["max_iter"], vals).astype(np.int64).sum())
+        if "reference_module" in recs:
+            records_differ += int(same_pixels(recs["dropin_module"], recs["reference_module"]).sum())
+        del buf
+    vp_clk = vp_clocks.stop()
+    for m in mods:
+        drv.unload(m)
+    plain_forms = {name: {"value": st["iters"] / (st["ms"] / 1e3) / 1e9, "ms": st["ms"],
+                          "pixel_iterations": st["iters"]} for name, st in vp_stats.items()}
+    dropin_value = plain_forms["library"]["value"]
 
     # CPU leg: the reference's own computeFractal<double> (host build, all host
     # threads) at seeded pixels of every viewport, the same binary64 sample
@@ -618,7 +739,7 @@ def run_batch(args):
     orc = Oracle()
     rng = np.random.default_rng(44)
     cpu_iters, cpu_s, cpu_n, cpu_bad = 0, 0.0, 0, {"rounded": 0, "tiered": 0, "tiered_deep": 0, "f64_fma": 0}
-    per_vp = 1024 if args.workload == "c4" else 256
+    per_vp = 256 if (compact or workload != "c4") else 1024
     for k, sp in enumerate(specs):
         n_pix = sp["width"] * sp["height"]
         pix = np.sort(rng.choice(n_pix, size=min(per_vp, n_pix), replace=False))
@@ -638,49 +759,75 @@ def run_batch(args):
                 "sample": f"{cpu_n} seeded pixels ({per_vp} per viewport) at the batch's sample points, "
                           f"FP64 computeFractal, {cpu_iters} pixel-iterations in {cpu_s:.2f} s"}
     oracle_mismatch = {name: bad / cpu_n for name, bad in cpu_bad.items()}
-    line = {"metric": "Gpixel-iter/s (batched uneven launch)", "value": value, "unit": "Gpixel-iter/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(ms) / args.steps,
+    ref_mod = plain_forms.get("reference_module")
+    out = {
+        "workload": "C4: 64 Mandelbrot viewports, side log-uniform 256..2048, span log-uniform 1e-12..1e-3, "
+                    "maxIter log-uniform 500..50000, one CUDA-graph launch",
+        "crop": "central 256x256 of each viewport" if workload == "c4-crop" else None,
+        "pixels": total, "steps": steps, "warmup": warmup,
+        "tiered": {"value": value, "ms": ms, "pixel_iterations": per_launch,
+                   "tiers": {"f32": tiers.count(0), "floatfloat": tiers.count(2), "f64": tiers.count(1)},
+                   "escape_count_mismatch_vs_fp64_oracle": vs_oracle(tiered_counts),
+                   "speedup_of_plain_f64_dropin": value / dropin_value, "clocks": clk},
+        "rounded_f64_batch": {
+            "value": rounded_value, "ms": r_ms, "pixel_iterations": rounded_iters,
+            "escape_count_mismatch_vs_fp64_oracle_cpu_sample": oracle_mismatch["rounded"],
+            "speedup_of_plain_f64_dropin": rounded_value / dropin_value,
+            "speedup_of_reference_module": rounded_value / ref_mod["value"] if ref_mod else None,
+            "what": "all 64 viewports in binary64 rounded as the reference's computeFractal<double> "
+                    "(tier F64_ROUNDED, one graph launch): the form within 0.1% of the FP64 oracle",
+            "clocks": rclk},
+        "tiered_deep": {"value": deep_value, "ms": min(deep_ms),
+                        "tiers": {"f32": deep_tiers.count(0), "floatfloat": deep_tiers.count(2),
+                                  "perturb_f32": deep_tiers.count(3), "perturb_f64": deep_tiers.count(4)},
+                        "escape_count_mismatch_vs_fp64_oracle": vs_oracle(deep_counts),
+                        "speedup_of_plain_f64_dropin": deep_value / dropin_value,
+                        "what": "binary32 / float-float / perturbation on per-viewport reference orbits "
+                                "(orbits computed at batch creation, outside the timed launch)"},
+        "f64_fma_batch": {"value": plain_value, "ms": plain_ms,
+                          "escape_count_mismatch_vs_fp64_oracle": vs_oracle(plain_counts)},
+        "plain_f64_dropin": dict(plain_forms["library"], what=(
+            "fractalRenderMainDouble semantics (binary64, rounded arithmetic, 1 sample per pixel) viewport by "
+            "viewport through the C ABI (chaos_render_main_f64): the north-star's plain FP64 drop-in")),
+        "plain_f64_java_shape": {
+            "dropin_module": plain_forms.get("dropin_module"), "reference_module": ref_mod,
+            "records_differing_dropin_vs_reference": records_differ / total if ref_mod else None,
+            "what": "the same viewports through cudaKernels_parity/mandelbrot.ptx and the reference's own module "
+                    "built --fmad=false, 32x32 blocks per viewport on the default stream", "clocks": vp_clk},
+        "north_star": {
+            "bar": ">= 3x the plain FP64 drop-in at <= 0.1% escape-count mismatch vs the FP64 oracle",
+            "within_bar_form": "rounded_f64_batch",
+            "within_bar_speedup_of_plain_f64_dropin": rounded_value / dropin_value,
+            "within_bar_speedup_of_reference_module": rounded_value / ref_mod["value"] if ref_mod else None,
+            "tiered_speedup_and_mismatch": [value / dropin_value, vs_oracle(tiered_counts)],
+            "tiered_deep_speedup_and_mismatch": [deep_value / dropin_value, vs_oracle(deep_counts)]},
+        "escape_count_mismatch_vs_fp64_oracle_cpu_sample": oracle_mismatch,
+        "autotune": {"seconds": t_tune,
+                     "shape": {name: {"threads": tuned.block_threads[k], "escape_block": tuned.escape_block[k],
+                                      "chunk": tuned.chunk[k]}
+                               for k, name in enumerate(("f32", "floatfloat", "f64"))},
+                     "fp64_warps_per_sm_when_shared": tuned.fp64_warps_per_sm,
+                     "default_shape_ms": untuned_ms, "tuned_ms": min(ms)},
+        "cpu_baseline": cpu_base,
+        "gpu_launches": steps * sum(1 for t in (0, 1, 2) if t in tiers)}
+    if per_tier:
+        out["per_tier"] = per_tier
+    return out
+
+
+def run_batch(args):
+    """The C4 line: tiered batch value, with every other form beside it."""
+    c4 = measure_c4(args.workload, args.steps, args.warmup)
+    t = c4["tiered"]
+    line = {"metric": "Gpixel-iter/s (batched uneven launch)", "value": t["value"], "unit": "Gpixel-iter/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(t["ms"]) / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/ff/f64 per viewport",
             "data": "synthetic: seeded viewports and boundary centres",
-            "config": {"workload": "C4: 64 Mandelbrot viewports, side log-uniform 256..2048, span log-uniform "
-                                   "1e-12..1e-3, maxIter log-uniform 500..50000, one CUDA-graph launch",
-                       "pixels": total, "l2": "flushed between launches",
-                       "crop": "central 256x256 of each viewport" if args.workload == "c4-crop" else None},
-            "tiers": {"f32": tiers.count(0), "floatfloat": tiers.count(2), "f64": tiers.count(1)},
-            "pixel_iterations_per_step": per_launch,
-            "plain_f64_dropin": {"value": dropin_value, "ms": dm_ms, "speedup_of_tiered": value / dropin_value,
-                                 "what": "fractalRenderMainDouble semantics: binary64, rounded arithmetic, "
-                                         "1 sample per pixel, per viewport"},
-            "f64_fma_batch": {"value": plain_value, "ms": plain_ms, "speedup_of_tiered": value / plain_value},
-            "autotune": {"seconds": t_tune,
-                         "shape": {name: {"threads": tuned.block_threads[k], "escape_block": tuned.escape_block[k],
-                                          "chunk": tuned.chunk[k]}
-                                   for k, name in enumerate(("f32", "floatfloat", "f64"))},
-                         "fp64_warps_per_sm_when_shared": tuned.fp64_warps_per_sm,
-                         "default_shape_ms": min(u_ms), "tuned_ms": min(ms),
-                         "default_shape_value": per_launch / (min(u_ms) / 1e3) / 1e9},
-            "tiered_deep": {"value": deep_value, "ms": min(deep_ms),
-                            "tiers": {"f32": deep_tiers.count(0), "floatfloat": deep_tiers.count(2),
-                                      "perturb_f32": deep_tiers.count(3), "perturb_f64": deep_tiers.count(4)},
-                            "escape_count_mismatch_vs_f64_batch": deep_diff / total,
-                            "what": "binary32 / float-float / perturbation on per-viewport reference orbits "
-                                    "(orbits computed at batch creation, outside the timed launch)"},
-            "per_tier": per_tier,
-            "escape_count_mismatch_vs_f64_batch": diff / total,
-            "rounded_f64_batch": {
-                "value": rounded_value, "ms": min(r_ms), "pixel_iterations": rounded_iters,
-                "speedup_of_plain_f64_dropin": rounded_value / dropin_value,
-                "escape_count_mismatch_vs_fp64_oracle_cpu_sample": oracle_mismatch["rounded"],
-                "what": "all 64 viewports in binary64 rounded as the reference's computeFractal<double> "
-                        "(tier F64_ROUNDED, one graph launch): the form within 0.1% of the FP64 oracle"},
-            "escape_count_mismatch_vs_fp64_oracle": {
-                "all_pixels_vs_rounded_batch": {"tiered": vs_oracle(tiered_counts),
-                                                "tiered_deep": vs_oracle(deep_counts),
-                                                "f64_fma_batch": vs_oracle(plain_counts)},
-                "cpu_sample_vs_reference": oracle_mismatch},
-            "cpu_baseline": cpu_base,
-            "gpu_launches": args.steps * sum(1 for t in (0, 1, 2) if t in tiers),
-            "gpu_launches_note": "one persistent kernel per tier present per graph launch", "clocks": clk}
+            "config": {"workload": c4["workload"], "pixels": c4["pixels"], "l2": "flushed between launches",
+                       "crop": c4["crop"]},
+            "cpu_baseline": c4["cpu_baseline"], "gpu_launches": c4["gpu_launches"],
+            "gpu_launches_note": "one persistent kernel per tier present per graph launch", "clocks": t["clocks"],
+            "c4": c4}
     print(json.dumps(line), flush=True)
 
 
@@ -731,9 +878,13 @@ def run_c1(args):
         torch.cuda.synchronize()
         return int(total.item()), sum(a.elapsed_time(b) for a, b in ev)
 
+    # the timed region lasts at least MIN_TIMED_S, so that the clock sampler
+    # (one sample per 200 ms) sees it: more frames than --steps when needed
+    _, probe_ms = timed(cg.ARITH_PARITY, 3, args.warmup)
+    args.steps = max(args.steps, math.ceil(MIN_TIMED_S * 1e3 / max(probe_ms / 3, 1e-3)))
     clocks = ClockSampler(0)
     clocks.start()
-    iters, ms = timed(cg.ARITH_PARITY, args.steps, args.warmup)
+    iters, ms = timed(cg.ARITH_PARITY, args.steps, 1)
     clk = clocks.stop()
     per_frame = iters // args.steps
     c = counts.cpu().numpy().view(np.uint32)
@@ -749,7 +900,8 @@ def run_c1(args):
     d = desc(cg.ARITH_PARITY)
     cg.render_frame_host(d, pal, 0xFF000000, host)
     e0 = time.perf_counter()
-    e_iters = sum(cg.render_frame_host(d, pal, 0xFF000000, host) for _ in range(args.steps))
+    e_frames = min(args.steps, 2000)
+    e_iters = sum(cg.render_frame_host(d, pal, 0xFF000000, host) for _ in range(e_frames))
     e_s = time.perf_counter() - e0
 
     # roofline: FP32 pipe against the plain step's 6 instructions (the binary32
@@ -873,9 +1025,12 @@ def run_deep(args):
         cg.render_frame_perturb(desc(sp, cg.TIER_PERTURB_F32), orbit, out, stream=stream)
         span_iters.append(int(total.item()))
 
+    # the timed region lasts at least MIN_TIMED_S (more steps than --steps when needed)
+    _, probe_ms, _ = timed(cg.TIER_PERTURB_F32, 2, args.warmup)
+    args.steps = max(args.steps, math.ceil(MIN_TIMED_S * 1e3 / max(sum(probe_ms) / 2, 1e-3)))
     clocks = ClockSampler(0)
     clocks.start()
-    iters, span_ms, rb = timed(cg.TIER_PERTURB_F32, args.steps, args.warmup)
+    iters, span_ms, rb = timed(cg.TIER_PERTURB_F32, args.steps, 1)
     clk = clocks.stop()
     kernel_ms = sum(span_ms)
     value = iters / (kernel_ms / 1e3) / 1e9
@@ -885,7 +1040,8 @@ def run_deep(args):
     host = torch.empty(n, dtype=torch.int32, pin_memory=True)
     e0 = time.perf_counter()
     e2e_iters = 0
-    for _ in range(args.steps):
+    e2e_steps = min(args.steps, 100)
+    for _ in range(e2e_steps):
         o2 = cg.Orbit(d["center_x"], d["center_y"], DEEP_ORBIT_BITS, DEEP_MAX_ITER)
         pal.copy_(torch.from_numpy(pal_host.view(np.int32)), non_blocking=False)
         for sp in DEEP_SPANS:
@@ -955,7 +1111,7 @@ def run_deep(args):
             "e2e": {"value": e2e_iters / e2e_s / 1e9, "unit": "Gpixel-iter/s", "h2d_bytes_per_step": 4 * len(pal_host),
                     "d2h_bytes_per_step": 2 * 4 * n,
                     "call": "chaos_orbit_create + chaos_render_frame_perturb x2 + image reads",
-                    "seconds_per_step": e2e_s / args.steps},
+                    "seconds_per_step": e2e_s / e2e_steps, "steps": e2e_steps},
             "gpu_launches": 2 * args.steps, "clocks": clk}
     print(json.dumps(line), flush=True)
     orbit.close()
@@ -1097,10 +1253,15 @@ def run_reuse(args):
     print(json.dumps(line), flush=True)
 
 
-def run_serve(args):
+C5_BENCH_SECONDS = 10.0
+
+
+def measure_c5(seconds=10.0, compact=False, n_cap=40):
     """C5: 16 zoom sessions (720p..2160p), 1.02x zoom per frame toward seeded
-    boundary points, Poisson arrivals at 60 Hz per session, HBM-budget admission,
-    sample reuse from the previous frame; p50/p99 frame latency."""
+    boundary points, Poisson arrivals at 60 Hz per session for `seconds`,
+    HBM-budget admission, sample reuse from the previous frame; p50/p99 frame
+    latency, queueing delay and render time apart, and the capacity of a
+    saturated server (n_cap frames per session submitted at once)."""
     import numpy as np
     import torch
 
@@ -1111,7 +1272,7 @@ def run_serve(args):
     torch.cuda.set_device(0)
     rng = np.random.default_rng(5)
     res = [(1280, 720), (1920, 1080), (2560, 1440), (3840, 2160)]
-    n_sessions, seconds, hz = 16, 2.0, 60.0
+    n_sessions, hz = 16, 60.0
     targets = boundary_points(list(range(500, 500 + n_sessions)), max_iter=2000)
     srv = cg.Server(48 << 30, default_palette())
     sids, shapes = [], []
@@ -1150,39 +1311,50 @@ def run_serve(args):
     iters = sum(srv.read(sid)[1] for sid in sids) - it0
     value = iters / (t1 - t0) / 1e9
 
-    # capacity: every session asks for 40 more frames at once (a saturated server)
-    n_cap = 40
+    def pct(a, q):
+        return float(np.percentile(a, q)) if len(a) else None
+
+    # capacity: every session asks for n_cap more frames at once (a saturated server)
     it1 = sum(srv.read(sid)[1] for sid in sids)
     r0 = len(srv.records())
+    cap_clocks = ClockSampler(0)
+    cap_clocks.start()
     c0 = srv.clock()
     for _ in range(n_cap):
         for sid in sids:
             srv.submit(sid)
     srv.drain()
     c1 = srv.clock()
+    cap_clk = cap_clocks.stop()
     cap_iters = sum(srv.read(sid)[1] for sid in sids) - it1
     cap_lat = np.array([(r[4] - r[2]) * 1e3 for r in srv.records()[r0:]])
     capacity = {"frames": int(len(cap_lat)), "seconds": c1 - c0, "Gpixel_iter_s": cap_iters / (c1 - c0) / 1e9,
                 "frames_per_s": len(cap_lat) / (c1 - c0),
                 "what": f"{n_cap} frames per session submitted at once; latency includes queueing",
-                "latency_ms_p50": float(np.percentile(cap_lat, 50)),
-                "latency_ms_p99": float(np.percentile(cap_lat, 99))}
-    line = {"metric": "Gpixel-iter/s; p99 frame latency (serving)", "value": value, "unit": "Gpixel-iter/s",
-            "n_gpus": 1, "steps": len(recs), "warmup": warm, "ms_per_step": float(lat.mean()),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 per frame",
-            "data": "synthetic: seeded resolutions, boundary targets and Poisson arrivals",
-            "config": {"workload": f"C5: {n_sessions} sessions, 1280x720..3840x2160, zoom 1.02x/frame, "
-                                   f"Poisson {hz:g} Hz per session for {seconds:g} s, maxIter 2000, maxSS 2, "
-                                   "sample reuse + foveation", "resolutions": [f"{w}x{h}" for w, h in shapes],
-                       "hbm_budget_gib": 48, "hbm_used_gib": srv.usage()[0] / 2 ** 30},
-            "frames": len(recs), "trace_s": t1 - t0,
-            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                           "max": float(lat.max()),
-                           "p50_1080p": float(np.percentile(lat1080, 50)) if len(lat1080) else None,
-                           "p99_1080p": float(np.percentile(lat1080, 99)) if len(lat1080) else None},
-            "pixel_iterations": iters, "capacity": capacity, "clocks": clk}
-    print(json.dumps(line), flush=True)
+                "latency_ms_p50": pct(cap_lat, 50), "latency_ms_p99": pct(cap_lat, 99), "clocks": cap_clk}
+    out = {"workload": f"C5: {n_sessions} sessions, 1280x720..3840x2160, zoom 1.02x/frame, Poisson {hz:g} Hz per "
+                       f"session for {seconds:g} s, maxIter 2000, maxSS 2, sample reuse + foveation",
+           "resolutions": [f"{w}x{h}" for w, h in shapes], "hbm_budget_gib": 48,
+           "hbm_used_gib": srv.usage()[0] / 2 ** 30, "frames": len(recs), "warmup_frames": warm,
+           "trace_s": t1 - t0, "value": value, "unit": "Gpixel-iter/s", "pixel_iterations": iters,
+           "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": float(lat.max()) if len(lat) else None,
+                          "p50_1080p": pct(lat1080, 50), "p99_1080p": pct(lat1080, 99)},
+           "capacity": capacity, "clocks": clk}
     srv.close()
+    return out
+
+
+def run_serve(args):
+    """The C5 line."""
+    c5 = measure_c5(seconds=C5_BENCH_SECONDS)
+    line = {"metric": "Gpixel-iter/s; p99 frame latency (serving)", "value": c5["value"], "unit": "Gpixel-iter/s",
+            "n_gpus": 1, "steps": c5["frames"], "warmup": c5["warmup_frames"],
+            "ms_per_step": c5["latency_ms"]["p50"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32/f64 per frame",
+            "data": "synthetic: seeded resolutions, boundary targets and Poisson arrivals",
+            "config": {"workload": c5["workload"], "resolutions": c5["resolutions"]},
+            "latency_ms": c5["latency_ms"], "clocks": c5["clocks"], "c5": c5}
+    print(json.dumps(line), flush=True)
 
 
 def main():
@@ -1191,6 +1363,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="C2: leave out the reference-kernel, C4 and C5 sub-objects after the headline")
     ap.add_argument("--workload", choices=["c1", "c2", "c2-crop", "c3", "c4", "c4-crop", "c5", "compose", "reuse"],
                     default="c2",
                     help="c2-crop / c4-crop: the central 480x270 pixels of the frame / 256x256 of each viewport "
