@@ -118,9 +118,26 @@ class SessionDesc(C.Structure):
     ]
 
 
+SESSION_FLAG_BINARY64 = 1 << 16
+
+
 class FrameRecord(C.Structure):
     _fields_ = [("session", C.c_uint32), ("frame", C.c_uint32), ("arrival_s", C.c_double), ("start_s", C.c_double),
-                ("done_s", C.c_double), ("precision", C.c_int32), ("pad_", C.c_int32)]
+                ("done_s", C.c_double), ("precision", C.c_int32), ("status", C.c_int32), ("gpu_ms", C.c_double)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("max_frames_in_flight", C.c_uint32), ("max_launches_in_flight", C.c_uint32),
+                ("max_wait_s", C.c_double), ("frame_time_limit_s", C.c_double), ("call_timeout_s", C.c_double)]
+
+
+class ServedFrame(C.Structure):
+    _fields_ = [("frame", C.c_uint32), ("precision", C.c_int32), ("advanced", C.c_uint32), ("flags", C.c_uint32),
+                ("arith", C.c_int32), ("max_iterations", C.c_uint32), ("max_super_sampling", C.c_float),
+                ("focus_x", C.c_uint32), ("focus_y", C.c_uint32), ("pad_", C.c_uint32),
+                ("rect", C.c_double * 4), ("rect_reused", C.c_double * 4),
+                ("pixels", C.c_void_p), ("pixels_pitch", C.c_long),
+                ("previous", C.c_void_p), ("previous_pitch", C.c_long)]
 
 _F4 = C.c_float * 4
 _D4 = C.c_double * 4
@@ -184,6 +201,10 @@ SIGNATURES = {
     "chaos_server_usage": (_int, [_vp, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     "chaos_server_clock": (C.c_double, [_vp]),
     "chaos_server_destroy": (_int, [_vp]),
+    "chaos_server_configure": (_int, [_vp, C.POINTER(ServerConfig)]),
+    "chaos_server_get_config": (_int, [_vp, C.POINTER(ServerConfig)]),
+    "chaos_server_queue": (_int, [_vp, C.POINTER(_u32), C.POINTER(_u32)]),
+    "chaos_server_frame_state": (_int, [_vp, _u32, C.POINTER(ServedFrame)]),
     "chaos_render_frame_host_noalloc": (_int, [C.POINTER(FrameDesc), _vp, _u32, _u32, _vp,
                                                C.POINTER(C.c_ulonglong), _vp]),
     "chaos_orbit_create": (_int, [C.c_char_p, C.c_char_p, _u32, _u32, C.POINTER(_vp)]),

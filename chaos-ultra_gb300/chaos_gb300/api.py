@@ -1,7 +1,8 @@
 """Thin object layer over the C ABI (names follow the reference's Java classes)."""
 import ctypes as C
 
-from ._native import (ARITH_FMA, BatchConfig, FrameDesc, FrameOut, FrameRecord, RenderingModel, SessionDesc, Viewport,
+from ._native import (ARITH_FMA, BatchConfig, FrameDesc, FrameOut, FrameRecord, RenderingModel, ServedFrame,
+                      ServerConfig, SessionDesc, Viewport,
                       _D4, _F4, check, lib)
 
 
@@ -301,6 +302,7 @@ class Server:
         return b.value
 
     def close_session(self, sid):
+        """Drop the session's queued frames, cancel those on the GPU, release its buffers."""
         check(lib().chaos_server_close(self.handle, sid))
         self.shapes.pop(sid, None)
 
@@ -320,11 +322,42 @@ class Server:
                                            len(s)))
 
     def records(self):
+        """(session, frame, arrival_s, start_s, done_s, precision, status, gpu_ms) per frame, oldest first;
+        start_s is the admission into a launch."""
         n = C.c_uint32()
         check(lib().chaos_server_records(self.handle, None, 0, C.byref(n)))
         buf = (FrameRecord * max(1, n.value))()
         check(lib().chaos_server_records(self.handle, buf, n.value, C.byref(n)))
-        return [(r.session, r.frame, r.arrival_s, r.start_s, r.done_s, r.precision) for r in buf[:n.value]]
+        return [(r.session, r.frame, r.arrival_s, r.start_s, r.done_s, r.precision, r.status, r.gpu_ms)
+                for r in buf[:n.value]]
+
+    def configure(self, **kw):
+        """Set chaos_server_config fields (max_frames_in_flight, max_launches_in_flight, max_wait_s,
+        frame_time_limit_s, call_timeout_s); the others keep their values."""
+        cfg = ServerConfig()
+        check(lib().chaos_server_get_config(self.handle, C.byref(cfg)))
+        for k, v in kw.items():
+            setattr(cfg, k, v)
+        check(lib().chaos_server_configure(self.handle, C.byref(cfg)))
+
+    def config(self):
+        cfg = ServerConfig()
+        check(lib().chaos_server_get_config(self.handle, C.byref(cfg)))
+        return {k: getattr(cfg, k) for k, _ in ServerConfig._fields_}
+
+    def queue(self):
+        """(frames waiting for admission, frames on the GPU)."""
+        w, f = C.c_uint32(), C.c_uint32()
+        check(lib().chaos_server_queue(self.handle, C.byref(w), C.byref(f)))
+        return w.value, f.value
+
+    def frame_state(self, sid):
+        """The session's latest finished frame (chaos_served_frame) as a dict."""
+        f = ServedFrame()
+        check(lib().chaos_server_frame_state(self.handle, sid, C.byref(f)))
+        out = {k: getattr(f, k) for k, _ in ServedFrame._fields_ if k != "pad_"}
+        out["rect"], out["rect_reused"] = tuple(f.rect), tuple(f.rect_reused)
+        return out
 
     def read(self, sid):
         import numpy as np

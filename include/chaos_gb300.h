@@ -367,12 +367,14 @@ int chaos_batch_destroy(chaos_batch *batch);
  * (RenderingController.zoomAt, J/rendering/RenderingController.java:130-150).
  * Frames follow CudaFractalRenderer: renderQuality first, then renderFast
  * (sample reuse from the previous frame, foveation around the target's pixel
- * when CHAOS_FLAG_FOVEATION is set). */
+ * when CHAOS_FLAG_FOVEATION is set).  The precision of each frame is
+ * chaos_select_precision's (binary32 where the reference's renderer would use
+ * it) unless CHAOS_SESSION_FLAG_BINARY64 is set. */
 typedef struct chaos_session_desc {
     uint32_t width, height;
     uint32_t max_iterations;
     float max_super_sampling;
-    uint32_t flags; /* CHAOS_FLAG_ADAPTIVE_SS | CHAOS_FLAG_SAMPLE_REUSE | CHAOS_FLAG_FOVEATION */
+    uint32_t flags; /* CHAOS_FLAG_ADAPTIVE_SS | CHAOS_FLAG_SAMPLE_REUSE | CHAOS_FLAG_FOVEATION | CHAOS_SESSION_FLAG_* */
     uint32_t fractal;
     int32_t arith;
     uint32_t pad_;
@@ -382,47 +384,111 @@ typedef struct chaos_session_desc {
     double julia_cx, julia_cy;
 } chaos_session_desc;
 
-/* One served frame; times in seconds on the server's clock. */
+/* Session flag (beside the kernel flags): every frame in binary64, also
+ * where the reference's renderer would pick binary32. */
+#define CHAOS_SESSION_FLAG_BINARY64 (1u << 16)
+
+/* One served frame; times in seconds on the server's clock.  start_s is the
+ * moment the frame was admitted into a launch (start_s - arrival_s is its
+ * queueing delay); gpu_ms is the device time of the launch that rendered it. */
 typedef struct chaos_frame_record {
     uint32_t session, frame;
-    double arrival_s, start_s, done_s; /* done_s < 0: not finished */
+    double arrival_s, start_s, done_s; /* start_s, done_s < 0: not admitted / not finished */
     int32_t precision;                 /* CHAOS_PRECISION_* the frame used */
-    int32_t pad_;
+    int32_t status; /* CHAOS_OK; CHAOS_ERR_TIMEOUT: waited past max_wait_s, or the launch ran past
+                       frame_time_limit_s (the frame is incomplete); CHAOS_ERR_STATE: its session was
+                       closed first (cancelled); CHAOS_ERR_CUDA: the launch failed */
+    double gpu_ms;
 } chaos_frame_record;
+
+/* Admission and time limits of a server (chaos_server_configure). */
+typedef struct chaos_server_config {
+    uint32_t max_frames_in_flight;   /* frames admitted and not finished, over all sessions (default 64, 1..4096) */
+    uint32_t max_launches_in_flight; /* launches queued on the GPU at once (default 2, 1..4) */
+    double max_wait_s;               /* a request not admitted within this time completes with
+                                        CHAOS_ERR_TIMEOUT (default 30; 0 = no limit) */
+    double frame_time_limit_s;       /* device time a launch may run before its unfinished frames stop
+                                        and complete with CHAOS_ERR_TIMEOUT (default 0 = none) */
+    double call_timeout_s;           /* longest wait of drain / read / close (default 120) */
+} chaos_server_config;
 
 typedef struct chaos_server chaos_server;
 
-/* A server with an HBM budget (bytes) for its sessions and one palette (host
- * array, copied).  Sessions are admitted against the budget. */
+/* A server with an HBM budget (bytes) for its sessions' device buffers and
+ * one palette (host array, copied).  Its scheduler thread admits frame
+ * requests and renders every admitted frame of all sessions in one launch
+ * (one persistent kernel per precision / arithmetic / fractal present, each
+ * pulling 8x4 tiles of all its frames from one work counter, then one
+ * compose over all frames).  Replaces, per session, the frame loop of
+ * CudaFractalRenderer.renderQuality / renderFast
+ * (J/cudarenderer/CudaFractalRenderer.java:159-206). */
 int chaos_server_create(size_t hbm_budget_bytes, const uint32_t *palette, uint32_t palette_len,
                         chaos_server **out);
+int chaos_server_configure(chaos_server *server, const chaos_server_config *config);
+int chaos_server_get_config(const chaos_server *server, chaos_server_config *config);
 /* Bytes a session of this shape is charged (two reuse buffers + RGBA8 output). */
 int chaos_server_session_bytes(const chaos_session_desc *desc, size_t *bytes);
-/* Open a session: refused with CHAOS_ERR_OUT_OF_MEMORY (nothing allocated)
- * when it does not fit the remaining budget.  The session keeps its buffers
- * and its own CUDA stream until closed. */
+/* Open a session.  Nothing is allocated yet: the session's buffers are
+ * allocated when its first frame is admitted, against the HBM budget, and
+ * held (with the session's reference orbit, for deep frames) until it is
+ * closed.  Fails with CHAOS_ERR_OUT_OF_MEMORY only when the session alone is
+ * larger than the whole budget. */
 int chaos_server_open(chaos_server *server, const chaos_session_desc *desc, uint32_t *session);
+/* Close a session: its queued frames are dropped (status CHAOS_ERR_STATE),
+ * its frames on the GPU are cancelled (their kernels stop taking the
+ * session's tiles), and its buffers are released, which admits waiting
+ * requests.  Returns once that is done, or CHAOS_ERR_TIMEOUT after
+ * call_timeout_s. */
 int chaos_server_close(chaos_server *server, uint32_t session);
-/* Enqueue the session's next frame and return at once (arrival_s is recorded
- * as the request's arrival time).  A Mandelbrot frame past binary64
- * (chaos_select_precision says CHAOS_PRECISION_TOO_BIG, where the reference's
- * renderer stops) is rendered by perturbation around the session's target
- * with binary64 differences, one sample per pixel centre; the target's
- * reference orbit is computed at the first such frame (again when the zoom
- * needs more bits) and held by the session until it closes. */
+/* Queue the session's next frame and return at once (arrival_s is recorded
+ * as the request's arrival time).  The request is admitted when a slot is
+ * free (max_frames_in_flight), the session's buffers fit the budget (its
+ * first frame; later ones are resident already) and the session's previous
+ * frame has been admitted; admitted frames of all sessions go to the GPU
+ * together in the next launch.  A Mandelbrot frame past binary64
+ * (chaos_select_precision says CHAOS_PRECISION_TOO_BIG, where the
+ * reference's renderer stops) is rendered by perturbation around the
+ * session's target with binary64 differences, one sample per pixel centre;
+ * the target's reference orbit is computed at the first such frame (again
+ * when the zoom needs more bits) and held by the session until it closes. */
 int chaos_server_submit(chaos_server *server, uint32_t session, double arrival_s);
-/* Wait until every submitted frame has finished. */
+/* Wait until every queued frame has finished (CHAOS_ERR_TIMEOUT after call_timeout_s). */
 int chaos_server_drain(chaos_server *server);
 /* Replay a request trace in real time: request k is submitted when the
  * server clock reaches (clock at the call) + arrival_s[k]; then drain. */
 int chaos_server_run_trace(chaos_server *server, const uint32_t *sessions, const double *arrival_s, uint32_t n);
-/* Records of all frames submitted so far (*n = their number; at most max are copied). */
+/* Records of the most recent frames (at most 65536 are kept, oldest first;
+ * *n = their number; at most max are copied). */
 int chaos_server_records(chaos_server *server, chaos_frame_record *out, uint32_t max, uint32_t *n);
+/* Frames waiting for admission and frames on the GPU. */
+int chaos_server_queue(chaos_server *server, uint32_t *waiting, uint32_t *in_flight);
 /* The session's latest RGBA8 image (width*height words) and the pixel-iterations
  * its frames have run so far; waits for the session's queued frames. */
 int chaos_server_read(chaos_server *server, uint32_t session, uint32_t *host_rgba,
                       unsigned long long *pixel_iterations);
-/* Bytes held by open sessions and the budget. */
+
+/* The session's latest finished frame, for checking it: its parameters and
+ * the device records it wrote (and, for a renderFast frame, the previous
+ * frame's records it reused, which stay intact until the session's next
+ * frame is admitted). */
+typedef struct chaos_served_frame {
+    uint32_t frame;
+    int32_t precision;  /* CHAOS_PRECISION_* */
+    uint32_t advanced;  /* 1: renderFast (fractalRenderAdvanced), 0: renderQuality (fractalRenderMain) */
+    uint32_t flags;     /* kernel flags the frame ran with */
+    int32_t arith;      /* CHAOS_ARITH_* */
+    uint32_t max_iterations;
+    float max_super_sampling;
+    uint32_t focus_x, focus_y;
+    uint32_t pad_;
+    double rect[4], rect_reused[4];
+    const chaos_pixel_info *pixels;
+    long pixels_pitch;
+    const chaos_pixel_info *previous;
+    long previous_pitch;
+} chaos_served_frame;
+int chaos_server_frame_state(chaos_server *server, uint32_t session, chaos_served_frame *out);
+/* Bytes held by sessions' buffers and the budget. */
 int chaos_server_usage(const chaos_server *server, size_t *used, size_t *budget);
 /* Seconds since the server was created. */
 double chaos_server_clock(const chaos_server *server);

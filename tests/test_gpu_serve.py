@@ -1,7 +1,14 @@
 """Serving (chaos_server_*): concurrent zoom sessions with device-resident
-reuse buffers, admitted by an HBM budget.  A session's frames are bit-exact
-whether it runs alone or mixed with others; a session's frame chain equals
-the oracle's renderQuality/renderFast restatement."""
+reuse buffers.  Frame requests queue and are admitted per request as frame
+slots and HBM budget free up; admitted frames of all sessions render together
+in one launch.  A session's frames are bit-exact whether it runs alone or
+mixed with others; a session's frame chain equals the oracle's
+renderQuality/renderFast restatement; queued frames wait for memory and are
+admitted when a session closes; frames past the wait limit or the launch time
+limit, and frames of a session closed while they run, end with the matching
+status and leave the server usable."""
+import time
+
 import numpy as np
 import pytest
 
@@ -81,24 +88,156 @@ def test_session_chain_matches_oracle(cuda, oracle):
     srv.close()
 
 
-def test_admission_by_hbm_budget(cuda):
+def _wait_queue(srv, pred, limit=60.0):
+    t0 = time.time()
+    while not pred(*srv.queue()):
+        assert time.time() - t0 < limit, srv.queue()
+        time.sleep(0.002)
+
+
+def _alone(cg, d, frames, pal):
+    srv = cg.Server(1 << 30, pal)
+    sid = srv.open(d)
+    for _ in range(frames):
+        srv.submit(sid)
+    srv.drain()
+    img, iters = srv.read(sid)
+    srv.close()
+    return img, iters
+
+
+def test_admission_waits_for_memory_and_slots(cuda):
+    """A full server queues the next session's frame instead of refusing it;
+    closing a session frees its memory and admits the waiting frame, whose
+    image equals the same session rendered alone."""
     import chaos_gb300 as cg
     from chaos_gb300.palette import default_palette
-    d = desc(cg, 1920, 1080, (-0.7453, 0.1127))
-    need = cg.Server.session_bytes(d)
-    srv = cg.Server(2 * need + need // 2, default_palette())
-    a = srv.open(d)
-    b = srv.open(d)
-    assert srv.usage() == (2 * need, 2 * need + need // 2)
-    with pytest.raises(cg.ChaosError) as e:
-        srv.open(d)
+    pal = default_palette()
+    descs = [desc(cg, 480, 270, t) for t in ((-0.7453, 0.1127), (-0.1011, 0.9563), (0.2925, 0.0148))]
+    need = cg.Server.session_bytes(descs[0])
+    srv = cg.Server(2 * need + need // 2, pal)
+    with pytest.raises(cg.ChaosError) as e:  # alone larger than the whole budget: refused at once
+        srv.open(desc(cg, 4096, 4096, (0.0, 0.0)))
     assert e.value.code == 6
-    srv.close_session(a)
-    c = srv.open(d)
-    srv.submit(b)
-    srv.submit(c)
-    srv.drain()
+    a, b, c = (srv.open(d) for d in descs)
+    assert srv.usage() == (0, 2 * need + need // 2)  # nothing allocated before a frame is admitted
+    for sid in (a, b, c):
+        srv.submit(sid)
+    _wait_queue(srv, lambda waiting, in_flight: waiting == 1 and in_flight == 0)
     assert srv.usage()[0] == 2 * need
+    recs = srv.records()
+    assert [r[3] >= 0 for r in recs] == [True, True, False]  # c's frame not admitted
+    srv.submit(a)  # a resident session goes on while c waits
+    _wait_queue(srv, lambda waiting, in_flight: waiting == 1 and in_flight == 0)
+    srv.close_session(a)
+    srv.drain()
+    recs = srv.records()
+    assert all(r[6] == 0 for r in recs), recs
+    rc_ = [r for r in recs if r[0] == c]
+    assert len(rc_) == 1 and rc_[0][3] >= rc_[0][2] and rc_[0][4] >= rc_[0][3]
+    assert srv.usage()[0] == 2 * need
+    img, iters = srv.read(c)
+    want, want_iters = _alone(cg, descs[2], 1, pal)
+    assert np.array_equal(img, want) and iters == want_iters
+    srv.close()
+
+
+def test_frame_slots_bound_frames_in_flight(cuda):
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import default_palette
+    srv = cg.Server(1 << 30, default_palette())
+    srv.configure(max_frames_in_flight=1)
+    ids = [srv.open(desc(cg, w, h, t)) for w, h, t in SESSIONS]
+    for _ in range(2):
+        for sid in ids:
+            srv.submit(sid)
+    srv.drain()
+    recs = sorted(srv.records(), key=lambda r: r[3])
+    assert len(recs) == 6 and all(r[6] == 0 for r in recs)
+    for prev, nxt in zip(recs, recs[1:]):  # one frame at a time: admitted after the previous one finished
+        assert nxt[3] >= prev[4]
+    srv.close()
+
+
+def test_wait_limit_expires_queued_frame(cuda):
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import default_palette
+    d = desc(cg, 480, 270, (-0.7453, 0.1127))
+    need = cg.Server.session_bytes(d)
+    srv = cg.Server(need + need // 2, default_palette())
+    srv.configure(max_wait_s=0.05)
+    a, b = srv.open(d), srv.open(d)
+    srv.submit(a)
+    srv.submit(b)  # no memory for b while a stays open
+    srv.drain()
+    recs = srv.records()
+    assert recs[0][6] == 0 and recs[1][6] == 7  # CHAOS_ERR_TIMEOUT
+    assert recs[1][4] - recs[1][2] >= 0.05 and recs[1][3] < 0
+    srv.close()
+
+
+HEAVY = dict(w=1920, h=1080, max_iter=20000)
+
+
+def _heavy(cg):
+    from chaos_gb300.workloads import boundary_point
+    t = boundary_point(2, 20000)
+    return cg.SessionDesc(width=HEAVY["w"], height=HEAVY["h"], max_iterations=HEAVY["max_iter"],
+                          max_super_sampling=4.0, flags=FLAGS_ADAPTIVE, fractal=cg.MANDELBROT,
+                          arith=cg.ARITH_PARITY, center_x=t[0], center_y=t[1], span=1e-10 / 2, target_x=t[0],
+                          target_y=t[1], zoom_per_frame=1.02)
+
+
+def test_launch_time_limit_stops_frames(cuda):
+    """A launch that runs past frame_time_limit_s stops taking tiles: its frame
+    ends with CHAOS_ERR_TIMEOUT well before the frame's full time, and the
+    next frames render correctly."""
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import default_palette
+    pal = default_palette()
+    srv = cg.Server(4 << 30, pal)
+    srv.configure(frame_time_limit_s=0.005)
+    sid = srv.open(_heavy(cg))
+    srv.submit(sid)
+    srv.drain()
+    r = srv.records()[0]
+    assert r[6] == 7, r  # CHAOS_ERR_TIMEOUT
+    assert r[7] < 500.0, r  # the full frame takes seconds
+    srv.configure(frame_time_limit_s=0.0)
+    small = desc(cg, 256, 144, SESSIONS[0][2])
+    s2 = srv.open(small)
+    for _ in range(3):
+        srv.submit(s2)
+    srv.drain()
+    img, iters = srv.read(s2)
+    want, want_iters = _alone(cg, small, 3, pal)
+    assert np.array_equal(img, want) and iters == want_iters
+    assert all(r[6] == 0 for r in srv.records()[1:])
+    srv.close()
+
+
+def test_close_cancels_frames_on_the_gpu(cuda):
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import default_palette
+    pal = default_palette()
+    srv = cg.Server(4 << 30, pal)
+    sid = srv.open(_heavy(cg))
+    srv.submit(sid)
+    _wait_queue(srv, lambda waiting, in_flight: in_flight == 1)
+    t0 = time.time()
+    srv.close_session(sid)
+    closed_in = time.time() - t0
+    r = srv.records()[0]
+    assert r[6] == 5, r  # CHAOS_ERR_STATE: cancelled
+    assert closed_in < 1.0 and r[7] < 1000.0, (closed_in, r)
+    assert srv.usage()[0] == 0
+    small = desc(cg, 256, 144, SESSIONS[1][2])
+    s2 = srv.open(small)
+    srv.submit(s2)
+    srv.drain()
+    img, iters = srv.read(s2)
+    want, want_iters = _alone(cg, small, 1, pal)
+    assert np.array_equal(img, want) and iters == want_iters
     srv.close()
 
 
@@ -124,7 +263,7 @@ def test_trace_replay_records_latency(cuda):
     for sid in ids:
         mine = [r for r in recs if r[0] == sid]
         assert [r[1] for r in mine] == list(range(len(mine)))
-        assert all(r[4] >= r[2] >= 0 for r in mine)
+        assert all(r[4] >= r[3] >= r[2] >= 0 and r[6] == 0 and r[7] > 0 for r in mine)
     srv.close()
 
 
