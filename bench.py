@@ -1306,13 +1306,26 @@ def measure_c5(seconds=10.0, compact=False, n_cap=40):
     t1 = srv.clock()
     clk = clocks.stop()
     recs = srv.records()[warm:]
-    lat = np.array([(r[4] - r[2]) * 1e3 for r in recs])
-    lat1080 = np.array([(r[4] - r[2]) * 1e3 for r in recs if shapes[r[0]] == (1920, 1080)])
+    ok = [r for r in recs if r[6] == 0]
+    lat = np.array([(r[4] - r[2]) * 1e3 for r in ok])
+    queue_ms = np.array([(r[3] - r[2]) * 1e3 for r in ok])
+    render_ms = np.array([(r[4] - r[3]) * 1e3 for r in ok])
+    lat1080 = np.array([(r[4] - r[2]) * 1e3 for r in ok if shapes[r[0]] == (1920, 1080)])
     iters = sum(srv.read(sid)[1] for sid in sids) - it0
     value = iters / (t1 - t0) / 1e9
+    precisions = {name: sum(1 for r in recs if r[5] == p) for name, p in
+                  (("binary32", cg.PRECISION_SINGLE), ("binary64", cg.PRECISION_DOUBLE),
+                   ("perturbation", cg.PRECISION_TOO_BIG))}
 
     def pct(a, q):
         return float(np.percentile(a, q)) if len(a) else None
+
+    # the served frames against the FP64 oracle: each session's last frame
+    # rendered again from the same previous records in binary64 with the
+    # reference's rounding (the library's parity path, identical to the
+    # reference's --fmad=false kernel); escape values compared on the pixels
+    # both renders sampled afresh (reused pixels hold filtered values)
+    mism = served_vs_fp64_oracle(srv, sids, shapes)
 
     # capacity: every session asks for n_cap more frames at once (a saturated server)
     it1 = sum(srv.read(sid)[1] for sid in sids)
@@ -1339,9 +1352,66 @@ def measure_c5(seconds=10.0, compact=False, n_cap=40):
            "trace_s": t1 - t0, "value": value, "unit": "Gpixel-iter/s", "pixel_iterations": iters,
            "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": float(lat.max()) if len(lat) else None,
                           "p50_1080p": pct(lat1080, 50), "p99_1080p": pct(lat1080, 99)},
+           "queueing_delay_ms": {"p50": pct(queue_ms, 50), "p99": pct(queue_ms, 99),
+                                 "what": "admission into a launch - arrival"},
+           "render_ms": {"p50": pct(render_ms, 50), "p99": pct(render_ms, 99),
+                         "what": "finished - admitted (the launch's GPU queue and run)"},
+           "frames_not_ok": len(recs) - len(ok), "precision_of_frames": precisions,
+           "served_vs_fp64_oracle": mism,
            "capacity": capacity, "clocks": clk}
     srv.close()
     return out
+
+
+def served_vs_fp64_oracle(srv, sids, shapes):
+    """Escape-value mismatch of each session's latest served frame against the
+    same frame in binary64 with the reference's rounding, over the pixels both
+    sampled afresh (not reused)."""
+    import numpy as np
+    import torch
+
+    import chaos_gb300 as cg
+    from chaos_gb300.dropin import Driver, pitched, read_pixels
+    drv = Driver()
+    module = cg.Module("mandelbrot")
+    fresh_total, differ, reused_total, pixels = 0, 0, 0, 0
+    per_prec = {}
+    for sid in sids:
+        st = srv.frame_state(sid)
+        if st["precision"] == cg.PRECISION_TOO_BIG:
+            continue
+        w, h = shapes[sid]
+        served = drv.read_pixels(st["pixels"], st["pixels_pitch"], w, h)
+        buf, pitch = pitched(torch, w, h)
+        if st["advanced"]:
+            module.render_advanced(buf.data_ptr(), pitch, w, h, st["rect"], st["max_iterations"],
+                                   st["max_super_sampling"], st["flags"], st["rect_reused"], st["previous"],
+                                   st["previous_pitch"], (st["focus_x"], st["focus_y"]), double=True,
+                                   arith=cg.ARITH_PARITY)
+        else:
+            module.render_main(buf.data_ptr(), pitch, w, h, st["rect"], st["max_iterations"],
+                               st["max_super_sampling"], st["flags"], double=True, arith=cg.ARITH_PARITY)
+        torch.cuda.synchronize()
+        ref = read_pixels(buf, w)
+        fresh = (served["is_reused"] == 0) & (ref["is_reused"] == 0)
+        d = int((fresh & (served["value"].view(np.uint32) != ref["value"].view(np.uint32))).sum())
+        f = int(fresh.sum())
+        fresh_total += f
+        differ += d
+        reused_total += int((served["is_reused"] != 0).sum())
+        pixels += w * h
+        name = {cg.PRECISION_SINGLE: "binary32", cg.PRECISION_DOUBLE: "binary64"}[st["precision"]]
+        a = per_prec.setdefault(name, [0, 0])
+        a[0] += d
+        a[1] += f
+        del buf
+    module.close()
+    return {"what": "each session's latest frame vs the same frame in binary64 with the reference's rounding "
+                    "(the FP64 oracle's arithmetic), escape values of the pixels both sampled afresh",
+            "fresh_pixels": fresh_total, "reused_fraction": reused_total / max(pixels, 1),
+            "escape_value_mismatch_rate": differ / max(fresh_total, 1),
+            "by_precision": {k: {"mismatch_rate": v[0] / max(v[1], 1), "fresh_pixels": v[1]}
+                             for k, v in per_prec.items()}}
 
 
 def run_serve(args):

@@ -92,6 +92,17 @@ class Driver:
         self._check(self.cu.cuMemcpyHtoD_v2(C.c_uint64(ptr), buf, C.c_size_t(size)), "cuMemcpyHtoD")
         return size
 
+    def read(self, ptr, nbytes):
+        """Copy nbytes of device memory at ptr to a new bytes object (cuMemcpyDtoH)."""
+        buf = C.create_string_buffer(nbytes)
+        self._check(self.cu.cuMemcpyDtoH_v2(buf, C.c_uint64(ptr), C.c_size_t(nbytes)), "cuMemcpyDtoH")
+        return buf.raw
+
+    def read_pixels(self, ptr, pitch, w, h):
+        """A pitched w x h array of pixel records at device address ptr -> (h, w) numpy array."""
+        raw = np.frombuffer(self.read(ptr, pitch * h), dtype=np.uint8).reshape(h, pitch)
+        return np.ascontiguousarray(raw[:, : 16 * w]).view(PIXEL_DTYPE).reshape(h, w)
+
     def launch(self, fn, grid, block, params, sync=True):
         """params: list of ctypes objects; kernelParams[i] = &params[i] (Pointer.to(...) in JCuda).
         The launch goes to the legacy default stream, like JCuda's."""

@@ -266,6 +266,8 @@ using Clock = std::chrono::steady_clock;
 constexpr uint32_t kRecordRing = 1u << 16;
 constexpr int kForkStreams = 4;
 constexpr int kMaxLaunchSlots = 4;
+constexpr uint32_t kMaxSessions = 4096;  // session slots (reused once released)
+constexpr uint32_t kMaxDeepPerLaunch = 16;
 
 enum RecordState : uint8_t { REC_FREE = 0, REC_WAITING, REC_ADMITTED, REC_DONE };
 
@@ -294,7 +296,7 @@ struct Session {
     uint32_t submitted = 0;                    // frames requested so far
     uint32_t waiting = 0, in_flight = 0;
     bool in_forming = false;                   // has a frame in the launch being built
-    uint32_t *cancel_host = nullptr;           // host-mapped cancel word
+    volatile uint32_t *cancel_host = nullptr;  // this slot's host-mapped cancel word
     const volatile uint32_t *cancel_dev = nullptr;
     chaos_served_frame last{};                 // the latest admitted frame
     bool last_valid = false;
@@ -361,10 +363,13 @@ struct chaos_server {
     uint64_t next_record = 0;
     uint32_t in_flight = 0;
     std::deque<std::unique_ptr<Launch>> launches;
+    std::vector<std::unique_ptr<Launch>> failed_launches;
     uint64_t launch_seq = 0;
     LaunchSlot slots[kMaxLaunchSlots];
     cudaStream_t stream = nullptr, fork[kForkStreams] = {};
     std::vector<chaos_orbit *> retired_orbits;  // freed by the scheduler once their launches ended
+    uint32_t *cancel_words = nullptr;           // pinned, mapped: one per session slot
+    uint32_t *cancel_words_dev = nullptr;
 
     std::thread scheduler;
     bool stop = false;
@@ -390,8 +395,9 @@ namespace {
 void CUDART_CB launch_done(void *p)
 {
     Launch *l = static_cast<Launch *>(p);
-    l->done_at.store(l->server->now());
-    l->server->poke();
+    chaos_server *srv = l->server;  // `l` may be reaped as soon as done_at is set
+    l->done_at.store(srv->now());
+    srv->poke();
 }
 
 void release_session_locked(chaos_server *srv, Session &s)
@@ -407,9 +413,6 @@ void release_session_locked(chaos_server *srv, Session &s)
     s.resident = false;
     if (s.orbit) srv->retired_orbits.push_back(s.orbit);
     s.orbit = nullptr;
-    if (s.cancel_host) cudaFreeHost(s.cancel_host);
-    s.cancel_host = nullptr;
-    s.cancel_dev = nullptr;
     s.open = false;
     s.closing = false;
     s.last_valid = false;
@@ -432,9 +435,13 @@ void reap_locked(chaos_server *srv)
         Launch &l = *srv->launches.front();
         LaunchSlot &sl = srv->slots[l.slot];
         if (!l.failed) {
-            cudaError_t q = cudaEventQuery(sl.ev1);
-            if (q == cudaErrorNotReady) break;
-            if (q != cudaSuccess) l.failed = true;
+            // the completion callback runs after the launch's last operation;
+            // until it has, the Launch stays alive
+            if (l.done_at.load() < 0) {
+                cudaError_t q = cudaEventQuery(sl.ev1);
+                if (q == cudaErrorNotReady || q == cudaSuccess) break;
+                l.failed = true;  // the stream failed: the callback never runs
+            }
         }
         float gpu_ms = 0.f;
         if (!l.failed) cudaEventElapsedTime(&gpu_ms, sl.ev0, sl.ev1);
@@ -454,6 +461,8 @@ void reap_locked(chaos_server *srv)
             if (s.closing && s.in_flight == 0 && s.waiting == 0) release_session_locked(srv, s);
         }
         sl.busy = false;
+        // a failed launch's callback may still run: keep it until the server goes
+        if (l.failed) srv->failed_launches.push_back(std::move(srv->launches.front()));
         srv->launches.pop_front();
         any = true;
     }
@@ -784,6 +793,7 @@ bool admit_and_launch(chaos_server *srv, std::unique_lock<std::mutex> &lk)
         if (!srv->slots[k].busy) free_launch++;
     if (!free_launch) return false;
     Forming fm;
+    uint32_t n_deep = 0;
     bool memory_blocked = false;  // an earlier request waits for memory: no later one overtakes it for memory
     for (auto it = srv->waiting.begin(); it != srv->waiting.end();) {
         if (fm.items.size() >= SERVE_MAX_FRAMES) break;
@@ -855,7 +865,19 @@ bool admit_and_launch(chaos_server *srv, std::unique_lock<std::mutex> &lk)
         Forming::Item item{};
         item.record = *it;
         item.session = rc.r.session;
+        {
+            Session probe = s;
+            double r[4];
+            int prec;
+            bool deep;
+            advance_zoom(probe, r, prec, deep);
+            if (deep && n_deep >= kMaxDeepPerLaunch) {  // one work counter each; the rest go next launch
+                ++it;
+                continue;
+            }
+        }
         advance_zoom(s, item.rect, item.prec, item.deep);
+        if (item.deep) n_deep++;
         item.fast = s.has_prev;
         if (item.deep) {
             // perturbation: offset of the frame centre from the target, pixel size
@@ -970,6 +992,11 @@ int chaos_server_create(size_t hbm_budget_bytes, const uint32_t *palette, uint32
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     for (int k = 0; k < kForkStreams && e == cudaSuccess; k++)
         e = cudaStreamCreateWithFlags(&s->fork[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&s->cancel_words, kMaxSessions * sizeof(uint32_t), cudaHostAllocMapped);
+    if (e == cudaSuccess) {
+        std::memset(s->cancel_words, 0, kMaxSessions * sizeof(uint32_t));
+        e = cudaHostGetDevicePointer((void **)&s->cancel_words_dev, s->cancel_words, 0);
+    }
     if (e == cudaSuccess) e = cudaMalloc(&s->palette, palette_len * sizeof(uint32_t));
     if (e == cudaSuccess)
         e = cudaMemcpy(s->palette, palette, palette_len * sizeof(uint32_t), cudaMemcpyHostToDevice);
@@ -1045,17 +1072,6 @@ int chaos_server_open(chaos_server *s, const chaos_session_desc *d, uint32_t *se
         return api_fail(CHAOS_ERR_OUT_OF_MEMORY, "session needs %zu bytes, the whole budget is %zu", bytes, s->budget);
     std::unique_ptr<Session> ss(new (std::nothrow) Session());
     if (!ss) return api_fail(CHAOS_ERR_OUT_OF_MEMORY, "out of host memory");
-    cudaError_t e = cudaHostAlloc((void **)&ss->cancel_host, sizeof(uint32_t), cudaHostAllocMapped);
-    if (e == cudaSuccess) {
-        *ss->cancel_host = 0;
-        uint32_t *dp = nullptr;
-        e = cudaHostGetDevicePointer((void **)&dp, ss->cancel_host, 0);
-        ss->cancel_dev = dp;
-    }
-    if (e != cudaSuccess) {
-        if (ss->cancel_host) cudaFreeHost(ss->cancel_host);
-        return api_fail(CHAOS_ERR_CUDA, "session cancel word: %s", cudaGetErrorString(e));
-    }
     ss->d = *d;
     ss->bytes = bytes;
     ss->open = true;
@@ -1071,6 +1087,10 @@ int chaos_server_open(chaos_server *s, const chaos_session_desc *d, uint32_t *se
     while (id < s->sessions.size() &&
            (s->sessions[id]->open || s->sessions[id]->in_flight || s->sessions[id]->reading))
         id++;
+    if (id >= kMaxSessions) return api_fail(CHAOS_ERR_OUT_OF_MEMORY, "%u sessions are open", kMaxSessions);
+    ss->cancel_host = s->cancel_words + id;
+    ss->cancel_dev = s->cancel_words_dev + id;
+    *ss->cancel_host = 0u;
     if (id == s->sessions.size()) {
         s->sessions.push_back(std::move(ss));
     } else {
@@ -1101,7 +1121,7 @@ int chaos_server_close(chaos_server *s, uint32_t session)
     ss->waiting = 0;
     ss->closing = true;
     if (ss->in_flight) {
-        *reinterpret_cast<volatile uint32_t *>(ss->cancel_host) = 1u;
+        *ss->cancel_host = 1u;
         s->poke();
         const uint64_t gen = ss->generation;
         if (!wait_locked(s, lk, [&] { return !ss->open || ss->generation != gen; }))
@@ -1269,7 +1289,7 @@ int chaos_server_destroy(chaos_server *s)
             for (auto &ss : s->sessions)
                 if (ss && ss->open) {
                     ss->waiting = 0;
-                    if (ss->cancel_host) *reinterpret_cast<volatile uint32_t *>(ss->cancel_host) = 1u;
+                    if (ss->cancel_host) *ss->cancel_host = 1u;
                 }
         }
         s->poke();
@@ -1297,6 +1317,7 @@ int chaos_server_destroy(chaos_server *s)
         if (s->fork[k]) cudaStreamDestroy(s->fork[k]);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->palette) cudaFree(s->palette);
+    if (s->cancel_words) cudaFreeHost(s->cancel_words);
     delete s;
     return CHAOS_OK;
 }
