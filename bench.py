@@ -1314,8 +1314,8 @@ def measure_c5(seconds=10.0, compact=False, n_cap=40):
     iters = sum(srv.read(sid)[1] for sid in sids) - it0
     value = iters / (t1 - t0) / 1e9
     precisions = {name: sum(1 for r in recs if r[5] == p) for name, p in
-                  (("binary32", cg.PRECISION_SINGLE), ("binary64", cg.PRECISION_DOUBLE),
-                   ("perturbation", cg.PRECISION_TOO_BIG))}
+                  (("binary32", cg.PRECISION_SINGLE), ("floatfloat", cg.PRECISION_FLOATFLOAT),
+                   ("binary64", cg.PRECISION_DOUBLE), ("perturbation", cg.PRECISION_TOO_BIG))}
 
     def pct(a, q):
         return float(np.percentile(a, q)) if len(a) else None
@@ -1400,7 +1400,8 @@ def served_vs_fp64_oracle(srv, sids, shapes):
         differ += d
         reused_total += int((served["is_reused"] != 0).sum())
         pixels += w * h
-        name = {cg.PRECISION_SINGLE: "binary32", cg.PRECISION_DOUBLE: "binary64"}[st["precision"]]
+        name = {cg.PRECISION_SINGLE: "binary32", cg.PRECISION_DOUBLE: "binary64",
+                cg.PRECISION_FLOATFLOAT: "floatfloat"}[st["precision"]]
         a = per_prec.setdefault(name, [0, 0])
         a[0] += d
         a[1] += f

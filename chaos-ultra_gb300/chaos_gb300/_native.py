@@ -37,6 +37,7 @@ ARITH_CONTRACTED = 2  # the reference module as nvcc builds it by default (refer
 PRECISION_SINGLE = 0
 PRECISION_DOUBLE = 1
 PRECISION_TOO_BIG = 2
+PRECISION_FLOATFLOAT = 3  # served frames: binary64 by the selector, escape loop in float-float
 
 SAMPLES_CENTER = 0
 SAMPLES_JITTER = 1

@@ -38,7 +38,10 @@ static_assert(sizeof(PixelInfo) == 16, "pixel_info_t is 16 bytes");
 // the sample's x coordinate fma(px + dx, psx, lbx), and in the reuse path
 // the warp to the old frame, the filter's chain of products and the blend.  The
 // squares x*x and y*y feed both the test and x' and stay rounded.
-enum Arith { ARITH_PARITY = 0, ARITH_FMA = 1, ARITH_CONTRACTED = 2 };
+// ARITH_FLOATFLOAT (binary64 frames only): the escape loop in float-float
+// (ff_step, about 48 bits on the binary32 pipe) from the binary64 sample
+// point; the sampling geometry stays binary64.
+enum Arith { ARITH_PARITY = 0, ARITH_FMA = 1, ARITH_CONTRACTED = 2, ARITH_FLOATFLOAT = 3 };
 enum FractalKind {
     FRACTAL_MANDELBROT = 0,
     FRACTAL_JULIA = 1,
@@ -331,11 +334,124 @@ template <class R> __device__ __forceinline__ bool blockable_c(R cx, R cy)
     return radius2<R, ARITH_PARITY>(cx, cy) <= R(3.99);
 }
 
+// ---------------------------------------------------------------------------
+// float-float: a value hi + lo of two binary32 numbers (|lo| <= ulp(hi)/2),
+// about 48 significant bits on the binary32 pipe.  Error-free transformations
+// after Knuth (TwoSum), Dekker (Fast2Sum) and the fma-based TwoProd; the
+// compositions are the usual double-word ones (Hida, Li, Bailey 2001).
+// ---------------------------------------------------------------------------
+struct FF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b)  // |a| >= |b|
+{
+    float s = __fadd_rn(a, b);
+    float e = __fsub_rn(b, __fsub_rn(s, a));
+    return FF{s, e};
+}
+
+__host__ __device__ __forceinline__ FF ff_from_double(double d)
+{
+    float hi = (float)d;
+    float lo = (float)(d - (double)hi);
+    return FF{hi, lo};
+}
+
+// Knuth's two-sum: s + err == a + b exactly.
+__device__ __forceinline__ float ff_two_sum(float a, float b, float &err)
+{
+    float s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+}
+
+// One z <- z^2 + c step in float-float, 43 binary32 operations.  The three
+// products stay unnormalised (leading product + error term by fused
+// multiply-add), the leading terms meet in two-sums, all error terms are
+// summed in one fixed order, and each coordinate is normalised once at the
+// end:
+//   x' = fast_two_sum(t, ((ex - ey) + e1) + e2 + cx.lo),
+//        s = two_sum(px, -py; e1), t = two_sum(s, cx.hi; e2)
+//   y' = fast_two_sum(u, fma(2, exy, e3) + cy.lo),  u = two_sum(2 pxy, cy.hi; e3)
+__device__ __forceinline__ void ff_step(FF &x, FF &y, FF cx, FF cy)
+{
+    const float px = __fmul_rn(x.hi, x.hi);
+    float ex = __fmaf_rn(x.hi, x.hi, -px);
+    ex = __fmaf_rn(__fadd_rn(x.hi, x.hi), x.lo, ex);
+    const float py = __fmul_rn(y.hi, y.hi);
+    float ey = __fmaf_rn(y.hi, y.hi, -py);
+    ey = __fmaf_rn(__fadd_rn(y.hi, y.hi), y.lo, ey);
+    const float pxy = __fmul_rn(x.hi, y.hi);
+    float exy = __fmaf_rn(x.hi, y.hi, -pxy);
+    exy = __fmaf_rn(x.hi, y.lo, exy);
+    exy = __fmaf_rn(x.lo, y.hi, exy);
+
+    float e1, e2, e3;
+    const float s = ff_two_sum(px, -py, e1);
+    const float t = ff_two_sum(s, cx.hi, e2);
+    float e = __fsub_rn(ex, ey);
+    e = __fadd_rn(e, e1);
+    e = __fadd_rn(e, e2);
+    e = __fadd_rn(e, cx.lo);
+    const FF xn = ff_fast_two_sum(t, e);
+
+    const float u = ff_two_sum(__fadd_rn(pxy, pxy), cy.hi, e3);
+    const float f = __fadd_rn(__fmaf_rn(2.f, exy, e3), cy.lo);
+    y = ff_fast_two_sum(u, f);
+    x = xn;
+}
+
+__device__ __forceinline__ float ff_radius2(FF x, FF y) { return __fmaf_rn(x.hi, x.hi, __fmul_rn(y.hi, y.hi)); }
+
+// The escape loop of escape() in float-float: blocks of ESCAPE_BLOCK untested
+// steps while |c| <= 1.9975 (after an escape the leading words grow until
+// they overflow, so a block whose last state tests below 4 holds no escape),
+// the rest one tested step at a time.  The test reads the leading words, as
+// the batched float-float tier's does; the count is the first step index
+// whose state tests >= 4, so both give the same count for the same c.
+__device__ __forceinline__ uint32_t escape_ff(uint32_t max_iter, FF x, FF y, FF cx, FF cy, bool blockable)
+{
+    if (max_iter == 0u || !(ff_radius2(x, y) < 4.f)) return 0u;
+    uint32_t i = 0;
+    if (blockable) {
+        while (max_iter - i >= (uint32_t)ESCAPE_BLOCK) {
+            const FF sx = x, sy = y;
+#pragma unroll
+            for (int k = 0; k < ESCAPE_BLOCK; k++) ff_step(x, y, cx, cy);
+            if (!(ff_radius2(x, y) < 4.f)) {
+                x = sx;
+                y = sy;
+                break;
+            }
+            i += ESCAPE_BLOCK;
+        }
+    }
+    while (i < max_iter) {
+        ff_step(x, y, cx, cy);
+        ++i;
+        if (!(ff_radius2(x, y) < 4.f)) break;
+    }
+    return i;
+}
+
+
 // computeFractal (mandelbrot.cu:11-25, julia.cu:5-17) as an unsigned escape
 // value: Mandelbrot maps an interior point (i == maxIterations) to 0, Julia
 // returns i.  `jc` is julia_c already converted to Real.
 template <class R, int A, int F> __device__ __forceinline__ uint32_t compute_fractal(uint32_t max_iter, R px, R py, R jcx, R jcy)
 {
+    if constexpr (A == ARITH_FLOATFLOAT) {
+        static_assert(sizeof(R) == 8, "float-float escape loops start from binary64 points");
+        const FF fx = ff_from_double(px), fy = ff_from_double(py);
+        if (F == FRACTAL_MANDELBROT) {
+            const uint32_t i = escape_ff(max_iter, FF{0.f, 0.f}, FF{0.f, 0.f}, fx, fy, blockable_c(fx.hi, fy.hi));
+            return i == max_iter ? 0u : i;
+        }
+        const FF jx = ff_from_double(jcx), jy = ff_from_double(jcy);
+        return escape_ff(max_iter, fx, fy, jx, jy, blockable_c(jx.hi, jy.hi));
+    }
     R r2;
     if (F == FRACTAL_MANDELBROT) {
         // from z1 = c, the first step's exact result (+0 in place of -0)

@@ -65,7 +65,14 @@ int api_perturb_enqueue(const chaos_frame_desc *desc, const chaos_orbit *orbit, 
 // ---------------------------------------------------------------------------
 
 constexpr uint32_t SERVE_MAX_FRAMES = 256;  // frames per launch
-constexpr uint32_t SERVE_GROUPS = 24;       // frame kind x precision x arithmetic x fractal
+constexpr uint32_t SERVE_GROUPS = 32;       // frame kind x precision x arithmetic x fractal
+
+// Kernel group of a frame: ((renderFast * 2 + binary64) * 4 + arithmetic) * 2 + fractal.
+__host__ __device__ constexpr uint32_t serve_group(bool adv, bool dbl, int arith, int fractal)
+{
+    return ((((adv ? 1u : 0u) * 2u + (dbl ? 1u : 0u)) * 4u + (uint32_t)arith) * 2u) + (uint32_t)fractal;
+}
+__host__ __device__ constexpr bool group_binary64(uint32_t g) { return (g / 8u) % 2u == 1u; }
 constexpr uint32_t SERVE_STATUS_CANCELLED = 1u, SERVE_STATUS_TIMEOUT = 2u;
 
 template <class R> struct ServeFrame {
@@ -228,15 +235,14 @@ static cudaError_t launch_serve_t(const ServeFrame<R> *frames, const uint32_t *b
     return cudaGetLastError();
 }
 
-// group = renderFast * 12 + precision (0 binary32, 1 binary64) * 6 + arithmetic * 2 + fractal
 template <class R>
 static cudaError_t launch_serve(uint32_t group, const ServeFrame<R> *frames, const uint32_t *begin,
                                 uint32_t n_frames, uint32_t n_jobs, uint32_t *counter, uint32_t *status,
                                 unsigned long long *const *totals, unsigned long long budget_ns, int sms,
                                 cudaStream_t s)
 {
-    const uint32_t a = (group % 6u) / 2u, f = group % 2u;
-    const bool adv = group >= 12u;
+    const uint32_t a = (group / 2u) % 4u, f = group % 2u;
+    const bool adv = group >= 16u;
 #define CHAOS_SERVE_CASE(AA, FF)                                                                                    \
     if (a == AA && f == FF)                                                                                         \
         return adv ? launch_serve_t<R, AA, FF, true>(frames, begin, n_frames, n_jobs, counter, status, totals,      \
@@ -249,6 +255,10 @@ static cudaError_t launch_serve(uint32_t group, const ServeFrame<R> *frames, con
     CHAOS_SERVE_CASE(ARITH_FMA, FRACTAL_JULIA)
     CHAOS_SERVE_CASE(ARITH_CONTRACTED, FRACTAL_MANDELBROT)
     CHAOS_SERVE_CASE(ARITH_CONTRACTED, FRACTAL_JULIA)
+    if constexpr (sizeof(R) == 8) {
+        CHAOS_SERVE_CASE(ARITH_FLOATFLOAT, FRACTAL_MANDELBROT)
+        CHAOS_SERVE_CASE(ARITH_FLOATFLOAT, FRACTAL_JULIA)
+    }
 #undef CHAOS_SERVE_CASE
     return cudaErrorInvalidValue;
 }
@@ -541,7 +551,13 @@ void advance_zoom(Session &s, double rect[4], int &prec, bool &deep)
     }
     rect_of(s, rect);
     prec = chaos_select_precision(rect, d.width, d.height);
-    if (prec == CHAOS_PRECISION_SINGLE && (d.flags & CHAOS_SESSION_FLAG_BINARY64)) prec = CHAOS_PRECISION_DOUBLE;
+    if (d.flags & CHAOS_SESSION_FLAG_BINARY64) {
+        if (prec == CHAOS_PRECISION_SINGLE) prec = CHAOS_PRECISION_DOUBLE;
+    } else if (prec == CHAOS_PRECISION_DOUBLE && d.arith == CHAOS_ARITH_FMA) {
+        // float-float while the pixel is at least 2^-42 of the plane's magnitude
+        const double m = std::max(std::max(std::fabs(s.cx), std::fabs(s.cy)), 1.0 / 256.0);
+        if (s.span / d.width >= std::ldexp(m, -42)) prec = CHAOS_PRECISION_FLOATFLOAT;
+    }
     deep = prec == CHAOS_PRECISION_TOO_BIG && d.fractal == 0 && s.span / d.width >= 1e-290;
 }
 
@@ -621,7 +637,7 @@ int enqueue_launch_locked(chaos_server *srv, Forming &fm)
         if (!it.deep) n_group[it.group]++;
     uint32_t n32 = 0, n64 = 0;
     for (uint32_t g = 0; g < SERVE_GROUPS; g++) {
-        if (g % 12u < 6u) {
+        if (!group_binary64(g)) {
             first_of[g] = n32;
             n32 += n_group[g];
         } else {
@@ -644,7 +660,7 @@ int enqueue_launch_locked(chaos_server *srv, Forming &fm)
         if (!it.deep) {
             const uint32_t g = it.group;
             const uint32_t idx = first_of[g] + fill[g]++;
-            if (g % 12u < 6u)
+            if (!group_binary64(g))
                 fill_frame<float>(T.f32[idx], s, it.rect, it.fast, k, flags);
             else
                 fill_frame<double>(T.f64[idx], s, it.rect, it.fast, k, flags);
@@ -671,7 +687,7 @@ int enqueue_launch_locked(chaos_server *srv, Forming &fm)
         uint32_t acc = 0;
         for (uint32_t j = 0; j < n_group[g]; j++) {
             T.job_begin[g][j] = acc;
-            if (g % 12u < 6u) {
+            if (!group_binary64(g)) {
                 T.f32[first_of[g] + j].chunk = chunk;
                 acc += (T.f32[first_of[g] + j].a.m.n_tiles + chunk - 1) / chunk;
             } else {
@@ -706,7 +722,7 @@ int enqueue_launch_locked(chaos_server *srv, Forming &fm)
         cudaStream_t fs = srv->fork[used_forks % kForkStreams];
         if (used_forks < kForkStreams) e = cudaStreamWaitEvent(fs, sl.table_ready, 0);
         if (e != cudaSuccess) break;
-        if (g % 12u < 6u)
+        if (!group_binary64(g))
             e = launch_serve<float>(g, sl.dev->f32 + first_of[g], sl.dev->job_begin[g], n_group[g], n_jobs,
                                     &sl.dev->counters[g], sl.dev->status, sl.totals_dev, budget_ns, srv->sms, fs);
         else
@@ -887,9 +903,8 @@ bool admit_and_launch(chaos_server *srv, std::unique_lock<std::mutex> &lk)
             item.rect[3] = 0;
             item.prec = CHAOS_PRECISION_TOO_BIG;
         } else {
-            const uint32_t p = item.prec == CHAOS_PRECISION_SINGLE ? 0u : 1u;
-            item.group = (item.fast ? 12u : 0u) + p * 6u + (uint32_t)internal_arith(s.d.arith) * 2u +
-                         (s.d.fractal == 1 ? 1u : 0u);
+            const int arith = item.prec == CHAOS_PRECISION_FLOATFLOAT ? ARITH_FLOATFLOAT : internal_arith(s.d.arith);
+            item.group = serve_group(item.fast, item.prec != CHAOS_PRECISION_SINGLE, arith, s.d.fractal == 1 ? 1 : 0);
         }
         // bookkeeping of the admitted frame: the served-frame view, the swap
         double plane[4];

@@ -164,6 +164,9 @@ int chaos_debug(chaos_module *m);
 #define CHAOS_PRECISION_SINGLE 0
 #define CHAOS_PRECISION_DOUBLE 1
 #define CHAOS_PRECISION_TOO_BIG 2
+/* Served frames only (chaos_frame_record.precision): a frame the selector puts
+ * in binary64, rendered with the escape loop in float-float. */
+#define CHAOS_PRECISION_FLOATFLOAT 3
 /* J/cudarenderer/RenderingKernel.java:124-138 + CudaFractalRenderer.updateFloatPrecision
  * (:409-419): single while the pixel is at least ulp((float)left_bottom) on both
  * axes, double below that, "too big" below ulp((double)left_bottom). */
@@ -369,7 +372,11 @@ int chaos_batch_destroy(chaos_batch *batch);
  * (sample reuse from the previous frame, foveation around the target's pixel
  * when CHAOS_FLAG_FOVEATION is set).  The precision of each frame is
  * chaos_select_precision's (binary32 where the reference's renderer would use
- * it) unless CHAOS_SESSION_FLAG_BINARY64 is set. */
+ * it), with two changes: a CHAOS_ARITH_FMA session runs the frames the
+ * selector puts in binary64 with the escape loop in float-float (sampling
+ * geometry in binary64; precision CHAOS_PRECISION_FLOATFLOAT) while the
+ * pixel is at least 2^-42 max(|cx|, |cy|, 1/256), and
+ * CHAOS_SESSION_FLAG_BINARY64 puts every frame in binary64. */
 typedef struct chaos_session_desc {
     uint32_t width, height;
     uint32_t max_iterations;

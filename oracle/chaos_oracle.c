@@ -49,6 +49,11 @@ float orc_newton_compute_f(int fractal, uint32_t max_iter, float x, float y, con
 float orc_newton_compute_d(int fractal, uint32_t max_iter, double x, double y, const double *roots,
                            const double *coeffs);
 enum { ORC_ARITH_FMA = 0, ORC_ARITH_PARITY = 1, ORC_ARITH_CONTRACTED = 2 }; /* same numbering as CHAOS_ARITH_* */
+/* Served float-float frames (binary64 kernels only): the escape loop of the
+ * library's ff_step from the binary64 sample point (chaos_device.cuh
+ * compute_fractal with ARITH_FLOATFLOAT). */
+enum { ORC_ARITH_FLOATFLOAT = 3 };
+static float orc_compute_fractal_ff(int fractal, uint32_t max_iter, double px, double py, double jcx, double jcy);
 
 /* kernel flag bits, gen.cu:157-161 */
 #define ORC_FLAG_ADAPTIVE_SS (1u << 0)
@@ -212,6 +217,7 @@ float orc_compute_fractal_d(int fractal, int arith, uint32_t max_iter, double px
     double r2;
     uint32_t i;
     if (fractal >= 2) return orc_newton_compute_d(fractal, max_iter, px, py, g_newton_roots, g_newton_coeffs);
+    if (arith == ORC_ARITH_FLOATFLOAT) return orc_compute_fractal_ff(fractal, max_iter, px, py, jcx, jcy);
     if (fractal == ORC_MANDELBROT) {
         i = esc_any_d(arith, max_iter, 0.0, 0.0, px, py, &r2);
         if (i == max_iter) return 0;
@@ -1193,6 +1199,34 @@ static void ff_step(ff_t *x, ff_t *y, ff_t cx, ff_t cy)
     float f = fmaf(2.f, exy, e3) + cy.lo;
     *y = ff_fast_two_sum(u, f);
     *x = xn;
+}
+
+static uint32_t esc_ff_from(uint32_t max_iter, ff_t x, ff_t y, ff_t cx, ff_t cy, float *r2_exit)
+{
+    uint32_t i = 0;
+    float r2;
+    for (;;) {
+        r2 = fmaf(x.hi, x.hi, y.hi * y.hi);
+        if (!(i < max_iter && r2 < 4.0f)) break;
+        ff_step(&x, &y, cx, cy);
+        ++i;
+    }
+    *r2_exit = r2;
+    return i;
+}
+
+/* computeFractal's escape value with the float-float loop: Mandelbrot from
+ * z = 0 (interior -> 0), Julia from z = point with c = julia_c. */
+static float orc_compute_fractal_ff(int fractal, uint32_t max_iter, double px, double py, double jcx, double jcy)
+{
+    float r2;
+    ff_t zero = {0.f, 0.f};
+    if (fractal == ORC_MANDELBROT) {
+        uint32_t i = esc_ff_from(max_iter, zero, zero, ff_from_double(px), ff_from_double(py), &r2);
+        return i == max_iter ? 0.f : (float)i;
+    }
+    return (float)esc_ff_from(max_iter, ff_from_double(px), ff_from_double(py), ff_from_double(jcx),
+                              ff_from_double(jcy), &r2);
 }
 
 static uint32_t esc_ff(uint32_t max_iter, ff_t cx, ff_t cy, float *r2_exit)

@@ -17,6 +17,7 @@ REF_LIB = os.path.join(HERE, "_ref", "libchaos_ref.so")
 
 MANDELBROT, JULIA = 0, 1
 ARITH_FMA, ARITH_PARITY, ARITH_CONTRACTED = 0, 1, 2  # same numbering as CHAOS_ARITH_* in include/chaos_gb300.h
+ARITH_FLOATFLOAT = 3  # reference-mode binary64 frames with the float-float escape loop (served frames)
 
 PIXEL_DTYPE = np.dtype([("value", "<f4"), ("weight", "<f4"), ("is_reused", "u1"), ("pad", "u1", 3),
                         ("weight_of_new_samples", "<f4")])

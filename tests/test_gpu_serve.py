@@ -88,6 +88,47 @@ def test_session_chain_matches_oracle(cuda, oracle):
     srv.close()
 
 
+def test_floatfloat_session_chain_matches_oracle(cuda, oracle):
+    """A CHAOS_ARITH_FMA session whose frames the selector puts in binary64
+    runs them with the float-float escape loop (precision FLOATFLOAT): its
+    renderQuality / renderFast chain equals the oracle's restatement with the
+    same float-float step."""
+    import chaos_gb300 as cg
+    from chaos_gb300.palette import default_palette
+    from oracle.oracle import ARITH_FLOATFLOAT, MANDELBROT
+    w, h, tgt, mi, span0 = 160, 96, (-0.7453, 0.1127), 1500, 4e-6
+    flags = FLAGS_ADAPTIVE | FLAGS_REUSE
+    pal = default_palette()
+    srv = cg.Server(1 << 28, pal)
+    center = (tgt[0] + 1e-6, tgt[1] - 5e-7)
+    sid = srv.open(desc(cg, w, h, tgt, max_iter=mi, flags=flags, span=span0, center=center))
+    cx, cy, span = center[0], center[1], span0
+    prev_pix, prev_rect = None, None
+    for f in range(4):
+        if f:
+            cx = tgt[0] + (cx - tgt[0]) / 1.02
+            cy = tgt[1] + (cy - tgt[1]) / 1.02
+            span /= 1.02
+        hw, hh = 0.5 * span, 0.5 * span * h / w
+        rect = (cx - hw, cy - hh, cx + hw, cy + hh)
+        assert cg.select_precision(rect, w, h) == cg.PRECISION_DOUBLE
+        if f == 0:
+            pix = oracle.render_main(MANDELBROT, True, ARITH_FLOATFLOAT, w, h, rect, mi, 2.0, flags & 1)
+        else:
+            fx = min(max((tgt[0] - rect[0]) / (rect[2] - rect[0]) * w, 0.0), w - 1.0)
+            fy = min(max((rect[3] - tgt[1]) / (rect[3] - rect[1]) * h, 0.0), h - 1.0)
+            pix = oracle.render_advanced(MANDELBROT, True, ARITH_FLOATFLOAT, w, h, rect, mi, 2.0, flags | 16 | 32,
+                                         prev_rect, prev_pix, (int(fx), int(fy)))
+        srv.submit(sid)
+        img, _ = srv.read(sid)
+        got = srv.frame_state(sid)
+        assert got["precision"] == cg.PRECISION_FLOATFLOAT
+        assert np.array_equal(img, oracle.compose(pix, pal, 2.0)), f
+        prev_pix, prev_rect = pix, rect
+    assert all(r[5] == cg.PRECISION_FLOATFLOAT for r in srv.records())
+    srv.close()
+
+
 def _wait_queue(srv, pred, limit=60.0):
     t0 = time.time()
     while not pred(*srv.queue()):
