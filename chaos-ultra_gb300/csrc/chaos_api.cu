@@ -23,6 +23,7 @@
 
 #include "../../include/chaos_gb300.h"
 #include "chaos_kernels.cuh"
+#include "chaos_trace.h"
 
 using namespace chaos;
 
@@ -457,6 +458,7 @@ template <class R>
 static int render_main(chaos_module *m, chaos_pixel_info *out, long pitch, uint32_t w, uint32_t h, const R rect[4],
                        uint32_t max_iter, float max_ss, uint32_t flags, int arith, cudaStream_t s, bool sync)
 {
+    TraceRange trace_("fractalRenderMain");
     if (!m || !rect) return fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL argument");
     int rc = check_size(w, h);
     if (rc) return rc;
@@ -490,6 +492,7 @@ static int render_advanced(chaos_module *m, chaos_pixel_info *out, long pitch, u
                            const chaos_pixel_info *in, long in_pitch, uint32_t fx, uint32_t fy, int arith,
                            cudaStream_t s, bool sync)
 {
+    TraceRange trace_("fractalRenderAdvanced");
     if (!m || !rect || !rect_reused) return fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL argument");
     int rc = check_size(w, h);
     if (rc) return rc;
@@ -563,6 +566,7 @@ static int compose_impl(chaos_module *m, const chaos_pixel_info *in, long pitch,
                         uint32_t w, uint32_t h, const uint32_t *palette, uint32_t palette_len, float max_ss,
                         cudaStream_t s, bool sync)
 {
+    TraceRange trace_("compose");
     if (!m) return fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL module");
     int rc = check_size(w, h);
     if (rc) return rc;
@@ -699,11 +703,13 @@ static int frame_entry(const chaos_frame_desc *dsc, const chaos_frame_out *o, cu
 
 int chaos_render_frame_async(const chaos_frame_desc *desc, const chaos_frame_out *out, void *stream)
 {
+    TraceRange trace_("chaos_render_frame");
     return frame_entry(desc, out, (cudaStream_t)stream, false);
 }
 
 int chaos_render_frame(const chaos_frame_desc *desc, const chaos_frame_out *out, void *stream)
 {
+    TraceRange trace_("chaos_render_frame");
     return frame_entry(desc, out, (cudaStream_t)stream, true);
 }
 
@@ -742,6 +748,7 @@ int grow(uint32_t **p, size_t *have, size_t need)
 int chaos_render_frame_host(const chaos_frame_desc *desc, const uint32_t *palette, uint32_t palette_len,
                             uint32_t interior_rgba, uint32_t *rgba_host, unsigned long long *total_host, void *stream)
 {
+    TraceRange trace_("chaos_render_frame_host");
     if (!desc || !palette || palette_len == 0 || !rgba_host)
         return fail(CHAOS_ERR_INVALID_ARGUMENT, "desc, palette and rgba_host are required");
     int rc = check_size(desc->width, desc->height);
@@ -947,6 +954,7 @@ int chaos_renderer_free_resources(chaos_renderer *r)
 
 int chaos_renderer_render_quality(chaos_renderer *r, chaos_rendering_model *model)
 {
+    TraceRange trace_("renderQuality");
     if (!r || !model) return fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL argument");
     if (!r->initialized) return fail(CHAOS_ERR_STATE, "Renderer has to be initialized first");
     int rc = check_model(model);
@@ -977,6 +985,7 @@ int chaos_renderer_render_quality(chaos_renderer *r, chaos_rendering_model *mode
 
 int chaos_renderer_render_fast(chaos_renderer *r, chaos_rendering_model *model)
 {
+    TraceRange trace_("renderFast");
     if (!r || !model) return fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL argument");
     if (!r->initialized) return fail(CHAOS_ERR_STATE, "Renderer has to be initialized first");
     int rc = check_model(model);

@@ -20,6 +20,7 @@
 
 #include "../../include/chaos_gb300.h"
 #include "chaos_frame.cuh"
+#include "chaos_trace.h"
 
 namespace chaos {
 
@@ -757,6 +758,7 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
 
 int chaos_batch_launch(chaos_batch *b, void *stream)
 {
+    TraceRange trace_("chaos_batch_launch");
     if (!b) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL batch");
     cudaError_t e = cudaGraphLaunch(b->exec, (cudaStream_t)stream);
     if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "cudaGraphLaunch: %s", cudaGetErrorString(e));

@@ -41,6 +41,7 @@
 #include "../../include/chaos_gb300.h"
 #include "bigfix.h"
 #include "chaos_kernels.cuh"
+#include "chaos_trace.h"
 
 namespace chaos {
 
@@ -493,6 +494,7 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
 int chaos_orbit_create(const char *center_x, const char *center_y, uint32_t bits, uint32_t max_iterations,
                        chaos_orbit **out)
 {
+    TraceRange trace_("chaos_orbit_create");
     if (!center_x || !center_y || !out) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL argument");
     if (max_iterations < 1) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "maxIterations must be a positive number");
     if (bits < 64 || bits > 64u * BIGFIX_MAX_LIMBS)
@@ -702,6 +704,7 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
 static int perturb_entry(const chaos_frame_desc *d, const chaos_orbit *orb, const chaos_frame_out *o, cudaStream_t s,
                          bool sync, uint32_t *counter = nullptr)
 {
+    TraceRange trace_("chaos_render_frame_perturb");
     if (!d || !orb || !o) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL argument");
     if (d->width == 0 || d->height == 0 || (uint64_t)d->width * d->height > (1ull << 31))
         return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "bad frame size %u x %u", d->width, d->height);

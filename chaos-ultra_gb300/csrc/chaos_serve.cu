@@ -52,6 +52,7 @@
 
 #include "../../include/chaos_gb300.h"
 #include "chaos_refmode.cuh"
+#include "chaos_trace.h"
 
 namespace chaos {
 int api_fail(int code, const char *fmt, ...);  // chaos_api.cu
@@ -614,6 +615,7 @@ struct Forming {
 // asynchronous CUDA calls).
 int enqueue_launch_locked(chaos_server *srv, Forming &fm)
 {
+    TraceRange trace_("chaos_server launch");
     int slot_id = -1;
     for (int k = 0; k < (int)srv->cfg.max_launches_in_flight && k < kMaxLaunchSlots; k++)
         if (!srv->slots[k].busy) {
