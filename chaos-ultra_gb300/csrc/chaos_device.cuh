@@ -660,17 +660,21 @@ __device__ __forceinline__ PixelInfo make_pixel(float value, float weight)
 }
 
 // fractalRenderMain for one lane of an 8x4 warp tile (gen.cu:168-181).
+// Returns the record stored for the lane's pixel (meaningful where the pixel
+// lies in the image).
 template <class R, int A, int F>
-__device__ __forceinline__ void render_main_tile(const SampleGeometry<R> &g, void *out, long pitch, UInt2 size,
-                                                 uint32_t x0, uint32_t y0, uint32_t lane, float max_ss, uint32_t flags,
-                                                 unsigned long long &iters)
+__device__ __forceinline__ PixelInfo render_main_tile(const SampleGeometry<R> &g, void *out, long pitch, UInt2 size,
+                                                      uint32_t x0, uint32_t y0, uint32_t lane, float max_ss,
+                                                      uint32_t flags, unsigned long long &iters)
 {
     UInt2 p = tile_pixel(x0, y0, lane);
     bool valid = p.x < size.x && p.y < size.y;
     float sc = max_ss;
     uint32_t result =
         sample_the_fractal<R, A, F>(g, p.x, p.y, sc, (flags & FLAG_ADAPTIVE_SS) != 0, valid, 0xffffffffu, iters);
-    if (valid) store_pixel(pixel_ptr(out, pitch, p.x, p.y), make_pixel((float)result, sc));
+    const PixelInfo rec = make_pixel((float)result, sc);
+    if (valid) store_pixel(pixel_ptr(out, pitch, p.x, p.y), rec);
+    return rec;
 }
 
 // ---------------------------------------------------------------------------
@@ -769,8 +773,9 @@ __device__ __forceinline__ void foveation(UInt2 p, UInt2 focus, float max_ss, fl
 
 // fractalRenderAdvanced for one lane of an 8x4 warp tile (gen.cu:307-368).
 // Lanes that reach the same sampleTheFractal call site vote together.
+// Returns the record stored for the lane's pixel.
 template <class R, int A, int F>
-__device__ __forceinline__ void render_advanced_tile(const SampleGeometry<R> &g, const Rect<R> &image,
+__device__ __forceinline__ PixelInfo render_advanced_tile(const SampleGeometry<R> &g, const Rect<R> &image,
                                                      const Rect<R> &image_reused, void *out, long pitch, UInt2 size,
                                                      const void *in, long in_pitch, UInt2 focus, uint32_t x0,
                                                      uint32_t y0, uint32_t lane, float max_ss, uint32_t flags,
@@ -822,6 +827,7 @@ __device__ __forceinline__ void render_advanced_tile(const SampleGeometry<R> &g,
         res.weight = sc;
     }
     if (valid) store_pixel(pixel_ptr(out, pitch, p.x, p.y), res);
+    return res;
 }
 
 // ---------------------------------------------------------------------------

@@ -16,13 +16,18 @@
 //      past the wait limit;
 //   3. it renders every admitted frame of all sessions in one launch: the
 //      frame table goes to the device in one copy, one persistent kernel per
-//      (precision, arithmetic, fractal) present pulls 8x4 tiles of all its
-//      frames from one work counter (the kernels of one launch run side by
-//      side on fork streams), perturbation frames follow, then one compose
-//      kernel colours every frame, and a host callback stamps completion.
-// Up to max_launches_in_flight launches are queued on the GPU at once, so a
-// request that arrives while a launch runs joins the next one (continuous
-// batching: new frames enter at launch granularity, each frame a few ms).
+//      (precision, arithmetic, fractal, frame kind) present pulls strips of
+//      8x4 tiles of all its frames from one work counter and composes each
+//      pixel as it stores it (the kernels of one launch run side by side on
+//      the launch slot's streams); perturbation frames and their compose
+//      follow, and a host callback marks the launch's end.
+// A frame completes as soon as the warp that finishes its last strip
+// publishes it (a done word in host-mapped memory), not when its launch
+// ends: the scheduler polls those words, so a small frame is not held back
+// by a large one in the same launch.  A session's next frame is admitted
+// once its previous frame has completed, into a new launch on another slot
+// that runs beside the launches still on the GPU (continuous batching: new
+// frames enter while others run, up to max_launches_in_flight launches).
 //
 // The frame sequence per session is the reference renderer's:
 // renderQuality for the first frame (fractalRenderMain + compose), then
@@ -79,10 +84,14 @@ constexpr uint32_t SERVE_STATUS_CANCELLED = 1u, SERVE_STATUS_TIMEOUT = 2u;
 template <class R> struct ServeFrame {
     AdvancedArgs<R> a;               // frame parameters (a.in etc. for renderFast frames)
     uint32_t advanced;               // 1: fractalRenderAdvanced, 0: fractalRenderMain
-    uint32_t slot;                   // the frame's index in the launch (status word)
+    uint32_t slot;                   // the frame's index in the launch (status, done words)
     uint32_t chunk;                  // tiles per job
-    uint32_t pad_;
+    uint32_t n_jobs;                 // jobs of this frame
     const volatile uint32_t *cancel; // host-mapped; nonzero stops the frame
+    uint32_t *rgba;                  // the frame's image, composed tile by tile
+    long rgba_pitch;
+    float compose_max_ss;
+    uint32_t pad_;
 };
 
 // Everything a launch sends to the device, copied in one piece.  Jobs of a
@@ -91,10 +100,11 @@ struct ServeTable {
     ServeFrame<float> f32[SERVE_MAX_FRAMES];   // binary32 frames, grouped
     ServeFrame<double> f64[SERVE_MAX_FRAMES];  // binary64 frames, grouped
     uint32_t job_begin[SERVE_GROUPS][SERVE_MAX_FRAMES + 1];
-    ComposeArgs compose[SERVE_MAX_FRAMES];
+    ComposeArgs compose[SERVE_MAX_FRAMES];     // perturbation frames (composed after their kernel)
     uint32_t compose_begin[SERVE_MAX_FRAMES + 1];
-    uint32_t counters[32];             // one work counter per kernel (zero on arrival)
-    uint32_t status[SERVE_MAX_FRAMES]; // SERVE_STATUS_* bits per frame (zero on arrival)
+    uint32_t counters[32];                     // one work counter per kernel (zero on arrival)
+    uint32_t status[SERVE_MAX_FRAMES];         // SERVE_STATUS_* bits per frame (zero on arrival)
+    uint32_t jobs_done[SERVE_MAX_FRAMES];      // finished jobs per frame (zero on arrival)
 };
 
 __device__ __forceinline__ unsigned long long global_ns()
@@ -120,20 +130,28 @@ __device__ __forceinline__ uint32_t find_frame(const uint32_t *begin, uint32_t n
 // Tiles of every frame of one group (ADV: renderFast frames, else
 // renderQuality frames).  A job is a strip of `chunk` tiles of one frame
 // (chunk > 1 for large frames, whose reuse tiles take few loads each); the
-// next job is claimed while this one renders.
+// next job is claimed while this one renders.  Each pixel is composed into
+// the frame's RGBA8 image as soon as its record is stored (compose is
+// per pixel, gen.cu:455-475), and the warp that finishes a frame's last job
+// publishes the frame: a system-scope fence, then the frame's done word in
+// host-mapped memory (1 | status << 8), so the host completes frames one by
+// one while the launch goes on.
 template <class R, int A, int F, bool ADV>
 __global__ void __launch_bounds__(PERSIST_THREADS)
     k_serve(const ServeFrame<R> *__restrict__ frames, const uint32_t *__restrict__ job_begin, uint32_t n_frames,
-            uint32_t *counter, uint32_t *status, unsigned long long *const *totals, unsigned long long budget_ns)
+            uint32_t *counter, uint32_t *status, uint32_t *jobs_done, volatile uint32_t *done_words,
+            unsigned long long *const *totals, unsigned long long budget_ns, const uint32_t *palette,
+            uint32_t palette_len)
 {
+    __shared__ uint32_t s_pal[4096];
     __shared__ uint32_t s_begin[SERVE_MAX_FRAMES + 1];
     for (uint32_t k = threadIdx.x; k <= n_frames; k += blockDim.x) s_begin[k] = job_begin[k];
+    for (uint32_t k = threadIdx.x; k < palette_len; k += blockDim.x) s_pal[k] = palette[k];
     __syncthreads();
     const uint32_t n_jobs = s_begin[n_frames];
     const uint32_t lane = threadIdx.x & 31u;
     const unsigned long long t0 = global_ns();
-    unsigned long long iters = 0;
-    uint32_t cur = 0xffffffffu;  // frame whose pixel-iterations `iters` holds
+    uint32_t cur = 0xffffffffu;  // frame of the previous job
     uint32_t seen = 0;           // cancel word of frame `cur` read one job ago
     bool stopped = false;
     uint32_t claim = 0;
@@ -144,8 +162,6 @@ __global__ void __launch_bounds__(PERSIST_THREADS)
         const uint32_t f = find_frame(s_begin, n_frames, job);
         const ServeFrame<R> &fr = frames[f];
         if (f != cur) {
-            if (cur != 0xffffffffu) add_total(totals[frames[cur].slot], iters, lane);
-            iters = 0;
             cur = f;
             seen = 0;
             stopped = false;
@@ -161,25 +177,46 @@ __global__ void __launch_bounds__(PERSIST_THREADS)
             claim = atomicAdd(counter, 1u);
         }
         stop = __shfl_sync(FULL, stop, 0);
+        unsigned long long iters = 0;
         if (stop) {
             stopped = true;
-            continue;
+        } else {
+            SampleGeometry<R> g = make_geometry(fr.a.m.image, fr.a.m.size, fr.a.m.max_iter, fr.a.m.jcx, fr.a.m.jcy);
+            const uint32_t t_first = (job - s_begin[f]) * fr.chunk;
+            const uint32_t t_end = min(t_first + fr.chunk, fr.a.m.n_tiles);
+            for (uint32_t t = t_first; t < t_end; t++) {
+                const uint32_t x0 = 8u * (t % fr.a.m.tiles_x), y0 = 4u * (t / fr.a.m.tiles_x);
+                PixelInfo rec;
+                if constexpr (ADV)
+                    rec = render_advanced_tile<R, A, F>(g, fr.a.m.image, fr.a.image_reused, fr.a.m.out, fr.a.m.pitch,
+                                                        fr.a.m.size, fr.a.in, fr.a.in_pitch, fr.a.focus, x0, y0, lane,
+                                                        fr.a.m.max_ss, fr.a.m.flags, iters);
+                else
+                    rec = render_main_tile<R, A, F>(g, fr.a.m.out, fr.a.m.pitch, fr.a.m.size, x0, y0, lane,
+                                                    fr.a.m.max_ss, fr.a.m.flags, iters);
+                const UInt2 p = tile_pixel(x0, y0, lane);
+                if (p.x < fr.a.m.size.x && p.y < fr.a.m.size.y) {
+                    uint32_t *row = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(fr.rgba) +
+                                                                 (size_t)p.y * (size_t)fr.rgba_pitch);
+                    row[p.x] = compose_pixel(rec, s_pal, palette_len, fr.compose_max_ss, false, COLOR_PALETTE, 1);
+                }
+            }
         }
-        SampleGeometry<R> g = make_geometry(fr.a.m.image, fr.a.m.size, fr.a.m.max_iter, fr.a.m.jcx, fr.a.m.jcy);
-        const uint32_t t_first = (job - s_begin[f]) * fr.chunk;
-        const uint32_t t_end = min(t_first + fr.chunk, fr.a.m.n_tiles);
-        for (uint32_t t = t_first; t < t_end; t++) {
-            const uint32_t x0 = 8u * (t % fr.a.m.tiles_x), y0 = 4u * (t / fr.a.m.tiles_x);
-            if constexpr (ADV)
-                render_advanced_tile<R, A, F>(g, fr.a.m.image, fr.a.image_reused, fr.a.m.out, fr.a.m.pitch,
-                                              fr.a.m.size, fr.a.in, fr.a.in_pitch, fr.a.focus, x0, y0, lane,
-                                              fr.a.m.max_ss, fr.a.m.flags, iters);
-            else
-                render_main_tile<R, A, F>(g, fr.a.m.out, fr.a.m.pitch, fr.a.m.size, x0, y0, lane, fr.a.m.max_ss,
-                                          fr.a.m.flags, iters);
+        // the job is finished (rendered or skipped): its pixel-iterations go to
+        // the session's counter, then the job is counted; the last one
+        // publishes the frame (after which nothing here touches its buffers)
+        add_total(totals[fr.slot], iters, lane);
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) {
+            const uint32_t prev = atomicAdd(&jobs_done[fr.slot], 1u);
+            if (prev + 1u == fr.n_jobs) {
+                __threadfence_system();
+                const uint32_t st = atomicOr(&status[fr.slot], 0u);
+                done_words[fr.slot] = 1u | (st << 8);
+            }
         }
     }
-    if (cur != 0xffffffffu) add_total(totals[frames[cur].slot], iters, lane);
 }
 
 // compose (gen.cu:455-475) of every frame of a launch: a warp takes a run of
@@ -224,32 +261,39 @@ template <class R, int A, int F, bool ADV> static int serve_occupancy()
     return occ;
 }
 
+// What every kernel of a launch shares.
+struct ServeLaunchArgs {
+    uint32_t *status, *jobs_done;
+    volatile uint32_t *done_words;
+    unsigned long long *const *totals;
+    unsigned long long budget_ns;
+    const uint32_t *palette;
+    uint32_t palette_len;
+    int sms;
+};
+
 template <class R, int A, int F, bool ADV>
 static cudaError_t launch_serve_t(const ServeFrame<R> *frames, const uint32_t *begin, uint32_t n_frames,
-                                  uint32_t n_jobs, uint32_t *counter, uint32_t *status,
-                                  unsigned long long *const *totals, unsigned long long budget_ns, int sms,
-                                  cudaStream_t s)
+                                  uint32_t n_jobs, uint32_t *counter, const ServeLaunchArgs &L, cudaStream_t s)
 {
     const int occ = serve_occupancy<R, A, F, ADV>();
-    k_serve<R, A, F, ADV><<<grid_for(n_jobs, occ, sms), PERSIST_THREADS, 0, s>>>(frames, begin, n_frames, counter, status,
-                                                                           totals, budget_ns);
+    k_serve<R, A, F, ADV><<<grid_for(n_jobs, occ, L.sms), PERSIST_THREADS, 0, s>>>(
+        frames, begin, n_frames, counter, L.status, L.jobs_done, L.done_words, L.totals, L.budget_ns, L.palette,
+        L.palette_len);
     return cudaGetLastError();
 }
 
 template <class R>
 static cudaError_t launch_serve(uint32_t group, const ServeFrame<R> *frames, const uint32_t *begin,
-                                uint32_t n_frames, uint32_t n_jobs, uint32_t *counter, uint32_t *status,
-                                unsigned long long *const *totals, unsigned long long budget_ns, int sms,
+                                uint32_t n_frames, uint32_t n_jobs, uint32_t *counter, const ServeLaunchArgs &L,
                                 cudaStream_t s)
 {
     const uint32_t a = (group / 2u) % 4u, f = group % 2u;
     const bool adv = group >= 16u;
 #define CHAOS_SERVE_CASE(AA, FF)                                                                                    \
     if (a == AA && f == FF)                                                                                         \
-        return adv ? launch_serve_t<R, AA, FF, true>(frames, begin, n_frames, n_jobs, counter, status, totals,      \
-                                                     budget_ns, sms, s)                                             \
-                   : launch_serve_t<R, AA, FF, false>(frames, begin, n_frames, n_jobs, counter, status, totals,     \
-                                                      budget_ns, sms, s);
+        return adv ? launch_serve_t<R, AA, FF, true>(frames, begin, n_frames, n_jobs, counter, L, s)                \
+                   : launch_serve_t<R, AA, FF, false>(frames, begin, n_frames, n_jobs, counter, L, s);
     CHAOS_SERVE_CASE(ARITH_PARITY, FRACTAL_MANDELBROT)
     CHAOS_SERVE_CASE(ARITH_PARITY, FRACTAL_JULIA)
     CHAOS_SERVE_CASE(ARITH_FMA, FRACTAL_MANDELBROT)
@@ -275,8 +319,8 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 constexpr uint32_t kRecordRing = 1u << 16;
-constexpr int kForkStreams = 4;
-constexpr int kMaxLaunchSlots = 4;
+constexpr int kForkStreams = 3;     // per launch slot, beside its own stream
+constexpr int kMaxLaunchSlots = 6;
 constexpr uint32_t kMaxSessions = 4096;  // session slots (reused once released)
 constexpr uint32_t kMaxDeepPerLaunch = 16;
 
@@ -319,17 +363,24 @@ struct Launch {
     int slot = 0;
     std::vector<uint64_t> records;  // frame k of the launch -> record id
     std::vector<uint32_t> sessions;
+    std::vector<uint8_t> deep;      // perturbation frames complete with the launch
+    std::vector<uint8_t> finished;  // frames completed so far
     std::atomic<double> done_at{-1.0};
     struct chaos_server *server = nullptr;
     bool failed = false;
 };
 
+// A launch slot: its tables, its streams (launches in different slots run
+// side by side), and the host-mapped done words its kernels write.
 struct LaunchSlot {
     ServeTable *host = nullptr;    // pinned
     ServeTable *dev = nullptr;
     uint32_t *status_host = nullptr;  // pinned copy of dev->status after the launch
     unsigned long long **totals_host = nullptr;  // pinned: per frame, its session's counter
     unsigned long long **totals_dev = nullptr;
+    volatile uint32_t *done_host = nullptr;  // pinned, mapped: per frame 1 | status << 8 once finished
+    uint32_t *done_dev = nullptr;
+    cudaStream_t stream = nullptr, fork[kForkStreams] = {};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, table_ready = nullptr;
     cudaEvent_t fork_done[kForkStreams] = {};
     bool busy = false;
@@ -364,7 +415,7 @@ struct chaos_server {
     size_t budget = 0, used = 0;
     uint32_t *palette = nullptr;
     uint32_t palette_len = 0;
-    chaos_server_config cfg{64, 2, 30.0, 0.0, 120.0};
+    chaos_server_config cfg{64, 4, 30.0, 0.0, 120.0};
 
     std::mutex mu;                    // all state below
     std::condition_variable changed;  // frames finished, sessions released (waiters: drain, read, close)
@@ -377,7 +428,7 @@ struct chaos_server {
     std::vector<std::unique_ptr<Launch>> failed_launches;
     uint64_t launch_seq = 0;
     LaunchSlot slots[kMaxLaunchSlots];
-    cudaStream_t stream = nullptr, fork[kForkStreams] = {};
+    cudaStream_t stream = nullptr;  // buffer frees
     std::vector<chaos_orbit *> retired_orbits;  // freed by the scheduler once their launches ended
     uint32_t *cancel_words = nullptr;           // pinned, mapped: one per session slot
     uint32_t *cancel_words_dev = nullptr;
@@ -438,43 +489,68 @@ void finish_record_locked(chaos_server *srv, uint64_t id, int status, double don
     rc.state = REC_DONE;
 }
 
-// Finished launches, in order: records, slots, closing sessions.
+void complete_frame_locked(chaos_server *srv, Launch &l, size_t k, int status, double done)
+{
+    l.finished[k] = 1;
+    finish_record_locked(srv, l.records[k], status, done, -1.0);
+    Session &s = *srv->sessions[l.sessions[k]];
+    s.in_flight--;
+    srv->in_flight--;
+    if (s.closing && s.in_flight == 0 && s.waiting == 0) release_session_locked(srv, s);
+}
+
+int frame_status(uint32_t bits)
+{
+    return (bits & SERVE_STATUS_CANCELLED) ? CHAOS_ERR_STATE : (bits & SERVE_STATUS_TIMEOUT) ? CHAOS_ERR_TIMEOUT
+                                                                                             : CHAOS_OK;
+}
+
+// Frames the kernels have published complete one by one; a launch whose last
+// operation (and completion callback) has run completes the rest (its
+// perturbation frames) and frees its slot.
 void reap_locked(chaos_server *srv)
 {
     bool any = false;
-    while (!srv->launches.empty()) {
-        Launch &l = *srv->launches.front();
+    const double now = srv->now();
+    for (auto it = srv->launches.begin(); it != srv->launches.end();) {
+        Launch &l = **it;
         LaunchSlot &sl = srv->slots[l.slot];
-        if (!l.failed) {
-            // the completion callback runs after the launch's last operation;
-            // until it has, the Launch stays alive
-            if (l.done_at.load() < 0) {
-                cudaError_t q = cudaEventQuery(sl.ev1);
-                if (q == cudaErrorNotReady || q == cudaSuccess) break;
-                l.failed = true;  // the stream failed: the callback never runs
+        if (!l.failed)
+            for (size_t k = 0; k < l.records.size(); k++) {
+                if (l.finished[k] || l.deep[k]) continue;
+                const uint32_t w = sl.done_host[k];
+                if (w & 1u) {
+                    complete_frame_locked(srv, l, k, frame_status(w >> 8), now);
+                    any = true;
+                }
             }
+        bool ended = l.failed;
+        if (!ended && l.done_at.load() >= 0) ended = true;
+        if (!ended && !l.failed) {
+            cudaError_t q = cudaEventQuery(sl.ev1);
+            if (q != cudaErrorNotReady && q != cudaSuccess) {
+                l.failed = true;  // the stream failed: the callback never runs
+                ended = true;
+            }
+        }
+        if (!ended) {
+            ++it;
+            continue;
         }
         float gpu_ms = 0.f;
         if (!l.failed) cudaEventElapsedTime(&gpu_ms, sl.ev0, sl.ev1);
-        const double done = l.done_at.load() >= 0 ? l.done_at.load() : srv->now();
+        const double done = l.done_at.load() >= 0 ? l.done_at.load() : now;
         for (size_t k = 0; k < l.records.size(); k++) {
-            int st = CHAOS_OK;
-            if (l.failed)
-                st = CHAOS_ERR_CUDA;
-            else if (sl.status_host[k] & SERVE_STATUS_CANCELLED)
-                st = CHAOS_ERR_STATE;
-            else if (sl.status_host[k] & SERVE_STATUS_TIMEOUT)
-                st = CHAOS_ERR_TIMEOUT;
-            finish_record_locked(srv, l.records[k], st, done, gpu_ms);
-            Session &s = *srv->sessions[l.sessions[k]];
-            s.in_flight--;
-            srv->in_flight--;
-            if (s.closing && s.in_flight == 0 && s.waiting == 0) release_session_locked(srv, s);
+            if (!l.finished[k]) {
+                int st = l.failed ? CHAOS_ERR_CUDA : frame_status(sl.status_host[k]);
+                complete_frame_locked(srv, l, k, st, done);
+            }
+            srv->rec(l.records[k]).r.gpu_ms = gpu_ms;
         }
         sl.busy = false;
         // a failed launch's callback may still run: keep it until the server goes
-        if (l.failed) srv->failed_launches.push_back(std::move(srv->launches.front()));
-        srv->launches.pop_front();
+        if (l.failed) srv->failed_launches.push_back(std::move(*it));
+        it = srv->launches.erase(it);
         any = true;
     }
     if (any && srv->launches.empty() && !srv->retired_orbits.empty()) {
@@ -505,22 +581,24 @@ void expire_locked(chaos_server *srv, double now)
     if (any) srv->changed.notify_all();
 }
 
-bool allocate_session_locked(chaos_server *srv, Session &s)
+// The session's buffers, allocated on the stream of the launch that first
+// uses them (stream-ordered, so nothing waits).
+bool allocate_session_locked(chaos_server *srv, Session &s, cudaStream_t st)
 {
     const chaos_session_desc &d = s.d;
     s.pitch = round_up(16 * (size_t)d.width, 512);
     s.rgba_pitch = round_up(4 * (size_t)d.width, 512);
-    cudaError_t e = cudaMallocAsync((void **)&s.buf[0], s.pitch * d.height, srv->stream);
-    if (e == cudaSuccess) e = cudaMallocAsync((void **)&s.buf[1], s.pitch * d.height, srv->stream);
-    if (e == cudaSuccess) e = cudaMallocAsync((void **)&s.rgba, s.rgba_pitch * d.height, srv->stream);
-    if (e == cudaSuccess) e = cudaMallocAsync((void **)&s.iters, sizeof(unsigned long long), srv->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(s.iters, 0, sizeof(unsigned long long), srv->stream);
+    cudaError_t e = cudaMallocAsync((void **)&s.buf[0], s.pitch * d.height, st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&s.buf[1], s.pitch * d.height, st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&s.rgba, s.rgba_pitch * d.height, st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&s.iters, sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.iters, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) {
         api_fail(CHAOS_ERR_CUDA, "session buffers: %s", cudaGetErrorString(e));
         for (int k = 0; k < 2; k++)
-            if (s.buf[k]) cudaFreeAsync(s.buf[k], srv->stream);
-        if (s.rgba) cudaFreeAsync(s.rgba, srv->stream);
-        if (s.iters) cudaFreeAsync(s.iters, srv->stream);
+            if (s.buf[k]) cudaFreeAsync(s.buf[k], st);
+        if (s.rgba) cudaFreeAsync(s.rgba, st);
+        if (s.iters) cudaFreeAsync(s.iters, st);
         s.buf[0] = s.buf[1] = nullptr;
         s.rgba = nullptr;
         s.iters = nullptr;
@@ -581,6 +659,9 @@ void fill_frame(ServeFrame<R> &f, const Session &s, const double rect[4], bool f
     f.advanced = fast ? 1u : 0u;
     f.slot = slot;
     f.cancel = s.cancel_dev;
+    f.rgba = s.rgba;
+    f.rgba_pitch = (long)s.rgba_pitch;
+    f.compose_max_ss = d.max_super_sampling;
     if (fast) {
         // this frame writes buf[1] (the older one) from buf[0]; the swap happens on admission
         m.out = s.buf[1];
@@ -609,6 +690,7 @@ struct Forming {
         uint32_t group;  // kernel group (not deep)
     };
     std::vector<Item> items;
+    int slot = -1;  // launch slot the frames go to
 };
 
 // Build and enqueue one launch of the admitted frames (under the lock: only
@@ -616,23 +698,23 @@ struct Forming {
 int enqueue_launch_locked(chaos_server *srv, Forming &fm)
 {
     TraceRange trace_("chaos_server launch");
-    int slot_id = -1;
-    for (int k = 0; k < (int)srv->cfg.max_launches_in_flight && k < kMaxLaunchSlots; k++)
-        if (!srv->slots[k].busy) {
-            slot_id = k;
-            break;
-        }
-    if (slot_id < 0) return CHAOS_ERR_STATE;  // caller checked
+    const int slot_id = fm.slot;
     LaunchSlot &sl = srv->slots[slot_id];
     ServeTable &T = *sl.host;
     std::memset(T.counters, 0, sizeof T.counters);
     std::memset(T.status, 0, sizeof T.status);
+    std::memset(T.jobs_done, 0, sizeof T.jobs_done);
     std::unique_ptr<Launch> L(new Launch());
     L->seq = ++srv->launch_seq;
     L->slot = slot_id;
     L->server = srv;
+    const size_t n = fm.items.size();
+    L->deep.assign(n, 0);
+    L->finished.assign(n, 0);
+    for (size_t k = 0; k < n; k++) sl.done_host[k] = 0u;
 
-    // frames per group (binary32 frames first in f32[], binary64 in f64[])
+    // frames per group (binary32 frames in f32[], binary64 in f64[]); within a
+    // group the smaller frames come first, so they finish first
     uint32_t n_group[SERVE_GROUPS] = {0};
     uint32_t first_of[SERVE_GROUPS] = {0};
     for (auto &it : fm.items)
@@ -647,39 +729,51 @@ int enqueue_launch_locked(chaos_server *srv, Forming &fm)
             n64 += n_group[g];
         }
     }
+    std::vector<uint32_t> order(n);
+    for (uint32_t k = 0; k < n; k++) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+        const chaos_session_desc &a = srv->sessions[fm.items[x].session]->d;
+        const chaos_session_desc &b = srv->sessions[fm.items[y].session]->d;
+        return (uint64_t)a.width * a.height < (uint64_t)b.width * b.height;
+    });
     uint32_t fill[SERVE_GROUPS] = {0};
     uint64_t tiles_all = 0;
-    std::vector<uint32_t> comp_order;
-    for (uint32_t k = 0; k < fm.items.size(); k++) {
+    uint32_t n_deep = 0;
+    for (uint32_t k = 0; k < n; k++) {
         auto &it = fm.items[k];
         Session &s = *srv->sessions[it.session];
         L->records.push_back(it.record);
         L->sessions.push_back(it.session);
         sl.totals_host[k] = s.iters;
-        const chaos_session_desc &d = s.d;
-        uint32_t flags = it.fast ? (d.flags & 0xffffu) | CHAOS_FLAG_IS_ZOOMING | CHAOS_FLAG_ZOOMING_IN
-                                 : (d.flags & CHAOS_FLAG_ADAPTIVE_SS);
-        if (!it.deep) {
-            const uint32_t g = it.group;
-            const uint32_t idx = first_of[g] + fill[g]++;
-            if (!group_binary64(g))
-                fill_frame<float>(T.f32[idx], s, it.rect, it.fast, k, flags);
-            else
-                fill_frame<double>(T.f64[idx], s, it.rect, it.fast, k, flags);
-            tiles_all += (uint64_t)((d.width + 7u) / 8u) * ((d.height + 3u) / 4u);
-        }
-        // the compose of this frame reads the buffer the frame writes
-        ComposeArgs &c = T.compose[k];
+        L->deep[k] = it.deep ? 1 : 0;
+        if (!it.deep) continue;
+        // perturbation frames are composed after their own kernel
+        ComposeArgs &c = T.compose[n_deep++];
         std::memset(&c, 0, sizeof c);
-        c.in = it.deep ? s.buf[0] : (it.fast ? s.buf[1] : s.buf[0]);
+        c.in = s.buf[0];
         c.pitch = (long)s.pitch;
         c.out = s.rgba;
         c.out_pitch = (long)s.rgba_pitch;
-        c.w = d.width;
-        c.h = d.height;
-        c.max_ss = it.deep ? 1.f : d.max_super_sampling;
+        c.w = s.d.width;
+        c.h = s.d.height;
+        c.max_ss = 1.f;
         c.color_mode = COLOR_PALETTE;
         c.magnifier = 1;
+    }
+    for (uint32_t k : order) {
+        auto &it = fm.items[k];
+        if (it.deep) continue;
+        Session &s = *srv->sessions[it.session];
+        const chaos_session_desc &d = s.d;
+        const uint32_t flags = it.fast ? (d.flags & 0xffffu) | CHAOS_FLAG_IS_ZOOMING | CHAOS_FLAG_ZOOMING_IN
+                                       : (d.flags & CHAOS_FLAG_ADAPTIVE_SS);
+        const uint32_t g = it.group;
+        const uint32_t idx = first_of[g] + fill[g]++;
+        if (!group_binary64(g))
+            fill_frame<float>(T.f32[idx], s, it.rect, it.fast, k, flags);
+        else
+            fill_frame<double>(T.f64[idx], s, it.rect, it.fast, k, flags);
+        tiles_all += (uint64_t)((d.width + 7u) / 8u) * ((d.height + 3u) / 4u);
     }
     // strips of tiles per job, as for single frames: up to 4 while every
     // resident warp still gets 8 jobs
@@ -689,56 +783,70 @@ int enqueue_launch_locked(chaos_server *srv, Forming &fm)
         uint32_t acc = 0;
         for (uint32_t j = 0; j < n_group[g]; j++) {
             T.job_begin[g][j] = acc;
+            uint32_t tiles;
             if (!group_binary64(g)) {
-                T.f32[first_of[g] + j].chunk = chunk;
-                acc += (T.f32[first_of[g] + j].a.m.n_tiles + chunk - 1) / chunk;
+                ServeFrame<float> &f = T.f32[first_of[g] + j];
+                f.chunk = chunk;
+                f.n_jobs = (f.a.m.n_tiles + chunk - 1) / chunk;
+                tiles = f.n_jobs;
             } else {
-                T.f64[first_of[g] + j].chunk = chunk;
-                acc += (T.f64[first_of[g] + j].a.m.n_tiles + chunk - 1) / chunk;
+                ServeFrame<double> &f = T.f64[first_of[g] + j];
+                f.chunk = chunk;
+                f.n_jobs = (f.a.m.n_tiles + chunk - 1) / chunk;
+                tiles = f.n_jobs;
             }
+            acc += tiles;
         }
         T.job_begin[g][n_group[g]] = acc;
     }
     uint32_t cacc = 0;
-    for (uint32_t k = 0; k < fm.items.size(); k++) {
+    for (uint32_t k = 0; k < n_deep; k++) {
         T.compose_begin[k] = cacc;
         cacc += ((T.compose[k].w + 127u) / 128u) * T.compose[k].h;
     }
-    T.compose_begin[fm.items.size()] = cacc;
+    T.compose_begin[n_deep] = cacc;
 
-    // the table, then the kernels of each group side by side, then deep
-    // frames, compose, status back, completion
-    cudaStream_t s0 = srv->stream;
+    // the table, then the kernels of each group side by side, then the
+    // perturbation frames and their compose, status back, completion
+    cudaStream_t s0 = sl.stream;
     cudaError_t e = cudaEventRecord(sl.ev0, s0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(sl.dev, sl.host, sizeof(ServeTable), cudaMemcpyHostToDevice, s0);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(sl.totals_dev, sl.totals_host, SERVE_MAX_FRAMES * sizeof(unsigned long long *),
                             cudaMemcpyHostToDevice, s0);
     if (e == cudaSuccess) e = cudaEventRecord(sl.table_ready, s0);
-    const unsigned long long budget_ns =
-        srv->cfg.frame_time_limit_s > 0 ? (unsigned long long)(srv->cfg.frame_time_limit_s * 1e9) : 0ull;
-    int used_forks = 0;
+    ServeLaunchArgs LA{};
+    LA.status = sl.dev->status;
+    LA.jobs_done = sl.dev->jobs_done;
+    LA.done_words = sl.done_dev;
+    LA.totals = sl.totals_dev;
+    LA.budget_ns = srv->cfg.frame_time_limit_s > 0 ? (unsigned long long)(srv->cfg.frame_time_limit_s * 1e9) : 0ull;
+    LA.palette = srv->palette;
+    LA.palette_len = srv->palette_len;
+    LA.sms = srv->sms;
+    // the first group on the slot's own stream, the others on its fork streams
+    int used = 0;
     for (uint32_t g = 0; g < SERVE_GROUPS && e == cudaSuccess; g++) {
         if (!n_group[g]) continue;
         const uint32_t n_jobs = T.job_begin[g][n_group[g]];
-        cudaStream_t fs = srv->fork[used_forks % kForkStreams];
-        if (used_forks < kForkStreams) e = cudaStreamWaitEvent(fs, sl.table_ready, 0);
+        cudaStream_t fs = used == 0 ? s0 : sl.fork[(used - 1) % kForkStreams];
+        if (used >= 1 && used <= kForkStreams) e = cudaStreamWaitEvent(fs, sl.table_ready, 0);
         if (e != cudaSuccess) break;
         if (!group_binary64(g))
             e = launch_serve<float>(g, sl.dev->f32 + first_of[g], sl.dev->job_begin[g], n_group[g], n_jobs,
-                                    &sl.dev->counters[g], sl.dev->status, sl.totals_dev, budget_ns, srv->sms, fs);
+                                    &sl.dev->counters[g], LA, fs);
         else
             e = launch_serve<double>(g, sl.dev->f64 + first_of[g], sl.dev->job_begin[g], n_group[g], n_jobs,
-                                     &sl.dev->counters[g], sl.dev->status, sl.totals_dev, budget_ns, srv->sms, fs);
-        used_forks++;
+                                     &sl.dev->counters[g], LA, fs);
+        used++;
     }
-    for (int k = 0; k < std::min(used_forks, kForkStreams) && e == cudaSuccess; k++) {
-        e = cudaEventRecord(sl.fork_done[k], srv->fork[k]);
+    for (int k = 0; k < std::min(used - 1, kForkStreams) && e == cudaSuccess; k++) {
+        e = cudaEventRecord(sl.fork_done[k], sl.fork[k]);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s0, sl.fork_done[k], 0);
     }
     // perturbation frames (a session past binary64), one after another
-    uint32_t deep_counter = 16;
-    for (uint32_t k = 0; k < fm.items.size() && e == cudaSuccess; k++) {
+    uint32_t deep_counter = SERVE_GROUPS;
+    for (uint32_t k = 0; k < n && e == cudaSuccess; k++) {
         auto &it = fm.items[k];
         if (!it.deep) continue;
         Session &s = *srv->sessions[it.session];
@@ -762,8 +870,8 @@ int enqueue_launch_locked(chaos_server *srv, Forming &fm)
     if (e == cudaSuccess && cacc) {
         const unsigned warps_needed = (cacc + 7u) / 8u;
         const unsigned blocks = std::max(1u, std::min(warps_needed, (unsigned)srv->sms * 8u));
-        k_compose_frames<<<blocks, 256, 0, s0>>>(sl.dev->compose, sl.dev->compose_begin, (uint32_t)fm.items.size(),
-                                                 srv->palette, srv->palette_len);
+        k_compose_frames<<<blocks, 256, 0, s0>>>(sl.dev->compose, sl.dev->compose_begin, n_deep, srv->palette,
+                                                 srv->palette_len);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)
@@ -806,11 +914,18 @@ void commit_launch_locked(chaos_server *srv, Forming &fm)
 bool admit_and_launch(chaos_server *srv, std::unique_lock<std::mutex> &lk)
 {
     if (srv->waiting.empty()) return false;
-    uint32_t free_launch = 0;
-    for (int k = 0; k < (int)srv->cfg.max_launches_in_flight && k < kMaxLaunchSlots; k++)
-        if (!srv->slots[k].busy) free_launch++;
-    if (!free_launch) return false;
+    int slot = -1;
+    uint32_t busy = 0;
+    for (int k = 0; k < kMaxLaunchSlots; k++) {
+        if (srv->slots[k].busy)
+            busy++;
+        else if (slot < 0)
+            slot = k;
+    }
+    if (slot < 0 || busy >= srv->cfg.max_launches_in_flight) return false;
     Forming fm;
+    fm.slot = slot;
+    const cudaStream_t st = srv->slots[slot].stream;
     uint32_t n_deep = 0;
     bool memory_blocked = false;  // an earlier request waits for memory: no later one overtakes it for memory
     for (auto it = srv->waiting.begin(); it != srv->waiting.end();) {
@@ -818,7 +933,9 @@ bool admit_and_launch(chaos_server *srv, std::unique_lock<std::mutex> &lk)
         if (srv->in_flight + fm.items.size() >= srv->cfg.max_frames_in_flight) break;
         Record &rc = srv->rec(*it);
         Session &s = *srv->sessions[rc.r.session];
-        if (s.in_forming || s.reading || s.closing) {
+        // a session's next frame waits for its previous one (launches in
+        // different slots run side by side)
+        if (s.in_forming || s.in_flight || s.reading || s.closing) {
             ++it;
             continue;
         }
@@ -828,7 +945,7 @@ bool admit_and_launch(chaos_server *srv, std::unique_lock<std::mutex> &lk)
                 ++it;
                 continue;
             }
-            if (!allocate_session_locked(srv, s)) {
+            if (!allocate_session_locked(srv, s, st)) {
                 finish_record_locked(srv, *it, CHAOS_ERR_CUDA, srv->now(), 0.0);
                 s.waiting--;
                 it = srv->waiting.erase(it);
@@ -1007,8 +1124,6 @@ int chaos_server_create(size_t hbm_budget_bytes, const uint32_t *palette, uint32
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device);
     s->budget = hbm_budget_bytes;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
-    for (int k = 0; k < kForkStreams && e == cudaSuccess; k++)
-        e = cudaStreamCreateWithFlags(&s->fork[k], cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaHostAlloc((void **)&s->cancel_words, kMaxSessions * sizeof(uint32_t), cudaHostAllocMapped);
     if (e == cudaSuccess) {
         std::memset(s->cancel_words, 0, kMaxSessions * sizeof(uint32_t));
@@ -1024,6 +1139,15 @@ int chaos_server_create(size_t hbm_budget_bytes, const uint32_t *palette, uint32
         if (e == cudaSuccess) e = cudaMallocHost(&sl.status_host, SERVE_MAX_FRAMES * sizeof(uint32_t));
         if (e == cudaSuccess) e = cudaMallocHost(&sl.totals_host, SERVE_MAX_FRAMES * sizeof(unsigned long long *));
         if (e == cudaSuccess) e = cudaMalloc(&sl.totals_dev, SERVE_MAX_FRAMES * sizeof(unsigned long long *));
+        if (e == cudaSuccess) e = cudaHostAlloc((void **)&sl.done_host, SERVE_MAX_FRAMES * sizeof(uint32_t),
+                                                cudaHostAllocMapped);
+        if (e == cudaSuccess) {
+            std::memset((void *)sl.done_host, 0, SERVE_MAX_FRAMES * sizeof(uint32_t));
+            e = cudaHostGetDevicePointer((void **)&sl.done_dev, (void *)sl.done_host, 0);
+        }
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+        for (int f = 0; f < kForkStreams && e == cudaSuccess; f++)
+            e = cudaStreamCreateWithFlags(&sl.fork[f], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreate(&sl.ev0);
         if (e == cudaSuccess) e = cudaEventCreate(&sl.ev1);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.table_ready, cudaEventDisableTiming);
@@ -1312,6 +1436,8 @@ int chaos_server_destroy(chaos_server *s)
         s->poke();
         s->scheduler.join();  // ends once the launches on the GPU have ended
     }
+    for (int k = 0; k < kMaxLaunchSlots; k++)
+        if (s->slots[k].stream) cudaStreamSynchronize(s->slots[k].stream);
     if (s->stream) cudaStreamSynchronize(s->stream);
     for (auto &ss : s->sessions)
         if (ss && ss->open) release_session_locked(s, *ss);
@@ -1327,11 +1453,13 @@ int chaos_server_destroy(chaos_server *s)
         if (sl.ev0) cudaEventDestroy(sl.ev0);
         if (sl.ev1) cudaEventDestroy(sl.ev1);
         if (sl.table_ready) cudaEventDestroy(sl.table_ready);
-        for (int f = 0; f < kForkStreams; f++)
+        for (int f = 0; f < kForkStreams; f++) {
             if (sl.fork_done[f]) cudaEventDestroy(sl.fork_done[f]);
+            if (sl.fork[f]) cudaStreamDestroy(sl.fork[f]);
+        }
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+        if (sl.done_host) cudaFreeHost((void *)sl.done_host);
     }
-    for (int k = 0; k < kForkStreams; k++)
-        if (s->fork[k]) cudaStreamDestroy(s->fork[k]);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->palette) cudaFree(s->palette);
     if (s->cancel_words) cudaFreeHost(s->cancel_words);

@@ -411,7 +411,8 @@ typedef struct chaos_frame_record {
 /* Admission and time limits of a server (chaos_server_configure). */
 typedef struct chaos_server_config {
     uint32_t max_frames_in_flight;   /* frames admitted and not finished, over all sessions (default 64, 1..4096) */
-    uint32_t max_launches_in_flight; /* launches queued on the GPU at once (default 2, 1..4) */
+    uint32_t max_launches_in_flight; /* launches on the GPU at once, side by side on their own
+                                        streams (default 4, 1..6) */
     double max_wait_s;               /* a request not admitted within this time completes with
                                         CHAOS_ERR_TIMEOUT (default 30; 0 = no limit) */
     double frame_time_limit_s;       /* device time a launch may run before its unfinished frames stop
@@ -425,8 +426,11 @@ typedef struct chaos_server chaos_server;
  * one palette (host array, copied).  Its scheduler thread admits frame
  * requests and renders every admitted frame of all sessions in one launch
  * (one persistent kernel per precision / arithmetic / fractal present, each
- * pulling 8x4 tiles of all its frames from one work counter, then one
- * compose over all frames).  Replaces, per session, the frame loop of
+ * pulling 8x4 tiles of all its frames from one work counter and composing
+ * each pixel as it is stored).  A frame completes as soon as its last tile
+ * is done (the kernel publishes it to the host), not when its launch ends;
+ * a session's next frame is admitted once its previous one has completed,
+ * into a new launch that runs beside the ones still on the GPU.  Replaces, per session, the frame loop of
  * CudaFractalRenderer.renderQuality / renderFast
  * (J/cudarenderer/CudaFractalRenderer.java:159-206). */
 int chaos_server_create(size_t hbm_budget_bytes, const uint32_t *palette, uint32_t palette_len,
