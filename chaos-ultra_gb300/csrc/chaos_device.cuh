@@ -712,6 +712,10 @@ __device__ __forceinline__ void warping_origin(UInt2 p, UInt2 grid, const Rect<R
 // after the first is a fused multiply-add onto the sum so far, the first two
 // as fma(w00, T00, w10*T10))
 template <int A = ARITH_PARITY>
+__device__ __forceinline__ void filter_bilinear(float alpha, float beta, float2 a, float2 b, float2 c, float2 d,
+                                                float &value, float &weight);
+
+template <int A = ARITH_PARITY>
 __device__ __forceinline__ void read_filtered(const void *in, long pitch, float x, float y, float &value, float &weight)
 {
     uint32_t i = (uint32_t)floorf(x), j = (uint32_t)floorf(y);
@@ -720,6 +724,20 @@ __device__ __forceinline__ void read_filtered(const void *in, long pitch, float 
     PixelInfo b = load_pixel(pixel_ptr(in, pitch, i + 1, j));
     PixelInfo c = load_pixel(pixel_ptr(in, pitch, i, j + 1));
     PixelInfo d = load_pixel(pixel_ptr(in, pitch, i + 1, j + 1));
+    filter_bilinear<A>(alpha, beta, make_float2(a.value, a.weight), make_float2(b.value, b.weight),
+                       make_float2(c.value, c.weight), make_float2(d.value, d.weight), value, weight);
+}
+
+// The filter of readFromArrayUsingFiltering on the four neighbours (value,
+// weight) a = (i, j), b = (i+1, j), c = (i, j+1), d = (i+1, j+1).
+template <int A>
+__device__ __forceinline__ void filter_bilinear(float alpha, float beta, float2 a2, float2 b2, float2 c2, float2 d2,
+                                                float &value, float &weight)
+{
+    struct VW {
+        float value, weight;
+    };
+    const VW a{a2.x, a2.y}, b{b2.x, b2.y}, c{c2.x, c2.y}, d{d2.x, d2.y};
     float oa = __fsub_rn(1.f, alpha), ob = __fsub_rn(1.f, beta);
     float w00 = __fmul_rn(oa, ob), w10 = __fmul_rn(alpha, ob), w01 = __fmul_rn(oa, beta), w11 = __fmul_rn(alpha, beta);
     float r, w;
@@ -741,6 +759,30 @@ __device__ __forceinline__ void read_filtered(const void *in, long pitch, float 
     value = r;
     weight = w;
 }
+
+// Where the reuse filter reads the previous frame: straight from global
+// memory, or from a warp's staged copy of the source footprint of the strip
+// it renders (shared memory, filled with cp.async; see chaos_refmode.cuh).
+// Both hand filter_bilinear the same four (value, weight) pairs.
+template <int A> struct GlobalGather {
+    const void *in;
+    long pitch;
+    __device__ __forceinline__ void operator()(float x, float y, float &value, float &weight) const
+    {
+        read_filtered<A>(in, pitch, x, y, value, weight);
+    }
+};
+template <int A> struct StagedGather {
+    const float2 *buf;  // rows x cols (value, weight) pairs of the previous frame from (x0, y0)
+    int x0, y0, cols;
+    __device__ __forceinline__ void operator()(float x, float y, float &value, float &weight) const
+    {
+        uint32_t i = (uint32_t)floorf(x), j = (uint32_t)floorf(y);
+        float alpha = __fsub_rn(x, (float)i), beta = __fsub_rn(y, (float)j);
+        const float2 *p = buf + ((int)j - y0) * cols + ((int)i - x0);
+        filter_bilinear<A>(alpha, beta, p[0], p[1], p[cols], p[cols + 1], value, weight);
+    }
+};
 
 // getFoveationAdvisedSampleCount + linearMapping<float>, gen.cu:209-257.
 // Uniform over the 8x4 warp tile (the pixel is snapped to the tile corner).
@@ -774,12 +816,12 @@ __device__ __forceinline__ void foveation(UInt2 p, UInt2 focus, float max_ss, fl
 // fractalRenderAdvanced for one lane of an 8x4 warp tile (gen.cu:307-368).
 // Lanes that reach the same sampleTheFractal call site vote together.
 // Returns the record stored for the lane's pixel.
-template <class R, int A, int F>
-__device__ __forceinline__ PixelInfo render_advanced_tile(const SampleGeometry<R> &g, const Rect<R> &image,
-                                                     const Rect<R> &image_reused, void *out, long pitch, UInt2 size,
-                                                     const void *in, long in_pitch, UInt2 focus, uint32_t x0,
-                                                     uint32_t y0, uint32_t lane, float max_ss, uint32_t flags,
-                                                     unsigned long long &iters)
+template <class R, int A, int F, class G>
+__device__ __forceinline__ PixelInfo render_advanced_tile_g(const SampleGeometry<R> &g, const Rect<R> &image,
+                                                            const Rect<R> &image_reused, void *out, long pitch,
+                                                            UInt2 size, const G &gather, UInt2 focus, uint32_t x0,
+                                                            uint32_t y0, uint32_t lane, float max_ss, uint32_t flags,
+                                                            unsigned long long &iters)
 {
     UInt2 p = tile_pixel(x0, y0, lane);
     bool valid = p.x < size.x && p.y < size.y;
@@ -795,7 +837,7 @@ __device__ __forceinline__ PixelInfo render_advanced_tile(const SampleGeometry<R
             warping_origin<R, A>(p, size, image, image_reused, ox, oy);
             int oix = (int)roundf(ox), oiy = (int)roundf(oy);
             if (!(oix < 2 || (uint32_t)oix >= size.x - 2 || oiy < 2 || (uint32_t)oiy >= size.y - 2)) {
-                read_filtered<A>(in, in_pitch, ox, oy, reused_v, reused_w);
+                gather(ox, oy, reused_v, reused_w);
                 reusing = !(reused_w < 0.1f);
             }
         }
@@ -828,6 +870,17 @@ __device__ __forceinline__ PixelInfo render_advanced_tile(const SampleGeometry<R
     }
     if (valid) store_pixel(pixel_ptr(out, pitch, p.x, p.y), res);
     return res;
+}
+
+template <class R, int A, int F>
+__device__ __forceinline__ PixelInfo render_advanced_tile(const SampleGeometry<R> &g, const Rect<R> &image,
+                                                          const Rect<R> &image_reused, void *out, long pitch,
+                                                          UInt2 size, const void *in, long in_pitch, UInt2 focus,
+                                                          uint32_t x0, uint32_t y0, uint32_t lane, float max_ss,
+                                                          uint32_t flags, unsigned long long &iters)
+{
+    return render_advanced_tile_g<R, A, F>(g, image, image_reused, out, pitch, size, GlobalGather<A>{in, in_pitch},
+                                           focus, x0, y0, lane, max_ss, flags, iters);
 }
 
 // ---------------------------------------------------------------------------

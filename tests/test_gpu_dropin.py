@@ -371,3 +371,46 @@ def test_random_julia_views_against_both_reference_builds(drv, cuda, seed):
             ours = replay_main(drv, cuda, module_path("julia", parity), w, h, rect, mi, mss, flags, dbl, julia_c=jc)
             bad = same_pixels(ours, ref)
             assert not bad.any(), (seed, dbl, parity, jc, (c, zoom, w, h, mi, mss, flags), int(bad.sum()))
+
+
+@pytest.mark.parametrize("case", ["zoom_in_f32", "zoom_out_f32", "zoom_in_f64", "pan_f64"])
+def test_large_reuse_frames_match_both_reference_builds(drv, cuda, case):
+    """Frames large enough for the library's persistent reuse kernel to claim
+    strips of tiles and stage each strip's source footprint in shared memory
+    (3840x2160: four tiles per claim) against the reference's own
+    fractalRenderAdvanced in the Java launch shape: the library with the
+    rounded arithmetic against the --fmad=false build and with the
+    contracted arithmetic against the default build, record for record.
+    The previous frame is the reference's own fractalRenderMain of the old
+    plane (maxIter small: the reuse path is what is checked)."""
+    import chaos_gb300 as cg
+    w, h, mi, mss = 3840, 2160, 150, 2.0
+    dbl = case.endswith("f64")
+    rng = np.random.default_rng(hash(case) % 1000)
+    focus = (int(rng.integers(w // 4, 3 * w // 4)), int(rng.integers(h // 4, 3 * h // 4)))
+    old = rect_for((-0.748, 0.1), 0.0014, w, h)
+    if case == "pan_f64":
+        dx = (old[2] - old[0]) * 0.013
+        new = (old[0] + dx, old[1] - dx / 3, old[2] + dx, old[3] - dx / 3)
+        flags = 8 | 16 | 1
+    else:
+        into = case.startswith("zoom_in")
+        new = zoom_at(old, focus, w, h, into=into)
+        flags = 8 | 16 | (32 if into else 0) | 1 | 4
+    if not dbl:
+        old = tuple(float(v) for v in np.float32(old))
+        new = tuple(float(v) for v in np.float32(new))
+    for parity in (True, False):
+        prev = replay_main(drv, cuda, ref_cubin("mandelbrot", nofma=parity), w, h, old, mi, mss, 1, dbl)
+        ref = replay_advanced(drv, cuda, ref_cubin("mandelbrot", nofma=parity), w, h, new, mi, mss, flags, old, prev,
+                              focus, dbl)
+        inbuf, in_pitch = upload_pixels(cuda, prev)
+        buf, pitch = pitched(cuda, w, h)
+        cg.Module("mandelbrot").render_advanced(buf.data_ptr(), pitch, w, h, new, mi, mss, flags, old,
+                                                inbuf.data_ptr(), in_pitch, focus, double=dbl,
+                                                arith=cg.ARITH_PARITY if parity else cg.ARITH_CONTRACTED)
+        cuda.cuda.synchronize()
+        got = read_pixels(buf, w)
+        assert float(got["is_reused"].mean()) > 0.9  # the reuse path carries the frame
+        bad = same_pixels(got, ref)
+        assert not bad.any(), (case, parity, int(bad.sum()), got[bad][:3], ref[bad][:3])
