@@ -199,7 +199,7 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
                     }
                 }
             }
-            if (!done) {
+            if (!done && !std::is_same<N, FF>::value) {
                 if (!blk) {
                     lim = 1;
                 } else if (window) {
@@ -212,7 +212,7 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
         }
         const bool stepping = active && !done;
         const bool partial = stepping && lim < (uint32_t)K;
-        const bool any_partial = __any_sync(FULLM, partial);
+        const bool any_partial = !std::is_same<N, FF>::value && __any_sync(FULLM, partial);
         // K steps of `stepper`, keeping the state after lim steps on partial lanes
         auto run_block = [&](auto stepper) {
             if (any_partial) {
@@ -234,7 +234,32 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
                 for (int k = 0; k < K; k++) stepper(x, y);
             }
         };
-        if (stepping) {
+        if constexpr (std::is_same<N, FF>::value) {
+            // float-float: every step carries its own test (two binary32
+            // operations on the leading words beside the step's 43), so a lane
+            // that escapes stops at its exact state: no roll-back, no search
+            if (stepping) {
+                const uint32_t rest = max_iter - i;
+                const uint32_t lim_t = rest >= (uint32_t)K ? (uint32_t)K : rest;
+                uint32_t k = 0;
+                bool esc = false;
+#pragma unroll
+                for (int u = 0; u < K; u++) {
+                    if ((uint32_t)u == lim_t) break;
+                    const float rr = P::r2(x, y);
+                    if (!(rr < 4.f)) {
+                        esc = true;
+                        r2 = rr;
+                        break;
+                    }
+                    P::step(x, y, cx, cy);
+                    k++;
+                }
+                i += k;
+                if (!esc && i == max_iter) r2 = P::r2(x, y);
+                if (esc || i == max_iter) done = true;
+            }
+        } else if (stepping) {
             const T sx = x, sy = y;
             if constexpr (std::is_same<N, double>::value) {
                 // 2x on the integer pipe; blocks it cannot double exactly are redone
