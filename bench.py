@@ -1417,7 +1417,7 @@ def served_vs_fp64_oracle(srv, sids, shapes):
 
 def run_serve(args):
     """The C5 line."""
-    c5 = measure_c5(seconds=C5_BENCH_SECONDS)
+    c5 = measure_c5(seconds=args.seconds or C5_BENCH_SECONDS)
     line = {"metric": "Gpixel-iter/s; p99 frame latency (serving)", "value": c5["value"], "unit": "Gpixel-iter/s",
             "n_gpus": 1, "steps": c5["frames"], "warmup": c5["warmup_frames"],
             "ms_per_step": c5["latency_ms"]["p50"], "higher_is_better": True, "scaling": "weak",
@@ -1434,6 +1434,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--seconds", type=float, default=None, help="c5: length of the request trace (default 10)")
     ap.add_argument("--headline-only", action="store_true",
                     help="C2: leave out the reference-kernel, C4 and C5 sub-objects after the headline")
     ap.add_argument("--workload", choices=["c1", "c2", "c2-crop", "c3", "c4", "c4-crop", "c5", "compose", "reuse"],

@@ -2,9 +2,8 @@
 
 Outputs (git-ignored):
   lib/libchaos_gb300.so                 the C-ABI library (include/chaos_gb300.h)
-  cudaKernels/<fractal>.ptx             drop-in modules: mandelbrot and julia with the
-                                        arithmetic of the reference's default build
-                                        (contraction on), Newton rounded as --fmad=false
+  cudaKernels/<fractal>.ptx             drop-in modules with the arithmetic of the
+                                        reference's default build (contraction on)
   cudaKernels_parity/<fractal>.ptx      drop-in modules, every product/sum rounded
 The drop-in files are cubin images; cuModuleLoad (which the Java host calls
 with <cudaKernelsDir>/<fractal>.ptx) accepts cubin as well as PTX.
@@ -68,14 +67,18 @@ def build(verbose=False, ptxas_info=False, force=False):
             jobs.append([exe, *ARCH, *COMMON, *extra, *fmad, "-Xcompiler", "-fPIC", "-c", src, "-o", obj])
     dropin = os.path.join(CSRC, "dropin_module.cu")
     for fractal, fid in FRACTALS.items():
-        # cudaKernels: mandelbrot and julia as nvcc builds the reference by default;
-        # the Newton modules rounded operation by operation (as cudaKernels_parity)
-        for sub, arith in (("cudaKernels", "chaos::ARITH_CONTRACTED" if fid <= 1 else "chaos::ARITH_PARITY"),
-                           ("cudaKernels_parity", "chaos::ARITH_PARITY")):
+        # cudaKernels: the arithmetic of the reference as nvcc builds it by
+        # default; cudaKernels_parity: every product and sum rounded
+        for sub, arith in (("cudaKernels", "chaos::ARITH_CONTRACTED"), ("cudaKernels_parity", "chaos::ARITH_PARITY")):
             out = os.path.join(HERE, sub, fractal + ".ptx")
             if force or not _newer(out, [dropin] + headers):
-                # every contraction a module makes is spelled out in the source
-                fmad = ["--fmad=false"]
+                # every contraction of the shared sampling / reuse / compose code is
+                # spelled out in the source (intrinsics, which nvcc never fuses).
+                # The Newton steps are thrust::complex expressions as in the
+                # reference: in the default-build modules nvcc contracts them as it
+                # contracts the reference's own (same compiler, same expressions)
+                newton_default = fid >= 2 and sub == "cudaKernels"
+                fmad = [] if newton_default else ["--fmad=false"]
                 jobs.append([exe, *ARCH, *COMMON, *extra, *fmad, "-cubin", f"-DCHAOS_DROPIN_FRACTAL={fid}",
                              f"-DCHAOS_DROPIN_ARITH={arith}", dropin, "-o", out])
     with ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:

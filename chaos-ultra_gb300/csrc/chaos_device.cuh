@@ -774,12 +774,19 @@ template <int A> struct GlobalGather {
 };
 template <int A> struct StagedGather {
     const float2 *buf;  // rows x cols (value, weight) pairs of the previous frame from (x0, y0)
-    int x0, y0, cols;
+    int x0, y0, cols, rows;
+    const void *in;     // the previous frame, for a pixel whose neighbours fall outside the copy
+    long pitch;
     __device__ __forceinline__ void operator()(float x, float y, float &value, float &weight) const
     {
         uint32_t i = (uint32_t)floorf(x), j = (uint32_t)floorf(y);
+        const int ci = (int)i - x0, cj = (int)j - y0;
+        if (ci < 0 || cj < 0 || ci + 1 >= cols || cj + 1 >= rows) {
+            read_filtered<A>(in, pitch, x, y, value, weight);
+            return;
+        }
         float alpha = __fsub_rn(x, (float)i), beta = __fsub_rn(y, (float)j);
-        const float2 *p = buf + ((int)j - y0) * cols + ((int)i - x0);
+        const float2 *p = buf + cj * cols + ci;
         filter_bilinear<A>(alpha, beta, p[0], p[1], p[cols], p[cols + 1], value, weight);
     }
 };

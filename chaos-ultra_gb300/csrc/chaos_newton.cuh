@@ -8,8 +8,10 @@
 // reference's operand types and order: with Real = float, a term like
 // coefficients[1] * x is a double times a complex<float> and is evaluated as
 // complex<double> before the assignment rounds it back, so the same
-// expression forms are what reproduce the reference's results.  Compile this
-// with --fmad=false to match the reference built the same way.
+// expression forms are what reproduce the reference's results.  Built with
+// --fmad=false it matches the reference built the same way; built with nvcc's
+// default contraction (the default-build drop-in modules) nvcc fuses these
+// expressions as it fuses the reference's own.
 #pragma once
 
 #include <thrust/complex.h>

@@ -95,16 +95,15 @@ def _replay(drv, cuda, path, kind, w, h, rect, dbl, params):
 
 @pytest.mark.parametrize("kind", [2, 3, 4])
 @pytest.mark.parametrize("dbl", [False, True])
-@pytest.mark.parametrize("parity_dir", [True, False])
-def test_dropin_newton_matches_reference_and_oracle(drv, cuda, oracle, kind, dbl, parity_dir):
-    """The Newton modules of both module directories are rounded operation by
-    operation: the reference built with --fmad=false, bit for bit."""
+def test_dropin_newton_matches_reference_and_oracle(drv, cuda, oracle, kind, dbl):
+    """The Newton modules of cudaKernels_parity are rounded operation by
+    operation: the oracle and the reference built with --fmad=false, bit for
+    bit."""
     import chaos_gb300 as cg
     w, h = 100, 60
     rect = rect_for((0.1, -0.05), 3.0, w, h)
     params = OTHER if kind != 2 else DEFAULT
-    directory = cg.DROPIN_PARITY_DIR if parity_dir else cg.DROPIN_DIR
-    ours = _replay(drv, cuda, os.path.join(directory, NAMES[kind] + ".ptx"), kind, w, h, rect, dbl, params)
+    ours = _replay(drv, cuda, os.path.join(cg.DROPIN_PARITY_DIR, NAMES[kind] + ".ptx"), kind, w, h, rect, dbl, params)
     oracle.set_newton(*params)
     want = oracle.render_main(kind, dbl, 1, w, h, rect, 200, 3.0, 1)
     oracle.set_newton()
@@ -115,3 +114,60 @@ def test_dropin_newton_matches_reference_and_oracle(drv, cuda, oracle, kind, dbl
     ref = _replay(drv, cuda, ref_path, kind, w, h, rect, dbl, params)
     bad = same_pixels(ours, ref)
     assert not bad.any(), (int(bad.sum()), ours[bad][:3], ref[bad][:3])
+
+
+def _replay_advanced(drv, cuda, path, kind, w, h, new, old, prev, focus, flags, dbl, params):
+    from tests.gpu_util import advanced_params
+    mod = drv.load(path)
+    try:
+        roots, coeffs, mag = params
+        if kind in (3, 4):
+            drv.write_constant(mod, "roots", np.array(roots, dtype=np.float64).tobytes())
+            drv.write_constant(mod, "coefficients", np.array(coeffs, dtype=np.float64).tobytes())
+        if kind == 4:
+            drv.write_constant(mod, "colorMagnifier", np.int32(mag).tobytes())
+        fn = drv.function(mod, "fractalRenderAdvancedDouble" if dbl else "fractalRenderAdvancedFloat")
+        inbuf, in_pitch = upload_pixels(cuda, prev)
+        buf, pitch = pitched(cuda, w, h)
+        grid, block = java_grid(w, h)
+        drv.launch(fn, grid, block, advanced_params(buf.data_ptr(), pitch, w, h, new, 200, 3.0, flags, old,
+                                                    inbuf.data_ptr(), in_pitch, focus, dbl))
+        return read_pixels(buf, w)
+    finally:
+        drv.unload(mod)
+
+
+@pytest.mark.parametrize("kind", [2, 3, 4])
+@pytest.mark.parametrize("dbl", [False, True])
+@pytest.mark.parametrize("view", [0, 1, 2])
+def test_default_build_newton_modules_are_the_reference_default_build(drv, cuda, kind, dbl, view):
+    """cudaKernels/newton_*.ptx against the reference's Newton modules as nvcc
+    builds them by default (contraction on, the build the Java application
+    loads): main frames and a zoom step with reuse, record for record, on
+    seeded views and both parameter sets."""
+    import chaos_gb300 as cg
+    rng = np.random.default_rng(300 + 10 * kind + view)
+    w, h = int(rng.integers(40, 121)), int(rng.integers(30, 91))
+    centre = (float(rng.uniform(-1.0, 1.0)), float(rng.uniform(-1.0, 1.0)))
+    zoom = 10 ** float(rng.uniform(-3 if not dbl else -9, 0.5))
+    rect = rect_for(centre, zoom, w, h)
+    if not dbl:
+        rect = tuple(float(v) for v in np.float32(rect))
+    params = (OTHER if view % 2 else DEFAULT) if kind != 2 else DEFAULT
+    ref_path = os.path.join(ROOT, "oracle", "_ref", f"ref_{NAMES[kind]}.cubin")
+    if not os.path.exists(ref_path):
+        pytest.skip("reference Newton cubin not built")
+    ours_path = os.path.join(cg.DROPIN_DIR, NAMES[kind] + ".ptx")
+    ref = _replay(drv, cuda, ref_path, kind, w, h, rect, dbl, params)
+    ours = _replay(drv, cuda, ours_path, kind, w, h, rect, dbl, params)
+    bad = same_pixels(ours, ref)
+    assert not bad.any(), ("main", kind, dbl, view, int(bad.sum()), ours[bad][:3], ref[bad][:3])
+    focus = (int(rng.integers(0, w)), int(rng.integers(0, h)))
+    new = zoom_at(rect, focus, w, h, into=bool(view != 1))
+    if not dbl:
+        new = tuple(float(v) for v in np.float32(new))
+    flags = 8 | 16 | (32 if view != 1 else 0) | 1 | (4 if view == 2 else 0)
+    ref_a = _replay_advanced(drv, cuda, ref_path, kind, w, h, new, rect, ref, focus, flags, dbl, params)
+    ours_a = _replay_advanced(drv, cuda, ours_path, kind, w, h, new, rect, ref, focus, flags, dbl, params)
+    bad = same_pixels(ours_a, ref_a)
+    assert not bad.any(), ("advanced", kind, dbl, view, int(bad.sum()), ours_a[bad][:3], ref_a[bad][:3])
