@@ -88,6 +88,7 @@ class FrameOut(C.Structure):
         ("counts", C.c_void_p), ("smooth", C.c_void_p), ("pixels", C.c_void_p), ("pixels_pitch", C.c_long),
         ("rgba", C.c_void_p), ("palette", C.c_void_p), ("palette_len", C.c_uint32),
         ("interior_rgba", C.c_uint32), ("total_iterations", C.c_void_p), ("rebases", C.c_void_p),
+        ("cycle_skipped", C.c_void_p),
     ]
 
 
@@ -202,6 +203,7 @@ SIGNATURES = {
     "chaos_server_usage": (_int, [_vp, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     "chaos_server_clock": (C.c_double, [_vp]),
     "chaos_server_destroy": (_int, [_vp]),
+    "chaos_batch_read_cycle_skipped": (_int, [_vp, C.POINTER(C.c_ulonglong)]),
     "chaos_server_configure": (_int, [_vp, C.POINTER(ServerConfig)]),
     "chaos_server_get_config": (_int, [_vp, C.POINTER(ServerConfig)]),
     "chaos_server_queue": (_int, [_vp, C.POINTER(_u32), C.POINTER(_u32)]),

@@ -251,6 +251,12 @@ class Batch:
         check(lib().chaos_batch_read_total(self.handle, C.byref(t)))
         return t.value
 
+    def read_cycle_skipped(self):
+        """Iterations of the last launch proven interior by a repeated state and not run."""
+        t = C.c_ulonglong()
+        check(lib().chaos_batch_read_cycle_skipped(self.handle, C.byref(t)))
+        return t.value
+
     def close(self):
         if self.handle:
             lib().chaos_batch_destroy(self.handle)

@@ -671,6 +671,7 @@ static int frame_impl(const chaos_frame_desc *dsc, const chaos_frame_out *o, cud
     a.palette_len = o->palette_len;
     a.interior_rgba = o->interior_rgba;
     a.total = o->total_iterations;
+    a.skipped = o->cycle_skipped;
     if ((rc = take_counter(d, s, &a.counter))) return rc;
     return finish(launch_frame<R>(a, arith_of(dsc->arith), (int)dsc->fractal, d->sms, s), s, sync);
 }

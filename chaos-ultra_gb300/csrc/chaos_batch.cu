@@ -46,7 +46,7 @@ struct BatchArgs {
     uint32_t n_vp, n_jobs;
     uint32_t chunk;  // consecutive jobs a lane claims per work-counter update
     uint32_t *counter;
-    unsigned long long *total;
+    unsigned long long *total;  // [0] pixel-iterations, [1] iterations proven interior by a repeated state, not run
     const uint32_t *palette;
     uint32_t palette_len;
     uint32_t interior_rgba;
@@ -123,7 +123,8 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
     T x = P::zero(), y = P::zero(), cx = P::zero(), cy = P::zero();
     bool blk = false, need = true, begin = false;
     float acc_v = 0.f, acc[4] = {0.f, 0.f, 0.f, 0.f};
-    unsigned long long iters = 0;
+    unsigned long long iters = 0, skipped = 0;
+    CycleWatch<T> cw;  // exact cycle detection at the end of every full block (see CycleWatch)
 
     // a job's viewport: the last one whose job_base <= job
     auto start_job = [&]() {
@@ -185,6 +186,7 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
                 blk = P::blockable(cx, cy);
                 i = 0;
                 window = 0;
+                cw.reset(x, y);
                 if (max_iter == 0) done = true;
                 if constexpr (is_binary64<N>()) {
                     // start at z = c, the first step's result (+0 for -0), so that no
@@ -192,6 +194,7 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
                     if (max_iter > 0) {
                         x = __dadd_rn(cx, 0.0);
                         y = __dadd_rn(cy, 0.0);
+                        cw.reset(x, y);
                         i = 1;
                         const double rr = P::r2(x, y);
                         r2 = (float)rr;
@@ -256,6 +259,10 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
                     k++;
                 }
                 i += k;
+                if (!esc && lim_t == (uint32_t)K && cw.check(x, y)) {  // a repeated state: interior
+                    skipped += max_iter - i;
+                    i = max_iter;
+                }
                 if (!esc && i == max_iter) r2 = P::r2(x, y);
                 if (esc || i == max_iter) done = true;
             }
@@ -286,8 +293,13 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
             auto rr = P::r2(x, y);
             r2 = (float)rr;
             if (rr < 4) {
+                const bool full = window == 0u && lim == (uint32_t)K;  // a checkpoint every K steps
                 i += lim;
                 window = window > 1u ? window - lim : 0u;
+                if (full && cw.check(x, y)) {  // a repeated state: interior
+                    skipped += max_iter - i;
+                    i = max_iter;
+                }
                 if (i == max_iter) done = true;
             } else if (lim == 1u) {
                 i += 1u;
@@ -335,6 +347,9 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) iters += __shfl_down_sync(FULLM, iters, o);
     if (lane == 0 && iters && a.total) atomicAdd(a.total, iters);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) skipped += __shfl_down_sync(FULLM, skipped, o);
+    if (lane == 0 && skipped && a.total) atomicAdd(a.total + 1, skipped);
     // when launched after a kernel that is still running (programmatic dependent
     // launch), the kernel ends only after that one has completed, so that the
     // stream's later work sees both.  Block 0 alone waits: the other blocks
@@ -502,7 +517,7 @@ static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s
 {
     // work counters: one per tier kernel, then one per perturbation viewport
     cudaError_t e = cudaMemsetAsync(b->d_counters, 0, (kTiers + b->perturb.size()) * sizeof(uint32_t), s0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_total, 0, sizeof(unsigned long long), s0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_total, 0, 2 * sizeof(unsigned long long), s0);
     if (e == cudaSuccess) e = cudaEventRecord(fork, s0);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s1, fork, 0);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, fork, 0);
@@ -705,7 +720,7 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
     size_t n_perturb = 0;
     for (uint32_t k = 0; k < n; k++) n_perturb += tiers[k] == CHAOS_TIER_PERTURB_F32 || tiers[k] == CHAOS_TIER_PERTURB_F64;
     cudaError_t e = cudaMalloc(&b->d_counters, (kTiers + n_perturb) * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_total, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_total, 2 * sizeof(unsigned long long));
     // reference orbits of the perturbation viewports (host, multi-word)
     for (uint32_t k = 0; k < n && e == cudaSuccess; k++) {
         if (tiers[k] != CHAOS_TIER_PERTURB_F32 && tiers[k] != CHAOS_TIER_PERTURB_F64) continue;
@@ -809,6 +824,14 @@ int chaos_batch_read_total(const chaos_batch *b, unsigned long long *total)
     if (!b || !total) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "bad argument");
     cudaError_t e = cudaMemcpy(total, b->d_total, sizeof *total, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "read total: %s", cudaGetErrorString(e));
+    return CHAOS_OK;
+}
+
+int chaos_batch_read_cycle_skipped(const chaos_batch *b, unsigned long long *skipped)
+{
+    if (!b || !skipped) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "bad argument");
+    cudaError_t e = cudaMemcpy(skipped, b->d_total + 1, sizeof *skipped, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "read skipped: %s", cudaGetErrorString(e));
     return CHAOS_OK;
 }
 

@@ -238,8 +238,48 @@ __device__ __forceinline__ void step_contracted4(double &x, double &y, double cx
 // arithmetic the test's products are the step's own, so a test costs one add,
 // a compare and a branch; a lane that stops waits for its warp at the end of
 // the block.  Exact for every c, with no roll-back or search.
+// Exact cycle detection (Brent's method on checkpoints).  The rounded
+// iteration is deterministic, so once a state repeats bit for bit the orbit
+// cycles through states that all tested below 4 and never escapes: the
+// sample is interior, with the reference's answer (maxIterations), however
+// many steps remain.  A checkpoint comes at the end of every full block of a
+// sample (a fixed number of steps); the state there is compared with the one
+// saved at the last power-of-two checkpoint (the saved state moves at
+// checkpoints 1, 2, 4, 8, ...).  Equal states under == (a zero's sign aside,
+// which changes no later magnitude) prove the cycle.  A check costs two
+// compares per block.
+constexpr uint32_t CYCLE_SPAN = 16;  // steps between checkpoints in the tested binary32 blocks
+
+template <class T> __device__ __forceinline__ bool same_state(T a, T b) { return a == b; }
+
+template <class T> struct CycleWatch {
+    T sx, sy;
+    uint32_t ck, save_at;
+    __device__ __forceinline__ void reset(T x, T y)
+    {
+        sx = x;
+        sy = y;
+        ck = 0;
+        save_at = 1;
+    }
+    // At a checkpoint: true when the state repeats the saved one.
+    __device__ __forceinline__ bool check(T x, T y)
+    {
+        if (same_state(x, sx) && same_state(y, sy)) return true;
+        if (++ck == save_at) {
+            sx = x;
+            sy = y;
+            save_at <<= 1;
+        }
+        return false;
+    }
+};
+
+// With a CycleWatch (unbounded blocks only, K a multiple of CYCLE_SPAN), a
+// checkpoint comes after every CYCLE_SPAN steps; `cyc` reports a repeat.
 template <class R, int A, int K, bool BOUNDED>
-__device__ __forceinline__ uint32_t tested_block(R &x, R &y, R cx, R cy, uint32_t lim, R &r2, bool &esc)
+__device__ __forceinline__ uint32_t tested_block(R &x, R &y, R cx, R cy, uint32_t lim, R &r2, bool &esc,
+                                                 CycleWatch<R> *cw = nullptr, bool *cyc = nullptr)
 {
 #pragma unroll
     for (int k = 0; k < K; k++) {
@@ -250,6 +290,10 @@ __device__ __forceinline__ uint32_t tested_block(R &x, R &y, R cx, R cy, uint32_
             return (uint32_t)k;
         }
         step<R, A>(x, y, cx, cy);
+        if (!BOUNDED && cw && ((k + 1) % (int)CYCLE_SPAN) == 0 && cw->check(x, y)) {
+            *cyc = true;
+            return (uint32_t)(k + 1);
+        }
     }
     return (uint32_t)K;
 }
@@ -264,6 +308,8 @@ __device__ __forceinline__ uint32_t tested_block(R &x, R &y, R cx, R cy, uint32_
 // binary32), and |z| keeps growing until it overflows to inf/NaN; neither
 // tests below 4, so a block whose last state tests below 4 contains no
 // escape.  Otherwise `blockable` is false and every step is tested.
+// Every kept block ends at a checkpoint of the exact cycle detection
+// (CycleWatch): a state that repeats proves the sample interior.
 // r2_exit is r2 of the final state.  (Tested blocks, which the binary32
 // frame kernel uses, were slower here: a tile's lanes run in lock step, so
 // every lane pays the per-step test for as long as the tile's slowest lane
@@ -283,6 +329,8 @@ __device__ __forceinline__ uint32_t escape(uint32_t max_iter, R x, R y, R cx, R 
     }
     uint32_t i = i0;
     if (blockable) {
+        CycleWatch<R> cw;
+        cw.reset(x, y);
         while (max_iter - i >= (uint32_t)ESCAPE_BLOCK) {
             R sx = x, sy = y;
             bool redo = false;
@@ -317,6 +365,10 @@ __device__ __forceinline__ uint32_t escape(uint32_t max_iter, R x, R y, R cx, R 
                 break;
             }
             i += ESCAPE_BLOCK;
+            if (cw.check(x, y)) {  // a repeated state: interior
+                r2_exit = radius2<R, A>(x, y);
+                return max_iter;
+            }
         }
     }
     while (i < max_iter) {
@@ -405,6 +457,8 @@ __device__ __forceinline__ void ff_step(FF &x, FF &y, FF cx, FF cy)
 
 __device__ __forceinline__ float ff_radius2(FF x, FF y) { return __fmaf_rn(x.hi, x.hi, __fmul_rn(y.hi, y.hi)); }
 
+template <> __device__ __forceinline__ bool same_state<FF>(FF a, FF b) { return a.hi == b.hi && a.lo == b.lo; }
+
 // The escape loop of escape() in float-float: blocks of ESCAPE_BLOCK untested
 // steps while |c| <= 1.9975 (after an escape the leading words grow until
 // they overflow, so a block whose last state tests below 4 holds no escape),
@@ -416,6 +470,8 @@ __device__ __forceinline__ uint32_t escape_ff(uint32_t max_iter, FF x, FF y, FF 
     if (max_iter == 0u || !(ff_radius2(x, y) < 4.f)) return 0u;
     uint32_t i = 0;
     if (blockable) {
+        CycleWatch<FF> cw;
+        cw.reset(x, y);
         while (max_iter - i >= (uint32_t)ESCAPE_BLOCK) {
             const FF sx = x, sy = y;
 #pragma unroll
@@ -426,6 +482,7 @@ __device__ __forceinline__ uint32_t escape_ff(uint32_t max_iter, FF x, FF y, FF 
                 break;
             }
             i += ESCAPE_BLOCK;
+            if (cw.check(x, y)) return max_iter;  // a repeated state: interior
         }
     }
     while (i < max_iter) {

@@ -46,6 +46,7 @@ __device__ __forceinline__ void frame_point(const FrameArgs<R> &a, uint32_t w_ma
 
 template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIST_THREADS) k_frame(FrameArgs<R> a)
 {
+    static_assert(sizeof(R) == 4 ? K % CYCLE_SPAN == 0 : K == ESCAPE_BLOCK, "cycle checkpoints at block ends");
     __shared__ uint32_t s_pal[PALETTE_SMEM];
     const uint32_t *pal = a.palette;
     if (a.rgba && a.palette_len <= PALETTE_SMEM) {
@@ -62,7 +63,8 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
     bool blk = false, need = true, begin = false;
     uint32_t window = 0;  // > 0: the escape lies within the next `window` steps
     float acc_v = 0.f, acc[4] = {0.f, 0.f, 0.f, 0.f};
-    unsigned long long iters = 0;
+    unsigned long long iters = 0, skipped = 0;
+    CycleWatch<R> cw;  // exact cycle detection (see CycleWatch)
 
     for (;;) {
         uint32_t need_mask = __ballot_sync(FULL, need);
@@ -113,6 +115,7 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
                 }
                 blk = blockable_c(cx, cy);
                 window = 0;
+                cw.reset(x, y);
                 r2 = radius2<R, A>(x, y);
                 if (i == a.max_iter || !(r2 < R(4))) done = true;
             }
@@ -159,10 +162,15 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
             // binary32: tested steps (see tested_block)
             if (stepping) {
                 const uint32_t rest = a.max_iter - i;
-                bool esc = false;
-                const uint32_t n = rest >= (uint32_t)K ? tested_block<R, A, K, false>(x, y, cx, cy, K, r2, esc)
-                                                       : tested_block<R, A, K, true>(x, y, cx, cy, rest, r2, esc);
+                bool esc = false, cyc = false;
+                const uint32_t n = rest >= (uint32_t)K
+                                       ? tested_block<R, A, K, false>(x, y, cx, cy, K, r2, esc, &cw, &cyc)
+                                       : tested_block<R, A, K, true>(x, y, cx, cy, rest, r2, esc);
                 i += n;
+                if (cyc) {  // a repeated state: interior
+                    skipped += a.max_iter - i;
+                    i = a.max_iter;
+                }
                 if (esc || i == a.max_iter) done = true;
             }
         } else if (stepping) {
@@ -192,8 +200,13 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
             }
             r2 = radius2<R, A>(x, y);
             if (r2 < R(4)) {
+                const bool full = window == 0u && lim == (uint32_t)K;  // a checkpoint every K steps
                 i += lim;
                 window = window > 1u ? window - lim : 0u;
+                if (full && cw.check(x, y)) {  // a repeated state: interior
+                    skipped += a.max_iter - i;
+                    i = a.max_iter;
+                }
                 if (i == a.max_iter) done = true;
             } else if (lim == 1u) {
                 i += 1u;  // the escape step
@@ -243,6 +256,11 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) iters += __shfl_down_sync(FULL, iters, o);
         if (lane == 0 && iters) atomicAdd(a.total, iters);
+    }
+    if (a.skipped) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) skipped += __shfl_down_sync(FULL, skipped, o);
+        if (lane == 0 && skipped) atomicAdd(a.skipped, skipped);
     }
 }
 

@@ -65,6 +65,7 @@ template <class R> struct FrameArgs {
     uint32_t interior_rgba;
     unsigned long long *total;
     uint32_t *counter;
+    unsigned long long *skipped;  // optional: iterations of interior samples proven by a repeated state, not run
 };
 
 struct ComposeArgs {

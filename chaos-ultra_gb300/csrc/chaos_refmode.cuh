@@ -85,6 +85,8 @@ template <class R, int A, int F> __global__ void __launch_bounds__(PERSIST_THREA
 // reads global memory, so the bound only has to be good, not exact.
 // ---------------------------------------------------------------------------
 
+// Off until the tile load's shared-memory layout is pinned on the GPU.
+constexpr bool kStageReuse = false;
 constexpr int STAGE_COLS = 36, STAGE_ROWS = 7;           // records per copy
 constexpr int STAGE_PAIRS = 256;                         // >= STAGE_COLS * STAGE_ROWS, 2 KiB per buffer
 constexpr uint32_t STAGE_BYTES = STAGE_COLS * STAGE_ROWS * 8u;
@@ -325,7 +327,7 @@ static cudaError_t launch_advanced_t(const AdvancedArgs<R> &args, int sms, cudaS
     a.m.tile_chunk = tile_chunk_for(a.m.n_tiles, occ, sms);
     StageParams sp;
     std::memset(&sp, 0, sizeof sp);
-    const bool staged = a.m.tile_chunk > 1 && (a.m.flags & FLAG_SAMPLE_REUSE) &&
+    const bool staged = kStageReuse && a.m.tile_chunk > 1 && (a.m.flags & FLAG_SAMPLE_REUSE) &&
                         (reinterpret_cast<uintptr_t>(a.in) & 15u) == 0 && (a.in_pitch & 15) == 0 &&
                         stage_params(a, sp);
     const unsigned jobs = (a.m.n_tiles + a.m.tile_chunk - 1) / a.m.tile_chunk;

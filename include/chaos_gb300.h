@@ -266,6 +266,11 @@ typedef struct chaos_frame_out {
     uint32_t interior_rgba;
     unsigned long long *total_iterations;
     unsigned long long *rebases; /* perturbation tiers: glitch repairs (rebasing events) */
+    /* one uint64 the kernel adds the iterations it did not run to: a sample
+     * whose state repeats bit for bit is interior (the iteration is
+     * deterministic), so it counts max_iterations without running the rest
+     * (binary32 and binary64 tiers; total_iterations counts it in full) */
+    unsigned long long *cycle_skipped;
 } chaos_frame_out;
 
 /* Enqueue one frame (does not synchronise). */
@@ -360,6 +365,9 @@ int chaos_batch_tiers(const chaos_batch *batch, uint32_t *tiers, uint32_t n);
 int chaos_batch_total(const chaos_batch *batch, unsigned long long **device_total);
 /* The same total copied to host memory (synchronises the device). */
 int chaos_batch_read_total(const chaos_batch *batch, unsigned long long *total);
+/* Iterations of the last launch not run because a sample's state repeated
+ * bit for bit (interior; counted in full in the total), copied to the host. */
+int chaos_batch_read_cycle_skipped(const chaos_batch *batch, unsigned long long *skipped);
 int chaos_batch_destroy(chaos_batch *batch);
 
 /* ---- serving: concurrent zoom sessions ----------------------------------- */
