@@ -270,19 +270,23 @@ def run_ours(args):
     pal = torch.from_numpy(wl["palette"].view(np.int32)).to(dev)
     rgba = torch.zeros(W * H, dtype=torch.int32, device=dev)
     total = torch.zeros(1, dtype=torch.int64, device=dev)
+    skipped = torch.zeros(1, dtype=torch.int64, device=dev)
     out = cg.FrameOut(rgba=rgba.data_ptr(), palette=pal.data_ptr(), palette_len=len(wl["palette"]),
-                      interior_rgba=wl["interior_rgba"], total_iterations=total.data_ptr())
+                      interior_rgba=wl["interior_rgba"], total_iterations=total.data_ptr(),
+                      cycle_skipped=skipped.data_ptr())
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
     def frame():
         total.zero_()
+        skipped.zero_()
         cg.render_frame(desc, out, stream=stream, sync=False)
 
     for _ in range(args.warmup):
         frame()
     torch.cuda.synchronize()
     iters_per_frame = int(total.item())
+    skipped_per_frame = int(skipped.item())
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -391,6 +395,8 @@ def run_ours(args):
                    "l2": "flushed between steps (256 MiB write, outside the events)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "pixel_iterations_per_step": iters_per_frame,
+        "cycle_skipped_per_step": skipped_per_frame,
+        "steps_executed_per_step": iters_per_frame - skipped_per_frame,
         "frame_latency_ms": {"p50": statistics.median(lat), "p99": float(np.percentile(lat, 99)),
                              "max": max(lat)},
         "mismatch": {"vs": f"FP64 oracle ({kind}: computeFractal<double>, rounded arithmetic)",
@@ -611,6 +617,7 @@ def measure_c4(workload="c4", steps=3, warmup=3, compact=False):
     r_ms = _timed_launches(torch, stream, flush, lambda: rounded.launch(stream), steps)
     rclk = rclocks.stop()
     rounded_iters = rounded.read_total()
+    rounded_skipped = rounded.read_cycle_skipped()
     rounded_value = rounded_iters * len(r_ms) / (sum(r_ms) / 1e3) / 1e9
     rounded_counts = [c.cpu().numpy() for c, _ in rbufs]
     rounded.close()
@@ -771,6 +778,7 @@ def measure_c4(workload="c4", steps=3, warmup=3, compact=False):
                    "speedup_of_plain_f64_dropin": value / dropin_value, "clocks": clk},
         "rounded_f64_batch": {
             "value": rounded_value, "ms": r_ms, "pixel_iterations": rounded_iters,
+            "cycle_skipped": rounded_skipped, "steps_executed": rounded_iters - rounded_skipped,
             "escape_count_mismatch_vs_fp64_oracle_cpu_sample": oracle_mismatch["rounded"],
             "speedup_of_plain_f64_dropin": rounded_value / dropin_value,
             "speedup_of_reference_module": rounded_value / ref_mod["value"] if ref_mod else None,
@@ -852,7 +860,9 @@ def run_c1(args):
     counts = torch.zeros(n, dtype=torch.int32, device=dev)
     smooth = torch.zeros(n, dtype=torch.float32, device=dev)
     total = torch.zeros(1, dtype=torch.int64, device=dev)
-    out = cg.FrameOut(counts=counts.data_ptr(), smooth=smooth.data_ptr(), total_iterations=total.data_ptr())
+    skipped = torch.zeros(1, dtype=torch.int64, device=dev)
+    out = cg.FrameOut(counts=counts.data_ptr(), smooth=smooth.data_ptr(), total_iterations=total.data_ptr(),
+                      cycle_skipped=skipped.data_ptr())
     stream = torch.cuda.current_stream()
     flush = _l2_flush(torch, dev)
 
@@ -867,6 +877,7 @@ def run_c1(args):
             cg.render_frame(d, out, stream=stream, sync=False)
         torch.cuda.synchronize()
         total.zero_()
+        skipped.zero_()
         ev = []
         for k in range(steps):
             flush(k)
@@ -886,6 +897,7 @@ def run_c1(args):
     clocks.start()
     iters, ms = timed(cg.ARITH_PARITY, args.steps, 1)
     clk = clocks.stop()
+    skipped_per_frame = int(skipped.item()) // args.steps
     per_frame = iters // args.steps
     c = counts.cpu().numpy().view(np.uint32)
     known = {"pixel_iterations": per_frame, "interior": int((c == C1_MAX_ITER).sum()),
@@ -909,10 +921,16 @@ def run_c1(args):
     peak = cg.measure_fma_peak(cg.TIER_F32)
     ops = 6
     achieved = per_frame / (ms / args.steps / 1e3) * ops
+    executed = per_frame - skipped_per_frame
     roof = {"bound": "fp32-pipe", "achieved": achieved / 1e12, "peak": peak / 2 / 1e12, "unit": "Top/s",
             "frac": achieved / (peak / 2), "traffic": None, "ops_per_iteration": ops,
             "peak_source": "measured in this run: chaos_measure_fma_peak (full-occupancy FFMA chains)",
-            "kernel": "k_frame<float,PARITY,mandelbrot,64>"}
+            "kernel": "k_frame<float,PARITY,mandelbrot,64>",
+            "steps_executed_per_frame": executed, "pixel_iterations_per_frame": per_frame,
+            "frac_of_steps_executed": executed / (ms / args.steps / 1e3) * ops / (peak / 2),
+            "note": "pixel-iterations count an interior sample as maxIter (the metric's unit); the kernel stops a "
+                    "sample whose rounded state repeats bit for bit (exact cycle detection), so it executes fewer "
+                    "steps: frac uses pixel-iterations, frac_of_steps_executed the steps the FP32 pipe ran"}
 
     # CPU leg: the reference's computeFractal<float> over the whole frame, all host threads
     cpu = None
@@ -945,6 +963,8 @@ def run_c1(args):
                                    f"{C1_MAX_ITER}, 1 sample per pixel centre", "arith": "rounded (reference)",
                        "l2": "flushed between steps"},
             "known_answer": known,
+            "pixel_iterations_per_step": per_frame, "steps_executed_per_step": executed,
+            "cycle_skipped_per_step": skipped_per_frame,
             "tiers": {"f32-fma": {"value": f_iters / (f_ms / 1e3) / 1e9, "unit": "Gpixel-iter/s"}},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e_iters / e_s / 1e9, "unit": "Gpixel-iter/s", "h2d_bytes_per_step": 4 * len(pal),

@@ -140,3 +140,26 @@ def test_julia_through_origin_exact(cuda, oracle, arith):
                       ps=3.0 / w, julia_c=jc)
         o = oracle.frame(w, h, 500, 1, 0, True, arith, JULIA, 0, (0.0, 0.0), 3.0 / w, julia_c=jc)
         assert np.array_equal(g["counts"], o["counts"]), jc
+
+
+@pytest.mark.parametrize("tier", [0, 1])
+def test_c1_cycles_skip_iterations_not_counts(cuda, tier):
+    """Most C1 interior pixels settle on an exact cycle of the rounded
+    iteration: the frame kernel stops them at a repeated state and reports the
+    iterations it did not run apart, while the counts (and so the reference's
+    known answer) stay the same."""
+    import chaos_gb300 as cg
+    torch = cuda
+    n = 1024 * 1024
+    counts = torch.zeros(n, dtype=torch.int32, device="cuda:0")
+    total = torch.zeros(1, dtype=torch.int64, device="cuda:0")
+    skipped = torch.zeros(1, dtype=torch.int64, device="cuda:0")
+    desc = cg.FrameDesc(width=1024, height=1024, max_iterations=1000, samples_per_pixel=1,
+                        sample_mode=cg.SAMPLES_CENTER, tier=tier, arith=cg.ARITH_PARITY, fractal=cg.MANDELBROT,
+                        seed=0, center_x=-0.5, center_y=0.0, pixel_size=3.0 / 1024)
+    cg.render_frame(desc, cg.FrameOut(counts=counts.data_ptr(), total_iterations=total.data_ptr(),
+                                      cycle_skipped=skipped.data_ptr()))
+    want_total, want_interior = (181_032_650, 175_986) if tier == 0 else (181_040_256, 176_008)
+    assert int(total.item()) == want_total
+    assert int((counts.cpu().numpy() == 1000).sum()) == want_interior
+    assert int(skipped.item()) > want_total // 2  # more than half of the work was interior cycles
