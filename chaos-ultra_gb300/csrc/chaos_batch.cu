@@ -296,7 +296,7 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
                 const bool full = window == 0u && lim == (uint32_t)K;  // a checkpoint every K steps
                 i += lim;
                 window = window > 1u ? window - lim : 0u;
-                if (full && cw.check(x, y)) {  // a repeated state: interior
+                if (full && cw.template check_every<cycle_blocks<T>()>(x, y)) {  // a repeated state: interior
                     skipped += max_iter - i;
                     i = max_iter;
                 }

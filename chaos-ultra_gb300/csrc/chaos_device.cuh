@@ -254,13 +254,14 @@ template <class T> __device__ __forceinline__ bool same_state(T a, T b) { return
 
 template <class T> struct CycleWatch {
     T sx, sy;
-    uint32_t ck, save_at;
+    uint32_t ck, save_at, tick;
     __device__ __forceinline__ void reset(T x, T y)
     {
         sx = x;
         sy = y;
         ck = 0;
         save_at = 1;
+        tick = 0;
     }
     // At a checkpoint: true when the state repeats the saved one.
     __device__ __forceinline__ bool check(T x, T y)
@@ -273,7 +274,18 @@ template <class T> struct CycleWatch {
         }
         return false;
     }
+    // Called at every full block; a checkpoint at every N-th one.  Binary64
+    // loops take N = 4: there the compares compete with the integer half of
+    // the rounded step and repeats are rare at the depths binary64 serves, so
+    // checkpoints every 64 steps cost little and find most cycles a little
+    // later.
+    template <int N> __device__ __forceinline__ bool check_every(T x, T y)
+    {
+        if (N > 1 && ((++tick) & (uint32_t)(N - 1)) != 0u) return false;
+        return check(x, y);
+    }
 };
+template <class T> constexpr int cycle_blocks() { return sizeof(T) == 8 ? 4 : 1; }
 
 // With a CycleWatch (unbounded blocks only, K a multiple of CYCLE_SPAN), a
 // checkpoint comes after every CYCLE_SPAN steps; `cyc` reports a repeat.
@@ -365,7 +377,7 @@ __device__ __forceinline__ uint32_t escape(uint32_t max_iter, R x, R y, R cx, R 
                 break;
             }
             i += ESCAPE_BLOCK;
-            if (cw.check(x, y)) {  // a repeated state: interior
+            if (cw.template check_every<cycle_blocks<R>()>(x, y)) {  // a repeated state: interior
                 r2_exit = radius2<R, A>(x, y);
                 return max_iter;
             }
@@ -569,8 +581,12 @@ __device__ __forceinline__ SampleGeometry<R> make_geometry(const Rect<R> &r, UIn
 }
 
 // Sample offset i (gen.cu:104-117) and plane point (gen.cu:119-124).  The
-// contracted build fuses the x coordinate's product into its add.
-template <class R, int A = ARITH_PARITY>
+// contracted build fuses the x coordinate's product into its add; in the
+// Newton modules it fuses the y coordinate's too (established, like the rest
+// of the contracted arithmetic, against outputs of the reference's own
+// default-build modules: with y fused every record of 24 seeded views of each
+// Newton module matches, without it some do not).
+template <class R, int A = ARITH_PARITY, int F = FRACTAL_MANDELBROT>
 __device__ __forceinline__ void sample_point(const SampleGeometry<R> &g, uint32_t px, uint32_t py, uint32_t i,
                                              float sample_count_f, R &cx, R &cy)
 {
@@ -589,7 +605,10 @@ __device__ __forceinline__ void sample_point(const SampleGeometry<R> &g, uint32_
         cx = O::fma(O::add((R)px, dx), g.psx, g.lbx);
     else
         cx = O::add(g.lbx, O::mul(O::add((R)px, dx), g.psx));
-    cy = O::add(g.rty, O::mul(-O::add((R)py, dy), g.psy));
+    if (A == ARITH_CONTRACTED && F >= FRACTAL_NEWTON_WIRED)
+        cy = O::fma(-O::add((R)py, dy), g.psy, g.rty);
+    else
+        cy = O::add(g.rty, O::mul(-O::add((R)py, dy), g.psy));
 }
 
 // computeDispersion (gen.cu:24-34) over the first data_length stored samples.
@@ -628,7 +647,7 @@ __device__ uint32_t sample_the_fractal(const SampleGeometry<R> &g, uint32_t px, 
         uint32_t e = 0;
         if (valid) {
             R cx, cy;
-            sample_point<R, A>(g, px, py, i, sample_count_f, cx, cy);
+            sample_point<R, A, F>(g, px, py, i, sample_count_f, cx, cy);
             e = compute_fractal_g<R, A, F>(g, cx, cy);
             // pixel-iterations (escape-time modules; the Newton modules return a root index)
             if (F < FRACTAL_NEWTON_WIRED) iters += (F == FRACTAL_MANDELBROT && e == 0u) ? g.max_iter : e;
@@ -817,37 +836,6 @@ __device__ __forceinline__ void filter_bilinear(float alpha, float beta, float2 
     weight = w;
 }
 
-// Where the reuse filter reads the previous frame: straight from global
-// memory, or from a warp's staged copy of the source footprint of the strip
-// it renders (shared memory, filled with cp.async; see chaos_refmode.cuh).
-// Both hand filter_bilinear the same four (value, weight) pairs.
-template <int A> struct GlobalGather {
-    const void *in;
-    long pitch;
-    __device__ __forceinline__ void operator()(float x, float y, float &value, float &weight) const
-    {
-        read_filtered<A>(in, pitch, x, y, value, weight);
-    }
-};
-template <int A> struct StagedGather {
-    const float2 *buf;  // rows x cols (value, weight) pairs of the previous frame from (x0, y0)
-    int x0, y0, cols, rows;
-    const void *in;     // the previous frame, for a pixel whose neighbours fall outside the copy
-    long pitch;
-    __device__ __forceinline__ void operator()(float x, float y, float &value, float &weight) const
-    {
-        uint32_t i = (uint32_t)floorf(x), j = (uint32_t)floorf(y);
-        const int ci = (int)i - x0, cj = (int)j - y0;
-        if (ci < 0 || cj < 0 || ci + 1 >= cols || cj + 1 >= rows) {
-            read_filtered<A>(in, pitch, x, y, value, weight);
-            return;
-        }
-        float alpha = __fsub_rn(x, (float)i), beta = __fsub_rn(y, (float)j);
-        const float2 *p = buf + cj * cols + ci;
-        filter_bilinear<A>(alpha, beta, p[0], p[1], p[cols], p[cols + 1], value, weight);
-    }
-};
-
 // getFoveationAdvisedSampleCount + linearMapping<float>, gen.cu:209-257.
 // Uniform over the 8x4 warp tile (the pixel is snapped to the tile corner).
 // Contracted: the distance's sum of squares and k*x + q are fused.
@@ -880,12 +868,12 @@ __device__ __forceinline__ void foveation(UInt2 p, UInt2 focus, float max_ss, fl
 // fractalRenderAdvanced for one lane of an 8x4 warp tile (gen.cu:307-368).
 // Lanes that reach the same sampleTheFractal call site vote together.
 // Returns the record stored for the lane's pixel.
-template <class R, int A, int F, class G>
-__device__ __forceinline__ PixelInfo render_advanced_tile_g(const SampleGeometry<R> &g, const Rect<R> &image,
-                                                            const Rect<R> &image_reused, void *out, long pitch,
-                                                            UInt2 size, const G &gather, UInt2 focus, uint32_t x0,
-                                                            uint32_t y0, uint32_t lane, float max_ss, uint32_t flags,
-                                                            unsigned long long &iters)
+template <class R, int A, int F>
+__device__ __forceinline__ PixelInfo render_advanced_tile(const SampleGeometry<R> &g, const Rect<R> &image,
+                                                          const Rect<R> &image_reused, void *out, long pitch,
+                                                          UInt2 size, const void *in, long in_pitch, UInt2 focus,
+                                                          uint32_t x0, uint32_t y0, uint32_t lane, float max_ss,
+                                                          uint32_t flags, unsigned long long &iters)
 {
     UInt2 p = tile_pixel(x0, y0, lane);
     bool valid = p.x < size.x && p.y < size.y;
@@ -901,7 +889,7 @@ __device__ __forceinline__ PixelInfo render_advanced_tile_g(const SampleGeometry
             warping_origin<R, A>(p, size, image, image_reused, ox, oy);
             int oix = (int)roundf(ox), oiy = (int)roundf(oy);
             if (!(oix < 2 || (uint32_t)oix >= size.x - 2 || oiy < 2 || (uint32_t)oiy >= size.y - 2)) {
-                gather(ox, oy, reused_v, reused_w);
+                read_filtered<A>(in, in_pitch, ox, oy, reused_v, reused_w);
                 reusing = !(reused_w < 0.1f);
             }
         }
@@ -934,17 +922,6 @@ __device__ __forceinline__ PixelInfo render_advanced_tile_g(const SampleGeometry
     }
     if (valid) store_pixel(pixel_ptr(out, pitch, p.x, p.y), res);
     return res;
-}
-
-template <class R, int A, int F>
-__device__ __forceinline__ PixelInfo render_advanced_tile(const SampleGeometry<R> &g, const Rect<R> &image,
-                                                          const Rect<R> &image_reused, void *out, long pitch,
-                                                          UInt2 size, const void *in, long in_pitch, UInt2 focus,
-                                                          uint32_t x0, uint32_t y0, uint32_t lane, float max_ss,
-                                                          uint32_t flags, unsigned long long &iters)
-{
-    return render_advanced_tile_g<R, A, F>(g, image, image_reused, out, pitch, size, GlobalGather<A>{in, in_pitch},
-                                           focus, x0, y0, lane, max_ss, flags, iters);
 }
 
 // ---------------------------------------------------------------------------

@@ -203,7 +203,7 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
                 const bool full = window == 0u && lim == (uint32_t)K;  // a checkpoint every K steps
                 i += lim;
                 window = window > 1u ? window - lim : 0u;
-                if (full && cw.check(x, y)) {  // a repeated state: interior
+                if (full && cw.template check_every<cycle_blocks<R>()>(x, y)) {  // a repeated state: interior
                     skipped += a.max_iter - i;
                     i = a.max_iter;
                 }
