@@ -892,7 +892,8 @@ def run_c1(args):
     # the timed region lasts at least MIN_TIMED_S, so that the clock sampler
     # (one sample per 200 ms) sees it: more frames than --steps when needed
     _, probe_ms = timed(cg.ARITH_PARITY, 3, args.warmup)
-    args.steps = max(args.steps, math.ceil(MIN_TIMED_S * 1e3 / max(probe_ms / 3, 1e-3)))
+    min_s = MIN_TIMED_S if args.min_seconds is None else args.min_seconds
+    args.steps = max(args.steps, math.ceil(min_s * 1e3 / max(probe_ms / 3, 1e-3)))
     clocks = ClockSampler(0)
     clocks.start()
     iters, ms = timed(cg.ARITH_PARITY, args.steps, 1)
@@ -1047,7 +1048,8 @@ def run_deep(args):
 
     # the timed region lasts at least MIN_TIMED_S (more steps than --steps when needed)
     _, probe_ms, _ = timed(cg.TIER_PERTURB_F32, 2, args.warmup)
-    args.steps = max(args.steps, math.ceil(MIN_TIMED_S * 1e3 / max(sum(probe_ms) / 2, 1e-3)))
+    min_s = MIN_TIMED_S if args.min_seconds is None else args.min_seconds
+    args.steps = max(args.steps, math.ceil(min_s * 1e3 / max(sum(probe_ms) / 2, 1e-3)))
     clocks = ClockSampler(0)
     clocks.start()
     iters, span_ms, rb = timed(cg.TIER_PERTURB_F32, args.steps, 1)
@@ -1455,6 +1457,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--seconds", type=float, default=None, help="c5: length of the request trace (default 10)")
+    ap.add_argument("--min-seconds", type=float, default=None,
+                    help="c1 / c3: shortest timed region (default 2.5; 0 times exactly --steps steps, e.g. under a "
+                         "profiler)")
     ap.add_argument("--headline-only", action="store_true",
                     help="C2: leave out the reference-kernel, C4 and C5 sub-objects after the headline")
     ap.add_argument("--workload", choices=["c1", "c2", "c2-crop", "c3", "c4", "c4-crop", "c5", "compose", "reuse"],
