@@ -12,7 +12,7 @@ data_ptr()).
 from ._native import (ARITH_CONTRACTED, ARITH_FMA, ARITH_PARITY, DROPIN_DIR, DROPIN_PARITY_DIR, FLAG_ADAPTIVE_SS, FLAG_FOVEATION,
                       FLAG_IS_ZOOMING, FLAG_SAMPLE_REUSE, FLAG_VISUALIZE_SAMPLE_COUNT, FLAG_ZOOMING_IN, JULIA,
                       LIB_PATH, MANDELBROT, PRECISION_DOUBLE, PRECISION_FLOATFLOAT, PRECISION_SINGLE, PRECISION_TOO_BIG, SAMPLES_CENTER,
-                      SAMPLES_JITTER, SESSION_FLAG_BINARY64, TIER_AUTO, TIER_AUTO_DEEP, TIER_F32, TIER_F64, TIER_F64_ROUNDED, TIER_FLOATFLOAT,
+                      SAMPLES_JITTER, SESSION_FLAG_BINARY64, STATUS_TIMEOUT, TIER_AUTO, TIER_AUTO_DEEP, TIER_F32, TIER_F64, TIER_F64_ROUNDED, TIER_FLOATFLOAT,
                       TIER_PERTURB_F32, TIER_PERTURB_F64, BatchConfig, ChaosError, FrameDesc, FrameOut, FrameRecord,
                       RenderingModel, ServedFrame, ServerConfig, SessionDesc, Viewport, lib)
 from .api import (Batch, Module, Orbit, Renderer, Server, auto_tier, autotune_batch, available_fractals,
@@ -23,7 +23,7 @@ __all__ = [
     "ARITH_CONTRACTED", "ARITH_FMA", "ARITH_PARITY", "DROPIN_DIR", "DROPIN_PARITY_DIR", "FLAG_ADAPTIVE_SS", "FLAG_FOVEATION",
     "FLAG_IS_ZOOMING", "FLAG_SAMPLE_REUSE", "FLAG_VISUALIZE_SAMPLE_COUNT", "FLAG_ZOOMING_IN", "JULIA", "LIB_PATH",
     "MANDELBROT", "PRECISION_DOUBLE", "PRECISION_FLOATFLOAT", "PRECISION_SINGLE", "PRECISION_TOO_BIG", "SAMPLES_CENTER", "SAMPLES_JITTER",
-    "SESSION_FLAG_BINARY64", "TIER_AUTO", "TIER_AUTO_DEEP", "TIER_F32", "TIER_F64", "TIER_F64_ROUNDED", "TIER_FLOATFLOAT", "TIER_PERTURB_F32", "TIER_PERTURB_F64",
+    "SESSION_FLAG_BINARY64", "STATUS_TIMEOUT", "TIER_AUTO", "TIER_AUTO_DEEP", "TIER_F32", "TIER_F64", "TIER_F64_ROUNDED", "TIER_FLOATFLOAT", "TIER_PERTURB_F32", "TIER_PERTURB_F64",
     "BatchConfig", "ChaosError", "FrameDesc", "FrameOut", "FrameRecord", "RenderingModel", "ServedFrame", "ServerConfig",
     "SessionDesc", "Viewport",
     "lib", "Batch", "Module", "Orbit", "Renderer", "Server", "auto_tier", "autotune_batch", "available_fractals",

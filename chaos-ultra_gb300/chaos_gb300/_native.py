@@ -21,6 +21,7 @@ ERR_NOT_FOUND = 4
 ERR_STATE = 5
 ERR_OUT_OF_MEMORY = 6
 ERR_TIMEOUT = 7
+STATUS_TIMEOUT = 1
 ERR_UNSUPPORTED = 8
 
 FLAG_ADAPTIVE_SS = 1 << 0
@@ -79,7 +80,7 @@ class FrameDesc(C.Structure):
         ("samples_per_pixel", C.c_uint32), ("sample_mode", C.c_uint32), ("tier", C.c_uint32),
         ("arith", C.c_int32), ("fractal", C.c_uint32), ("seed", C.c_uint64),
         ("center_x", C.c_double), ("center_y", C.c_double), ("pixel_size", C.c_double),
-        ("julia_cx", C.c_double), ("julia_cy", C.c_double),
+        ("julia_cx", C.c_double), ("julia_cy", C.c_double), ("time_limit_s", C.c_double),
     ]
 
 
@@ -88,7 +89,7 @@ class FrameOut(C.Structure):
         ("counts", C.c_void_p), ("smooth", C.c_void_p), ("pixels", C.c_void_p), ("pixels_pitch", C.c_long),
         ("rgba", C.c_void_p), ("palette", C.c_void_p), ("palette_len", C.c_uint32),
         ("interior_rgba", C.c_uint32), ("total_iterations", C.c_void_p), ("rebases", C.c_void_p),
-        ("cycle_skipped", C.c_void_p),
+        ("cycle_skipped", C.c_void_p), ("status", C.c_void_p),
     ]
 
 
@@ -103,7 +104,7 @@ class Viewport(C.Structure):
 
 class BatchConfig(C.Structure):
     _fields_ = [("block_threads", C.c_uint32 * 3), ("escape_block", C.c_uint32 * 3), ("chunk", C.c_uint32 * 3),
-                ("fp64_warps_per_sm", C.c_uint32)]
+                ("fp64_warps_per_sm", C.c_uint32), ("time_limit_s", C.c_double)]
 
 
 TIER_AUTO = 255
@@ -204,6 +205,7 @@ SIGNATURES = {
     "chaos_server_clock": (C.c_double, [_vp]),
     "chaos_server_destroy": (_int, [_vp]),
     "chaos_batch_read_cycle_skipped": (_int, [_vp, C.POINTER(C.c_ulonglong)]),
+    "chaos_batch_read_status": (_int, [_vp, C.POINTER(C.c_uint32)]),
     "chaos_server_configure": (_int, [_vp, C.POINTER(ServerConfig)]),
     "chaos_server_get_config": (_int, [_vp, C.POINTER(ServerConfig)]),
     "chaos_server_queue": (_int, [_vp, C.POINTER(_u32), C.POINTER(_u32)]),

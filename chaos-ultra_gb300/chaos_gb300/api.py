@@ -257,6 +257,12 @@ class Batch:
         check(lib().chaos_batch_read_cycle_skipped(self.handle, C.byref(t)))
         return t.value
 
+    def read_status(self):
+        """STATUS_* bits of the last launch (0, or STATUS_TIMEOUT when the config's time limit ran out)."""
+        t = C.c_uint32()
+        check(lib().chaos_batch_read_status(self.handle, C.byref(t)))
+        return t.value
+
     def close(self):
         if self.handle:
             lib().chaos_batch_destroy(self.handle)

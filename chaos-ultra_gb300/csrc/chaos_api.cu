@@ -79,7 +79,7 @@ int device_state(DeviceState **out)
     DeviceState &d = g_devices[dev];
     std::call_once(d.once, [&]() {
         cudaError_t e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess) e = cudaMalloc(&d.counters, kCounterSlots * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc(&d.counters, 2 * kCounterSlots * sizeof(uint32_t));
         d.init_error = e;
     });
     if (d.init_error != cudaSuccess) return cuda_fail(d.init_error, "device set-up");
@@ -92,6 +92,36 @@ int take_counter(DeviceState *d, cudaStream_t s, uint32_t **counter)
     uint32_t slot = d->next.fetch_add(1, std::memory_order_relaxed) % kCounterSlots;
     *counter = d->counters + slot;
     CHAOS_CUDA(cudaMemsetAsync(*counter, 0, sizeof(uint32_t), s), "cudaMemsetAsync(work counter)");
+    return CHAOS_OK;
+}
+
+// The status word that goes with a counter slot (a launch with a time limit
+// and no status word of the caller's), zeroed on the stream.
+int take_status(const DeviceState *d, const uint32_t *counter, cudaStream_t s, uint32_t **status)
+{
+    *status = d->counters + kCounterSlots + (counter - d->counters);
+    CHAOS_CUDA(cudaMemsetAsync(*status, 0, sizeof(uint32_t), s), "cudaMemsetAsync(status word)");
+    return CHAOS_OK;
+}
+
+// A launch's time limit in ns (0: none); false when the limit is negative or not finite.
+bool budget_of(double seconds, unsigned long long *ns)
+{
+    if (!(seconds >= 0.0) || !std::isfinite(seconds)) return false;
+    const double t = seconds * 1e9;
+    *ns = seconds == 0.0 ? 0ull : t < 1.0 ? 1ull : t > 1.8e19 ? 18000000000000000000ull : (unsigned long long)t;
+    return true;
+}
+
+// After a synchronous launch with a time limit: CHAOS_ERR_TIMEOUT when its
+// status word says that the limit ran out.
+int read_status(const uint32_t *status, cudaStream_t s, double seconds)
+{
+    uint32_t bits = 0;
+    CHAOS_CUDA(cudaMemcpyAsync(&bits, status, sizeof bits, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync(status)");
+    CHAOS_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    if (bits & RUN_STATUS_TIMEOUT)
+        return fail(CHAOS_ERR_TIMEOUT, "the launch ran past its time limit of %g s: outputs incomplete", seconds);
     return CHAOS_OK;
 }
 
@@ -284,6 +314,18 @@ int api_device_counter(cudaStream_t s, uint32_t **counter, int *sms)
     *sms = d->sms;
     return take_counter(d, s, counter);
 }
+
+int api_device_status(const uint32_t *counter, cudaStream_t s, uint32_t **status)
+{
+    DeviceState *d;
+    int rc = device_state(&d);
+    if (rc) return rc;
+    return take_status(d, counter, s, status);
+}
+
+bool api_budget(double seconds, unsigned long long *ns) { return budget_of(seconds, ns); }
+
+int api_read_status(const uint32_t *status, cudaStream_t s, double seconds) { return read_status(status, s, seconds); }
 }  // namespace chaos
 
 struct chaos_module {
@@ -641,8 +683,11 @@ int chaos_select_precision(const double rect[4], uint32_t width, uint32_t height
 
 // ---- frames ---------------------------------------------------------------
 
+// `status_used` (may be NULL): where an unsynchronised call with a time
+// limit and no out->status reports the status word it gave the kernel.
 template <class R>
-static int frame_impl(const chaos_frame_desc *dsc, const chaos_frame_out *o, cudaStream_t s, bool sync)
+static int frame_impl(const chaos_frame_desc *dsc, const chaos_frame_out *o, cudaStream_t s, bool sync,
+                      uint32_t **status_used)
 {
     DeviceState *d;
     int rc = device_state(&d);
@@ -672,11 +717,21 @@ static int frame_impl(const chaos_frame_desc *dsc, const chaos_frame_out *o, cud
     a.interior_rgba = o->interior_rgba;
     a.total = o->total_iterations;
     a.skipped = o->cycle_skipped;
+    budget_of(dsc->time_limit_s, &a.budget_ns);
     if ((rc = take_counter(d, s, &a.counter))) return rc;
-    return finish(launch_frame<R>(a, arith_of(dsc->arith), (int)dsc->fractal, d->sms, s), s, sync);
+    a.status = o->status;
+    if (a.budget_ns && !a.status) {
+        if (!sync && !status_used)
+            return fail(CHAOS_ERR_INVALID_ARGUMENT, "a time limit on an unsynchronised frame needs out->status");
+        if ((rc = take_status(d, a.counter, s, &a.status))) return rc;
+    }
+    if (status_used) *status_used = a.budget_ns ? a.status : nullptr;
+    if ((rc = finish(launch_frame<R>(a, arith_of(dsc->arith), (int)dsc->fractal, d->sms, s), s, sync))) return rc;
+    return sync && a.budget_ns ? read_status(a.status, s, dsc->time_limit_s) : CHAOS_OK;
 }
 
-static int frame_entry(const chaos_frame_desc *dsc, const chaos_frame_out *o, cudaStream_t s, bool sync)
+static int frame_entry(const chaos_frame_desc *dsc, const chaos_frame_out *o, cudaStream_t s, bool sync,
+                       uint32_t **status_used = nullptr)
 {
     if (!dsc || !o) return fail(CHAOS_ERR_INVALID_ARGUMENT, "NULL argument");
     int rc = check_size(dsc->width, dsc->height);
@@ -697,8 +752,10 @@ static int frame_entry(const chaos_frame_desc *dsc, const chaos_frame_out *o, cu
         return fail(CHAOS_ERR_INVALID_ARGUMENT, "rgba output needs a palette");
     if (dsc->arith != CHAOS_ARITH_FMA && dsc->arith != CHAOS_ARITH_PARITY)
         return fail(CHAOS_ERR_UNSUPPORTED, "frames take CHAOS_ARITH_FMA or CHAOS_ARITH_PARITY");
-    if (dsc->tier == CHAOS_TIER_F32) return frame_impl<float>(dsc, o, s, sync);
-    if (dsc->tier == CHAOS_TIER_F64) return frame_impl<double>(dsc, o, s, sync);
+    unsigned long long ns = 0;
+    if (!budget_of(dsc->time_limit_s, &ns)) return fail(CHAOS_ERR_INVALID_ARGUMENT, "time_limit_s must be >= 0");
+    if (dsc->tier == CHAOS_TIER_F32) return frame_impl<float>(dsc, o, s, sync, status_used);
+    if (dsc->tier == CHAOS_TIER_F64) return frame_impl<double>(dsc, o, s, sync, status_used);
     return fail(CHAOS_ERR_UNSUPPORTED, "unknown tier %u", dsc->tier);
 }
 
@@ -780,14 +837,15 @@ int chaos_render_frame_host(const chaos_frame_desc *desc, const uint32_t *palett
     o.palette_len = palette_len;
     o.interior_rgba = interior_rgba;
     o.total_iterations = ws.total;
-    if ((rc = frame_entry(desc, &o, s, false))) return rc;
+    uint32_t *status = nullptr;
+    if ((rc = frame_entry(desc, &o, s, false, &status))) return rc;
     CHAOS_CUDA(cudaMemcpyAsync(rgba_host, ws.rgba, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s),
                "cudaMemcpyAsync(rgba)");
     unsigned long long total = 0;
     CHAOS_CUDA(cudaMemcpyAsync(&total, ws.total, sizeof total, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync(total)");
     CHAOS_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
     if (total_host) *total_host = total;
-    return CHAOS_OK;
+    return status ? read_status(status, s, desc->time_limit_s) : CHAOS_OK;
 }
 
 int chaos_measure_fma_peak(uint32_t tier, double *flops_per_second)

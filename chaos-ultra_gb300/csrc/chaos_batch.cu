@@ -25,6 +25,7 @@
 namespace chaos {
 
 int api_fail(int code, const char *fmt, ...);  // chaos_api.cu
+bool api_budget(double seconds, unsigned long long *ns);
 int api_orbit_create_d(double center_x, double center_y, uint32_t bits, uint32_t max_iterations,
                        chaos_orbit **out);  // chaos_perturb.cu
 int api_perturb_enqueue(const chaos_frame_desc *desc, const chaos_orbit *orbit, const chaos_frame_out *out,
@@ -50,6 +51,8 @@ struct BatchArgs {
     const uint32_t *palette;
     uint32_t palette_len;
     uint32_t interior_rgba;
+    unsigned long long budget_ns;  // 0, or the run time after which warps stop (RUN_STATUS_TIMEOUT into *status)
+    uint32_t *status;
 };
 
 // Number policies: binary32, binary64 (fused multiply-adds) and float-float.
@@ -146,7 +149,10 @@ template <class N, int K> __global__ void __launch_bounds__(512) k_batch(BatchAr
         acc[0] = acc[1] = acc[2] = acc[3] = 0.f;
     };
 
+    const unsigned long long t_start = a.budget_ns ? global_ns() : 0ull;
     for (;;) {
+        // a time limit: the warp stops where it is (its samples in flight stay unwritten)
+        if (out_of_time(a.budget_ns, t_start, a.status, lane)) break;
         uint32_t need_mask = __ballot_sync(FULLM, need);
         if (need_mask) {
             uint32_t leader = __ffs(need_mask) - 1u;
@@ -472,7 +478,10 @@ struct chaos_batch {
     BatchViewport *d_vps[kTiers] = {nullptr, nullptr, nullptr};
     uint32_t n_vp[kTiers] = {0, 0, 0}, n_jobs[kTiers] = {0, 0, 0};
     uint32_t *d_counters = nullptr;
+    // [0] pixel-iterations, [1] iterations proven interior and not run,
+    // [2] low word: the RUN_STATUS_* bits of the last launch
     unsigned long long *d_total = nullptr;
+    unsigned long long budget_ns = 0;  // each launch's time limit (0: none)
     const uint32_t *palette = nullptr;
     uint32_t palette_len = 0, interior = 0;
     int threads[kTiers] = {256, 256, 256}, k[kTiers] = {16, 16, 16}, chunk[kTiers] = {1, 1, 1};
@@ -517,7 +526,7 @@ static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s
 {
     // work counters: one per tier kernel, then one per perturbation viewport
     cudaError_t e = cudaMemsetAsync(b->d_counters, 0, (kTiers + b->perturb.size()) * sizeof(uint32_t), s0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_total, 0, 2 * sizeof(unsigned long long), s0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_total, 0, 3 * sizeof(unsigned long long), s0);
     if (e == cudaSuccess) e = cudaEventRecord(fork, s0);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s1, fork, 0);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, fork, 0);
@@ -579,6 +588,8 @@ static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s
         a.palette = b->palette;
         a.palette_len = b->palette_len;
         a.interior_rgba = b->interior;
+        a.budget_ns = b->budget_ns;
+        a.status = reinterpret_cast<uint32_t *>(b->d_total + 2);
         cudaStream_t s = shared ? s0 : st[oi];
         const bool after = shared && t != 2;
         if (t == 0) e = launch_batch<float>(a, b->threads[t], b->k[t], b->sms, per_sm[t], after, s);
@@ -602,6 +613,8 @@ static cudaError_t batch_enqueue(chaos_batch *b, cudaStream_t s0, cudaStream_t s
         a.palette = b->palette;
         a.palette_len = b->palette_len;
         a.interior_rgba = b->interior;
+        a.budget_ns = b->budget_ns;
+        a.status = reinterpret_cast<uint32_t *>(b->d_total + 2);
         e = b->rounded64 ? launch_batch<R64>(a, b->threads[2], b->k[2], b->sms, 0, true, s0)
                          : launch_batch<double>(a, b->threads[2], b->k[2], b->sms, 0, true, s0);
     }
@@ -712,6 +725,10 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
             }
         }
         if (cfg->fp64_warps_per_sm) b->fp64_warps = (int)cfg->fp64_warps_per_sm;
+        if (!api_budget(cfg->time_limit_s, &b->budget_ns)) {
+            batch_free(b);
+            return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "time_limit_s must be >= 0");
+        }
         if (b->fp64_warps < 1 || b->fp64_warps > 32) {
             batch_free(b);
             return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "fp64_warps_per_sm must be 1..32");
@@ -720,7 +737,7 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
     size_t n_perturb = 0;
     for (uint32_t k = 0; k < n; k++) n_perturb += tiers[k] == CHAOS_TIER_PERTURB_F32 || tiers[k] == CHAOS_TIER_PERTURB_F64;
     cudaError_t e = cudaMalloc(&b->d_counters, (kTiers + n_perturb) * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_total, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_total, 3 * sizeof(unsigned long long));
     // reference orbits of the perturbation viewports (host, multi-word)
     for (uint32_t k = 0; k < n && e == cudaSuccess; k++) {
         if (tiers[k] != CHAOS_TIER_PERTURB_F32 && tiers[k] != CHAOS_TIER_PERTURB_F64) continue;
@@ -742,6 +759,7 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
         j.desc.fractal = 0;
         j.desc.seed = v.seed;
         j.desc.pixel_size = v.pixel_size;
+        j.desc.time_limit_s = cfg ? cfg->time_limit_s : 0.0;
         j.out.counts = v.counts;
         j.out.smooth = v.smooth;
         j.out.rgba = v.rgba;
@@ -749,6 +767,7 @@ int chaos_batch_create(const chaos_viewport *vps, uint32_t n, const uint32_t *pa
         j.out.palette_len = palette_len;
         j.out.interior_rgba = interior_rgba;
         j.out.total_iterations = b->d_total;
+        j.out.status = reinterpret_cast<uint32_t *>(b->d_total + 2);
         b->perturb.push_back(j);
     }
     for (int t = 0; t < kTiers && e == cudaSuccess; t++) {
@@ -832,6 +851,14 @@ int chaos_batch_read_cycle_skipped(const chaos_batch *b, unsigned long long *ski
     if (!b || !skipped) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "bad argument");
     cudaError_t e = cudaMemcpy(skipped, b->d_total + 1, sizeof *skipped, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "read skipped: %s", cudaGetErrorString(e));
+    return CHAOS_OK;
+}
+
+int chaos_batch_read_status(const chaos_batch *b, uint32_t *status)
+{
+    if (!b || !status) return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "bad argument");
+    cudaError_t e = cudaMemcpy(status, b->d_total + 2, sizeof *status, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "read status: %s", cudaGetErrorString(e));
     return CHAOS_OK;
 }
 

@@ -96,6 +96,32 @@ __device__ __forceinline__ void divmod_magic(uint32_t n, uint32_t d, uint32_t m,
     }
 }
 
+// The GPU's global nanosecond timer (the clock of the persistent kernels'
+// time limits).
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Status bits a persistent kernel ORs into its launch's status word.
+constexpr uint32_t RUN_STATUS_TIMEOUT = 1u;  // the launch's time limit ran out: outputs incomplete
+
+// A warp-uniform time-limit check: true (and the status bit set once per
+// warp) when `budget_ns` is non-zero and the warp has run longer than it
+// since `t0` (lane 0's clock).
+__device__ __forceinline__ bool out_of_time(unsigned long long budget_ns, unsigned long long t0, uint32_t *status,
+                                            uint32_t lane)
+{
+    if (!budget_ns) return false;
+    uint32_t late = 0;
+    if (lane == 0) late = global_ns() - t0 > budget_ns ? 1u : 0u;
+    late = __shfl_sync(0xffffffffu, late, 0);
+    if (late && lane == 0 && status) atomicOr(status, RUN_STATUS_TIMEOUT);
+    return late != 0;
+}
+
 // ---------------------------------------------------------------------------
 // Correctly rounded scalar operations.  Every product and sum is rounded on its
 // own unless an fma is written out, so the compiler cannot contract (the
@@ -232,12 +258,6 @@ __device__ __forceinline__ void step_contracted4(double &x, double &y, double cx
     emin = exact ? emin : 0u;
 }
 
-// Up to K steps of the reference loop, each with its own test (binary32
-// frames): stops at a state that tests >= 4 (esc, r2 = its test value) or
-// after `lim` steps when BOUNDED.  Returns the steps taken.  In rounded
-// arithmetic the test's products are the step's own, so a test costs one add,
-// a compare and a branch; a lane that stops waits for its warp at the end of
-// the block.  Exact for every c, with no roll-back or search.
 // Exact cycle detection (Brent's method on checkpoints).  The rounded
 // iteration is deterministic, so once a state repeats bit for bit the orbit
 // cycles through states that all tested below 4 and never escapes: the
@@ -245,12 +265,17 @@ __device__ __forceinline__ void step_contracted4(double &x, double &y, double cx
 // many steps remain.  A checkpoint comes at the end of every full block of a
 // sample (a fixed number of steps); the state there is compared with the one
 // saved at the last power-of-two checkpoint (the saved state moves at
-// checkpoints 1, 2, 4, 8, ...).  Equal states under == (a zero's sign aside,
-// which changes no later magnitude) prove the cycle.  A check costs two
-// compares per block.
+// checkpoints 1, 2, 4, 8, ...).  Equal states prove the cycle: binary64
+// states are compared as bit patterns (on the integer units, beside the
+// binary64 pipe's step), binary32 ones under == (where only a zero's sign
+// can differ between equal values, and it changes no later magnitude).
 constexpr uint32_t CYCLE_SPAN = 16;  // steps between checkpoints in the tested binary32 blocks
 
-template <class T> __device__ __forceinline__ bool same_state(T a, T b) { return a == b; }
+__device__ __forceinline__ bool same_state(float a, float b) { return a == b; }
+__device__ __forceinline__ bool same_state(double a, double b)
+{
+    return __double_as_longlong(a) == __double_as_longlong(b);
+}
 
 template <class T> struct CycleWatch {
     T sx, sy;
@@ -275,18 +300,24 @@ template <class T> struct CycleWatch {
         return false;
     }
     // Called at every full block; a checkpoint at every N-th one.  Binary64
-    // loops take N = 4: there the compares compete with the integer half of
-    // the rounded step and repeats are rare at the depths binary64 serves, so
-    // checkpoints every 64 steps cost little and find most cycles a little
-    // later.
+    // loops take N = 8: there repeats are rare at the depths binary64 serves
+    // and every instruction beside the step costs, so checkpoints every 128
+    // steps cost little (0.4 % of a deep frame without cycles) and find most
+    // cycles a little later.
     template <int N> __device__ __forceinline__ bool check_every(T x, T y)
     {
         if (N > 1 && ((++tick) & (uint32_t)(N - 1)) != 0u) return false;
         return check(x, y);
     }
 };
-template <class T> constexpr int cycle_blocks() { return sizeof(T) == 8 ? 4 : 1; }
+template <class T> constexpr int cycle_blocks() { return sizeof(T) == 8 ? 8 : 1; }
 
+// Up to K steps of the reference loop, each with its own test (binary32
+// frames): stops at a state that tests >= 4 (esc, r2 = its test value) or
+// after `lim` steps when BOUNDED.  Returns the steps taken.  In rounded
+// arithmetic the test's products are the step's own, so a test costs one add,
+// a compare and a branch; a lane that stops waits for its warp at the end of
+// the block.  Exact for every c, with no roll-back or search.
 // With a CycleWatch (unbounded blocks only, K a multiple of CYCLE_SPAN), a
 // checkpoint comes after every CYCLE_SPAN steps; `cyc` reports a repeat.
 template <class R, int A, int K, bool BOUNDED>
@@ -469,7 +500,7 @@ __device__ __forceinline__ void ff_step(FF &x, FF &y, FF cx, FF cy)
 
 __device__ __forceinline__ float ff_radius2(FF x, FF y) { return __fmaf_rn(x.hi, x.hi, __fmul_rn(y.hi, y.hi)); }
 
-template <> __device__ __forceinline__ bool same_state<FF>(FF a, FF b) { return a.hi == b.hi && a.lo == b.lo; }
+__device__ __forceinline__ bool same_state(FF a, FF b) { return same_state(a.hi, b.hi) && same_state(a.lo, b.lo); }
 
 // The escape loop of escape() in float-float: blocks of ESCAPE_BLOCK untested
 // steps while |c| <= 1.9975 (after an escape the leading words grow until
@@ -758,55 +789,64 @@ __device__ __forceinline__ PixelInfo render_main_tile(const SampleGeometry<R> &g
 // ---------------------------------------------------------------------------
 
 // getWarpingOriginOfSampleReuse, gen.cu:194-203 (contracted: the pixel's
-// position in the plane and the y flip are fused multiply-adds)
+// position in the plane and the y flip are fused multiply-adds).  The origin
+// is separable: its x depends on the pixel's column only, its y on the
+// pixel's row only, so a warp can compute each once per column and row.
 template <class R, int A = ARITH_PARITY>
-__device__ __forceinline__ void warping_origin(UInt2 p, UInt2 grid, const Rect<R> &cur, const Rect<R> &old, float &ox,
-                                               float &oy)
+__device__ __forceinline__ float warping_origin_x(uint32_t px, UInt2 grid, const Rect<R> &cur, const Rect<R> &old)
 {
     using O = Op<R>;
-    uint32_t qy = grid.y - p.y;
-    R ppx, ppy;
-    if (A == ARITH_CONTRACTED) {
-        ppx = O::fma(O::div((R)p.x, (R)grid.x), O::sub(cur.rtx, cur.lbx), cur.lbx);
-        ppy = O::fma(O::div((R)qy, (R)grid.y), O::sub(cur.rty, cur.lby), cur.lby);
-    } else {
-        ppx = O::add(O::mul(O::div((R)p.x, (R)grid.x), O::sub(cur.rtx, cur.lbx)), cur.lbx);
-        ppy = O::add(O::mul(O::div((R)qy, (R)grid.y), O::sub(cur.rty, cur.lby)), cur.lby);
-    }
+    R ppx;
+    if (A == ARITH_CONTRACTED)
+        ppx = O::fma(O::div((R)px, (R)grid.x), O::sub(cur.rtx, cur.lbx), cur.lbx);
+    else
+        ppx = O::add(O::mul(O::div((R)px, (R)grid.x), O::sub(cur.rtx, cur.lbx)), cur.lbx);
     R rx = O::div(O::sub(ppx, old.lbx), O::sub(old.rtx, old.lbx));
-    R ry = O::div(O::sub(ppy, old.lby), O::sub(old.rty, old.lby));
-    ox = __fmul_rn((float)rx, (float)grid.x);
-    if (A == ARITH_CONTRACTED) {
-        oy = __fmaf_rn(-(float)ry, (float)grid.y, (float)grid.y);
-    } else {
-        float oyv = __fmul_rn((float)ry, (float)grid.y);
-        oy = __fsub_rn((float)grid.y, oyv);
-    }
+    return __fmul_rn((float)rx, (float)grid.x);
 }
 
-// readFromArrayUsingFiltering<float>, gen.cu:259-302 (contracted: each term
-// after the first is a fused multiply-add onto the sum so far, the first two
-// as fma(w00, T00, w10*T10))
-template <int A = ARITH_PARITY>
-__device__ __forceinline__ void filter_bilinear(float alpha, float beta, float2 a, float2 b, float2 c, float2 d,
-                                                float &value, float &weight);
-
-template <int A = ARITH_PARITY>
-__device__ __forceinline__ void read_filtered(const void *in, long pitch, float x, float y, float &value, float &weight)
+template <class R, int A = ARITH_PARITY>
+__device__ __forceinline__ float warping_origin_y(uint32_t py, UInt2 grid, const Rect<R> &cur, const Rect<R> &old)
 {
-    uint32_t i = (uint32_t)floorf(x), j = (uint32_t)floorf(y);
-    float alpha = __fsub_rn(x, (float)i), beta = __fsub_rn(y, (float)j);
-    PixelInfo a = load_pixel(pixel_ptr(in, pitch, i, j));
-    PixelInfo b = load_pixel(pixel_ptr(in, pitch, i + 1, j));
-    PixelInfo c = load_pixel(pixel_ptr(in, pitch, i, j + 1));
-    PixelInfo d = load_pixel(pixel_ptr(in, pitch, i + 1, j + 1));
-    filter_bilinear<A>(alpha, beta, make_float2(a.value, a.weight), make_float2(b.value, b.weight),
-                       make_float2(c.value, c.weight), make_float2(d.value, d.weight), value, weight);
+    using O = Op<R>;
+    uint32_t qy = grid.y - py;
+    R ppy;
+    if (A == ARITH_CONTRACTED)
+        ppy = O::fma(O::div((R)qy, (R)grid.y), O::sub(cur.rty, cur.lby), cur.lby);
+    else
+        ppy = O::add(O::mul(O::div((R)qy, (R)grid.y), O::sub(cur.rty, cur.lby)), cur.lby);
+    R ry = O::div(O::sub(ppy, old.lby), O::sub(old.rty, old.lby));
+    if (A == ARITH_CONTRACTED) return __fmaf_rn(-(float)ry, (float)grid.y, (float)grid.y);
+    return __fsub_rn((float)grid.y, __fmul_rn((float)ry, (float)grid.y));
 }
 
-// The filter of readFromArrayUsingFiltering on the four neighbours (value,
-// weight) a = (i, j), b = (i+1, j), c = (i, j+1), d = (i+1, j+1).
-template <int A>
+// One coordinate of the reuse read (gen.cu:320-331): the range test of the
+// rounded origin (>= 2 and < n - 2) and the filter's corner and weight
+// (floor, fraction).  `at` holds the corner with bit 31 set when the
+// coordinate is in range.  Frames narrower than 5 pixels reuse nothing:
+// there the reference's test (an unsigned n - 2) can pass for a corner
+// outside the frame.
+struct ReuseAxis {
+    uint32_t at;
+    float frac;
+};
+
+__device__ __forceinline__ ReuseAxis reuse_axis(float o, uint32_t n)
+{
+    const int oi = (int)roundf(o);
+    const bool ok = n >= 5u && !(oi < 2 || (uint32_t)oi >= n - 2u);
+    const uint32_t f = (uint32_t)floorf(o);
+    ReuseAxis r;
+    r.frac = __fsub_rn(o, (float)f);
+    r.at = ok ? (f | 0x80000000u) : 0u;
+    return r;
+}
+
+// The filter of readFromArrayUsingFiltering<float> (gen.cu:259-302) on the
+// four neighbours (value, weight) a = (i, j), b = (i+1, j), c = (i, j+1),
+// d = (i+1, j+1) (contracted: each term after the first is a fused
+// multiply-add onto the sum so far, the first two as fma(w00, T00, w10*T10)).
+template <int A = ARITH_PARITY>
 __device__ __forceinline__ void filter_bilinear(float alpha, float beta, float2 a2, float2 b2, float2 c2, float2 d2,
                                                 float &value, float &weight)
 {
@@ -865,35 +905,67 @@ __device__ __forceinline__ void foveation(UInt2 p, UInt2 focus, float max_ss, fl
     advised = adv;
 }
 
-// fractalRenderAdvanced for one lane of an 8x4 warp tile (gen.cu:307-368).
-// Lanes that reach the same sampleTheFractal call site vote together.
-// Returns the record stored for the lane's pixel.
+// The previous-frame read of sample reuse for one lane (gen.cu:320-331:
+// getWarpingOriginOfSampleReuse, the range test, readFromArrayUsingFiltering),
+// in two halves so that a warp can put the reads of several tiles in flight
+// before it filters any of them: reuse_fetch issues the four neighbours'
+// (value, weight) loads for the column and row terms of the lane's pixel,
+// reuse_filter combines them.  An origin outside the reusable range reads
+// record (0, 0) four times (a record of every non-empty frame; its value is
+// not used), so the loads need no branch.  AL8: the previous frame's base and
+// pitch are multiples of 8 bytes, and each pair is one 8-byte load.
+struct ReuseFetch {
+    float2 a, b, c, d;
+    float alpha, beta;
+    bool in_range;
+};
+
+template <bool AL8> __device__ __forceinline__ float2 load_value_weight(const char *p)
+{
+    if (AL8) return __ldg(reinterpret_cast<const float2 *>(p));
+    const float *q = reinterpret_cast<const float *>(p);
+    return make_float2(__ldg(q), __ldg(q + 1));
+}
+
+template <bool AL8>
+__device__ __forceinline__ ReuseFetch reuse_fetch(ReuseAxis ax, ReuseAxis ay, const void *in, long in_pitch)
+{
+    ReuseFetch f;
+    f.in_range = ((ax.at & ay.at) >> 31) != 0u;
+    f.alpha = ax.frac;
+    f.beta = ay.frac;
+    const uint32_t i = f.in_range ? ax.at & 0x7fffffffu : 0u, j = f.in_range ? ay.at & 0x7fffffffu : 0u;
+    const long dx = f.in_range ? (long)sizeof(PixelInfo) : 0, dy = f.in_range ? in_pitch : 0;
+    const char *q = reinterpret_cast<const char *>(pixel_ptr(in, in_pitch, i, j));
+    f.a = load_value_weight<AL8>(q);
+    f.b = load_value_weight<AL8>(q + dx);
+    f.c = load_value_weight<AL8>(q + dy);
+    f.d = load_value_weight<AL8>(q + dy + dx);
+    return f;
+}
+
+template <int A> __device__ __forceinline__ void reuse_filter(const ReuseFetch &f, float &value, float &weight)
+{
+    filter_bilinear<A>(f.alpha, f.beta, f.a, f.b, f.c, f.d, value, weight);
+}
+
+// The rest of fractalRenderAdvanced for one lane of an 8x4 warp tile
+// (gen.cu:332-368), given the lane's reuse result: foveation, the vote
+// groups (lanes that reach the same sampleTheFractal call site vote
+// together), the samples, the record.  `reusing` is false for lanes outside
+// the image and without the sample-reuse flag.  Returns the record stored.
 template <class R, int A, int F>
-__device__ __forceinline__ PixelInfo render_advanced_tile(const SampleGeometry<R> &g, const Rect<R> &image,
-                                                          const Rect<R> &image_reused, void *out, long pitch,
-                                                          UInt2 size, const void *in, long in_pitch, UInt2 focus,
-                                                          uint32_t x0, uint32_t y0, uint32_t lane, float max_ss,
-                                                          uint32_t flags, unsigned long long &iters)
+__device__ __forceinline__ PixelInfo finish_advanced_tile(const SampleGeometry<R> &g, void *out, long pitch, UInt2 size,
+                                                          UInt2 focus, uint32_t x0, uint32_t y0, uint32_t lane,
+                                                          float max_ss, uint32_t flags, bool reusing, float reused_v,
+                                                          float reused_w, unsigned long long &iters)
 {
     UInt2 p = tile_pixel(x0, y0, lane);
     bool valid = p.x < size.x && p.y < size.y;
     float advised = max_ss;
     bool inside = false;
-    bool reusing = false;
-    float reused_v = 0.f, reused_w = 0.f;
-    if (valid) {
-        if ((flags & FLAG_FOVEATION) && (flags & FLAG_IS_ZOOMING) && (flags & FLAG_ZOOMING_IN))
-            foveation<A>(p, focus, max_ss, advised, inside);
-        if (flags & FLAG_SAMPLE_REUSE) {
-            float ox, oy;
-            warping_origin<R, A>(p, size, image, image_reused, ox, oy);
-            int oix = (int)roundf(ox), oiy = (int)roundf(oy);
-            if (!(oix < 2 || (uint32_t)oix >= size.x - 2 || oiy < 2 || (uint32_t)oiy >= size.y - 2)) {
-                read_filtered<A>(in, in_pitch, ox, oy, reused_v, reused_w);
-                reusing = !(reused_w < 0.1f);
-            }
-        }
-    }
+    if (valid && (flags & FLAG_FOVEATION) && (flags & FLAG_IS_ZOOMING) && (flags & FLAG_ZOOMING_IN))
+        foveation<A>(p, focus, max_ss, advised, inside);
     bool group_a = valid && reusing && (flags & FLAG_ZOOMING_IN) && inside;
     bool group_b = valid && !reusing;
     uint32_t mask_a = __ballot_sync(0xffffffffu, group_a);
@@ -922,6 +994,34 @@ __device__ __forceinline__ PixelInfo render_advanced_tile(const SampleGeometry<R
     }
     if (valid) store_pixel(pixel_ptr(out, pitch, p.x, p.y), res);
     return res;
+}
+
+// fractalRenderAdvanced for one lane of an 8x4 warp tile (gen.cu:307-368).
+// Returns the record stored for the lane's pixel.
+template <class R, int A, int F>
+__device__ __forceinline__ PixelInfo render_advanced_tile(const SampleGeometry<R> &g, const Rect<R> &image,
+                                                          const Rect<R> &image_reused, void *out, long pitch,
+                                                          UInt2 size, const void *in, long in_pitch, UInt2 focus,
+                                                          uint32_t x0, uint32_t y0, uint32_t lane, float max_ss,
+                                                          uint32_t flags, unsigned long long &iters)
+{
+    UInt2 p = tile_pixel(x0, y0, lane);
+    bool valid = p.x < size.x && p.y < size.y;
+    bool reusing = false;
+    float reused_v = 0.f, reused_w = 0.f;
+    if (valid && (flags & FLAG_SAMPLE_REUSE)) {
+        const ReuseAxis ax = reuse_axis(warping_origin_x<R, A>(p.x, size, image, image_reused), size.x);
+        const ReuseAxis ay = reuse_axis(warping_origin_y<R, A>(p.y, size, image, image_reused), size.y);
+        const ReuseFetch f = ((reinterpret_cast<uintptr_t>(in) | (uintptr_t)in_pitch) & 7u) == 0
+                                 ? reuse_fetch<true>(ax, ay, in, in_pitch)
+                                 : reuse_fetch<false>(ax, ay, in, in_pitch);
+        if (f.in_range) {
+            reuse_filter<A>(f, reused_v, reused_w);
+            reusing = !(reused_w < 0.1f);
+        }
+    }
+    return finish_advanced_tile<R, A, F>(g, out, pitch, size, focus, x0, y0, lane, max_ss, flags, reusing, reused_v,
+                                         reused_w, iters);
 }
 
 // ---------------------------------------------------------------------------

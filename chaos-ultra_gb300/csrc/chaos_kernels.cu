@@ -65,8 +65,11 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
     float acc_v = 0.f, acc[4] = {0.f, 0.f, 0.f, 0.f};
     unsigned long long iters = 0, skipped = 0;
     CycleWatch<R> cw;  // exact cycle detection (see CycleWatch)
+    const unsigned long long t_start = a.budget_ns ? global_ns() : 0ull;
 
     for (;;) {
+        // a time limit: the warp stops where it is (its samples in flight stay unwritten)
+        if (out_of_time(a.budget_ns, t_start, a.status, lane)) break;
         uint32_t need_mask = __ballot_sync(FULL, need);
         if (need_mask) {
             uint32_t leader = __ffs(need_mask) - 1u;

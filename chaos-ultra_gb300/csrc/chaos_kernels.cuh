@@ -66,6 +66,8 @@ template <class R> struct FrameArgs {
     unsigned long long *total;
     uint32_t *counter;
     unsigned long long *skipped;  // optional: iterations of interior samples proven by a repeated state, not run
+    unsigned long long budget_ns; // 0, or the run time after which warps stop (RUN_STATUS_TIMEOUT into *status)
+    uint32_t *status;
 };
 
 struct ComposeArgs {

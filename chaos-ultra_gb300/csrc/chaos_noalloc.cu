@@ -137,6 +137,8 @@ int chaos_render_frame_host_noalloc(const chaos_frame_desc *desc, const uint32_t
         return api_fail(CHAOS_ERR_UNSUPPORTED, "tier %u has no no-alloc variant", desc->tier);
     if (desc->arith != CHAOS_ARITH_FMA && desc->arith != CHAOS_ARITH_PARITY)
         return api_fail(CHAOS_ERR_UNSUPPORTED, "frames take CHAOS_ARITH_FMA or CHAOS_ARITH_PARITY");
+    if (desc->time_limit_s != 0.0)
+        return api_fail(CHAOS_ERR_UNSUPPORTED, "the no-alloc frame takes no time limit (time_limit_s = 0)");
     if (!std::isfinite(desc->center_x) || !std::isfinite(desc->center_y) || !(desc->pixel_size > 0) ||
         !std::isfinite(desc->pixel_size))
         return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "centre and pixel size must be finite, pixel size > 0");

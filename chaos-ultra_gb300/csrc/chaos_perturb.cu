@@ -47,6 +47,9 @@ namespace chaos {
 
 int api_fail(int code, const char *fmt, ...);  // chaos_api.cu
 int api_device_counter(cudaStream_t s, uint32_t **counter, int *sms);
+int api_device_status(const uint32_t *counter, cudaStream_t s, uint32_t **status);
+bool api_budget(double seconds, unsigned long long *ns);
+int api_read_status(const uint32_t *status, cudaStream_t s, double seconds);
 
 template <class D> struct Vec2T;
 template <> struct Vec2T<float> {
@@ -79,6 +82,8 @@ template <class D> struct PerturbArgs {
     unsigned long long *total;
     unsigned long long *rebases;
     uint32_t *counter;
+    unsigned long long budget_ns;  // 0, or the run time after which warps stop (RUN_STATUS_TIMEOUT into *status)
+    uint32_t *status;
 };
 
 __device__ __forceinline__ double unit53(uint64_t h) { return (double)(h >> 11) * 0x1p-53; }
@@ -151,8 +156,11 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
     bool need = true, begin = false;
     float acc_v = 0.f, acc[4] = {0.f, 0.f, 0.f, 0.f};
     unsigned long long iters = 0, rebases = 0;
+    const unsigned long long t_start = a.budget_ns ? global_ns() : 0ull;
 
     for (;;) {
+        // a time limit: the warp stops where it is (its samples in flight stay unwritten)
+        if (out_of_time(a.budget_ns, t_start, a.status, lane)) break;
         uint32_t need_mask = __ballot_sync(FULLM, need);
         if (need_mask) {
             uint32_t leader = __ffs(need_mask) - 1u;
@@ -677,6 +685,9 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
     a.interior_rgba = o->interior_rgba;
     a.total = o->total_iterations;
     a.rebases = o->rebases;
+    a.status = o->status;
+    if (!api_budget(d->time_limit_s, &a.budget_ns))
+        return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "time_limit_s must be >= 0");
     int sms = 0;
     if (counter) {
         a.counter = counter;
@@ -685,6 +696,12 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     } else {
         int rc = api_device_counter(s, &a.counter, &sms);
+        if (rc) return rc;
+    }
+    if (a.budget_ns && !a.status) {
+        if (!sync || counter)
+            return api_fail(CHAOS_ERR_INVALID_ARGUMENT, "a time limit on an unsynchronised frame needs out->status");
+        int rc = api_device_status(a.counter, s, &a.status);
         if (rc) return rc;
     }
     // binary32 differences are rescaled below pixel 1e-30 (2^-100)
@@ -697,6 +714,7 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
     if (sync) {
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return api_fail(CHAOS_ERR_CUDA, "cudaStreamSynchronize: %s", cudaGetErrorString(e));
+        if (a.budget_ns) return api_read_status(a.status, s, d->time_limit_s);
     }
     return CHAOS_OK;
 }

@@ -21,37 +21,54 @@ __device__ __forceinline__ void add_total(unsigned long long *total, unsigned lo
     if (lane == 0 && iters) atomicAdd(total, iters);
 }
 
-// Tiles are claimed `chunk` at a time (consecutive, so a claim is a strip of one
-// tile row), and the next claim is issued before the current strip is
-// rendered.  With one counter for the whole frame, a claim per tile made the
-// counter the bottleneck of large reuse-dominated frames, whose tiles take a
-// few loads each; small frames keep claims of one tile made when needed, the
-// finest balance (serving latency).
+// Tiles are claimed in strips of consecutive tiles, the next claim issued
+// before the current strip is rendered.  With one counter for the whole
+// frame, a claim per tile made the counter the bottleneck of large
+// reuse-dominated frames, whose tiles take a few loads each.  Claims are
+// guided: a quarter of an even share of the tiles left after the warp's
+// previous strip, between 1 and `max_chunk`, so long strips early keep the
+// counter quiet and short ones late keep the end of the frame balanced;
+// single tiles are claimed when needed (the finest balance, small frames).
+template <class Body>
+__device__ __forceinline__ void for_each_strip(uint32_t *counter, uint32_t n_tiles, uint32_t max_chunk, uint32_t lane,
+                                               Body body)
+{
+    const uint32_t share = 4u * gridDim.x * (blockDim.x >> 5);
+    auto size_after = [&](uint32_t at) -> uint32_t {
+        const uint32_t c = (at < n_tiles ? n_tiles - at : 0u) / share;
+        return c < 1u ? 1u : c > max_chunk ? max_chunk : c;
+    };
+    uint32_t size = size_after(0u), claim = 0;
+    if (lane == 0) claim = atomicAdd(counter, size);
+    uint32_t t0 = __shfl_sync(FULL, claim, 0);
+    while (t0 < n_tiles) {
+        const uint32_t t1 = min(t0 + size, n_tiles), next = size_after(t1);
+        if (size > 1u && lane == 0) claim = atomicAdd(counter, next);
+        body(t0, t1);
+        if (size == 1u && lane == 0) claim = atomicAdd(counter, next);
+        t0 = __shfl_sync(FULL, claim, 0);
+        size = next;
+    }
+}
+
 template <class Body>
 __device__ __forceinline__ void for_each_tile(uint32_t *counter, uint32_t n_tiles, uint32_t chunk, uint32_t lane,
                                               Body body)
 {
-    uint32_t claim = 0;
-    if (lane == 0) claim = atomicAdd(counter, chunk);
-    uint32_t t0 = __shfl_sync(FULL, claim, 0);
-    while (t0 < n_tiles) {
-        // with strips, the next strip is claimed while this one is rendered;
-        // single tiles (small frames) are claimed when needed, which keeps the
-        // end of the frame balanced
-        if (chunk > 1 && lane == 0) claim = atomicAdd(counter, chunk);
-        const uint32_t t1 = min(t0 + chunk, n_tiles);
+    for_each_strip(counter, n_tiles, chunk, lane, [&](uint32_t t0, uint32_t t1) {
         for (uint32_t t = t0; t < t1; t++) body(t);
-        if (chunk == 1 && lane == 0) claim = atomicAdd(counter, 1u);
-        t0 = __shfl_sync(FULL, claim, 0);
-    }
+    });
 }
 
-// Tiles per claim: up to 4, while every resident warp still gets 8 claims.
-static inline uint32_t tile_chunk_for(uint32_t n_tiles, int occ, int sms)
+// The longest strip a warp claims: up to `cap` tiles, while every resident
+// warp still gets 8 claims.  (An 8K reuse frame is a million tiles: at 4 per
+// claim its single work counter took a quarter of a million atomics in
+// ~0.3 ms.)
+static inline uint32_t tile_chunk_for(uint32_t n_tiles, int occ, int sms, uint32_t cap = 16)
 {
     const unsigned long long warps = (unsigned long long)occ * sms * (PERSIST_THREADS / 32);
     unsigned long long c = n_tiles / (warps * 8ull);
-    return (uint32_t)(c < 1 ? 1 : c > 4 ? 4 : c);
+    return (uint32_t)(c < 1 ? 1 : c > cap ? cap : c);
 }
 
 template <class R, int A, int F> __global__ void __launch_bounds__(PERSIST_THREADS) k_main(MainArgs<R> a)
@@ -67,17 +84,102 @@ template <class R, int A, int F> __global__ void __launch_bounds__(PERSIST_THREA
     add_total(a.total, iters, lane);
 }
 
+// Tiles whose previous-frame reads are in flight together.  A reuse-dominated
+// frame is a stream of small dependent steps per tile (origin -> four loads
+// -> filter -> store); with one tile's loads in flight per warp and the
+// origin's four divisions computed per pixel it ran at about half the copy
+// rate, bound by the loads' latency and the issue of the divisions.  Two
+// tiles (eight 8-byte loads per lane) measured best: four need registers
+// that cost a fifth of the warps.
+constexpr uint32_t REUSE_BATCH = 2;
+
+// The strip [t0, t1) of a fractalRenderAdvanced frame, in groups of four
+// tiles.  The origin's column and row terms of a group are computed once per
+// column and row (lane l: the column l & 7 of the group's tile l >> 3, and
+// the row l & 3 of its tile (l >> 2) & 3) and taken by shuffles.  Within a
+// group, the previous-frame reads of REUSE_BATCH tiles are issued before the
+// first of them is filtered; the filtered (value, weight) pairs wait in the
+// warp's `stage` (REUSE_BATCH x 32 pairs of shared memory, the weight -1
+// where the origin is out of range), not in registers, while each tile is
+// finished (votes, samples, record) in order and handed to on_tile(x0, y0,
+// record).
+template <class R, int A, int F, bool AL8, class OnTile>
+__device__ __forceinline__ void advanced_strip(const AdvancedArgs<R> &a, const SampleGeometry<R> &g, uint32_t lane,
+                                               float2 *stage, uint32_t t0, uint32_t t1, unsigned long long &iters,
+                                               OnTile on_tile)
+{
+    static_assert(REUSE_BATCH == 1 || REUSE_BATCH == 2 || REUSE_BATCH == 4, "a power of two up to 4");
+    const bool reuse = (a.m.flags & FLAG_SAMPLE_REUSE) != 0;
+    const uint32_t col = 4u * (lane >> 4) + (lane & 3u), row = (lane >> 2) & 3u;
+    for (uint32_t tg = t0; tg < t1; tg += 4u) {
+        const uint32_t ng = min(4u, t1 - tg);
+        ReuseAxis mx{0u, 0.f}, my{0u, 0.f};
+        if (reuse) {
+            // this lane's column and row terms (positions past the group's end repeat its last tile)
+            const uint32_t tc = tg + min(lane >> 3, ng - 1u), tr = tg + min((lane >> 2) & 3u, ng - 1u);
+            mx = reuse_axis(
+                warping_origin_x<R, A>(8u * (tc % a.m.tiles_x) + (lane & 7u), a.m.size, a.m.image, a.image_reused),
+                a.m.size.x);
+            my = reuse_axis(
+                warping_origin_y<R, A>(4u * (tr / a.m.tiles_x) + (lane & 3u), a.m.size, a.m.image, a.image_reused),
+                a.m.size.y);
+        }
+        for (uint32_t kb = 0; kb < ng; kb += REUSE_BATCH) {
+            const uint32_t nb = min(REUSE_BATCH, ng - kb);
+            if (reuse) {
+                ReuseFetch f[REUSE_BATCH];
+#pragma unroll
+                for (uint32_t k = 0; k < REUSE_BATCH; k++) {
+                    // tiles past the batch's end read its last tile's records again (unused)
+                    const uint32_t kk = kb + min(k, nb - 1u);
+                    ReuseAxis ax, ay;
+                    ax.at = __shfl_sync(FULL, mx.at, 8u * kk + col);
+                    ax.frac = __shfl_sync(FULL, mx.frac, 8u * kk + col);
+                    ay.at = __shfl_sync(FULL, my.at, 4u * kk + row);
+                    ay.frac = __shfl_sync(FULL, my.frac, 4u * kk + row);
+                    f[k] = reuse_fetch<AL8>(ax, ay, a.in, a.in_pitch);
+                }
+#pragma unroll
+                for (uint32_t k = 0; k < REUSE_BATCH; k++) {
+                    float v, w;
+                    reuse_filter<A>(f[k], v, w);
+                    stage[32u * k + lane] = make_float2(v, f[k].in_range ? w : -1.f);
+                }
+                __syncwarp();
+            }
+            for (uint32_t k = 0; k < nb; k++) {
+                const uint32_t t = tg + kb + k, x0 = 8u * (t % a.m.tiles_x), y0 = 4u * (t / a.m.tiles_x);
+                const UInt2 p = tile_pixel(x0, y0, lane);
+                const bool valid = p.x < a.m.size.x && p.y < a.m.size.y;
+                const float2 vw = reuse ? stage[32u * k + lane] : make_float2(0.f, 0.f);
+                const PixelInfo rec = finish_advanced_tile<R, A, F>(
+                    g, a.m.out, a.m.pitch, a.m.size, a.focus, x0, y0, lane, a.m.max_ss, a.m.flags,
+                    valid && reuse && !(vw.y < 0.1f), vw.x, vw.y, iters);
+                on_tile(x0, y0, rec);
+            }
+            __syncwarp();
+        }
+    }
+}
+
 template <class R, int A, int F> __global__ void __launch_bounds__(PERSIST_THREADS) k_advanced(AdvancedArgs<R> a)
 {
     const uint32_t lane = threadIdx.x & 31u;
     SampleGeometry<R> g = make_geometry(a.m.image, a.m.size, a.m.max_iter, a.m.jcx, a.m.jcy);
     g.newton = a.m.newton;
     unsigned long long iters = 0;
-    for_each_tile(a.m.counter, a.m.n_tiles, a.m.tile_chunk, lane, [&](uint32_t t) {
-        uint32_t x0 = 8u * (t % a.m.tiles_x), y0 = 4u * (t / a.m.tiles_x);
-        render_advanced_tile<R, A, F>(g, a.m.image, a.image_reused, a.m.out, a.m.pitch, a.m.size, a.in, a.in_pitch,
-                                      a.focus, x0, y0, lane, a.m.max_ss, a.m.flags, iters);
-    });
+    __shared__ float2 s_stage[PERSIST_THREADS / 32][REUSE_BATCH * 32];
+    float2 *stage = s_stage[threadIdx.x >> 5];
+    const bool al8 = ((reinterpret_cast<uintptr_t>(a.in) | (uintptr_t)a.in_pitch) & 7u) == 0;
+    auto none = [](uint32_t, uint32_t, const PixelInfo &) {};
+    if (al8)
+        for_each_strip(a.m.counter, a.m.n_tiles, a.m.tile_chunk, lane, [&](uint32_t t0, uint32_t t1) {
+            advanced_strip<R, A, F, true>(a, g, lane, stage, t0, t1, iters, none);
+        });
+    else
+        for_each_strip(a.m.counter, a.m.n_tiles, a.m.tile_chunk, lane, [&](uint32_t t0, uint32_t t1) {
+            advanced_strip<R, A, F, false>(a, g, lane, stage, t0, t1, iters, none);
+        });
     add_total(a.m.total, iters, lane);
 }
 

@@ -107,13 +107,6 @@ struct ServeTable {
     uint32_t jobs_done[SERVE_MAX_FRAMES];      // finished jobs per frame (zero on arrival)
 };
 
-__device__ __forceinline__ unsigned long long global_ns()
-{
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
 __device__ __forceinline__ uint32_t find_frame(const uint32_t *begin, uint32_t n, uint32_t job)
 {
     uint32_t lo = 0, hi = n - 1;
@@ -778,7 +771,7 @@ int enqueue_launch_locked(chaos_server *srv, Forming &fm)
     // strips of tiles per job, as for single frames: up to 4 while every
     // resident warp still gets 8 jobs
     const int occ_hint = 5;
-    const uint32_t chunk = tile_chunk_for((uint32_t)std::min<uint64_t>(tiles_all, 0xffffffffu), occ_hint, srv->sms);
+    const uint32_t chunk = tile_chunk_for((uint32_t)std::min<uint64_t>(tiles_all, 0xffffffffu), occ_hint, srv->sms, 4);
     for (uint32_t g = 0; g < SERVE_GROUPS; g++) {
         uint32_t acc = 0;
         for (uint32_t j = 0; j < n_group[g]; j++) {

@@ -246,6 +246,13 @@ typedef struct chaos_frame_desc {
     double center_x, center_y;
     double pixel_size;
     double julia_cx, julia_cy;
+    /* 0, or a limit on the frame's kernel run time in seconds: past it every
+     * warp stops where it is (samples in flight stay unwritten), and the
+     * frame completes with CHAOS_ERR_TIMEOUT (chaos_render_frame,
+     * chaos_render_frame_host, chaos_render_frame_perturb) or with
+     * CHAOS_STATUS_TIMEOUT in *out->status (the _async calls, which need
+     * out->status with a limit) */
+    double time_limit_s;
 } chaos_frame_desc;
 
 /* Outputs (device pointers, each optional):
@@ -271,7 +278,12 @@ typedef struct chaos_frame_out {
      * deterministic), so it counts max_iterations without running the rest
      * (binary32 and binary64 tiers; total_iterations counts it in full) */
     unsigned long long *cycle_skipped;
+    /* one uint32 the kernel ORs CHAOS_STATUS_* bits into (zeroed by the
+     * caller; used with desc->time_limit_s) */
+    uint32_t *status;
 } chaos_frame_out;
+
+#define CHAOS_STATUS_TIMEOUT 1u /* the launch's time limit ran out: outputs incomplete */
 
 /* Enqueue one frame (does not synchronise). */
 int chaos_render_frame_async(const chaos_frame_desc *desc, const chaos_frame_out *out, void *stream);
@@ -327,6 +339,10 @@ typedef struct chaos_batch_config {
     uint32_t escape_block[3];  /* 8, 16 or 32 */
     uint32_t chunk[3];         /* 1..64 consecutive pixels a lane claims per work-counter update */
     uint32_t fp64_warps_per_sm; /* 1..32, 0 = 8 */
+    /* 0, or a limit on each launch's kernel run time in seconds: past it every
+     * warp stops where it is (samples in flight stay unwritten) and the
+     * launch's status word gets CHAOS_STATUS_TIMEOUT (chaos_batch_read_status) */
+    double time_limit_s;
 } chaos_batch_config;
 
 typedef struct chaos_batch chaos_batch;
@@ -368,6 +384,9 @@ int chaos_batch_read_total(const chaos_batch *batch, unsigned long long *total);
 /* Iterations of the last launch not run because a sample's state repeated
  * bit for bit (interior; counted in full in the total), copied to the host. */
 int chaos_batch_read_cycle_skipped(const chaos_batch *batch, unsigned long long *skipped);
+/* CHAOS_STATUS_* bits of the last launch (after it has finished): 0, or
+ * CHAOS_STATUS_TIMEOUT when config->time_limit_s ran out. */
+int chaos_batch_read_status(const chaos_batch *batch, uint32_t *status);
 int chaos_batch_destroy(chaos_batch *batch);
 
 /* ---- serving: concurrent zoom sessions ----------------------------------- */
@@ -552,7 +571,8 @@ int chaos_render_frame_perturb(const chaos_frame_desc *desc, const chaos_orbit *
  * so make one call during set-up, before the GPU's memory is handed out and
  * before any stream capture.  A failed look-up is retried by the next call.
  * The call synchronises the stream before it returns.  All calls share the
- * array: calls whose GPU work overlaps race. */
+ * array: calls whose GPU work overlaps race.  It takes no time limit
+ * (desc->time_limit_s must be 0). */
 int chaos_render_frame_host_noalloc(const chaos_frame_desc *desc, const uint32_t *palette, uint32_t palette_len,
                                     uint32_t interior_rgba, uint32_t *rgba_host, unsigned long long *total_host,
                                     void *stream);

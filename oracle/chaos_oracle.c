@@ -563,7 +563,9 @@ void orc_render_advanced(int fractal, int dbl, int arith, void *out, long pitch,
                 float ox, oy;
                 warping_origin(&v, rect_reused, lx[l], ly[l], &ox, &oy);
                 int oix = (int)roundf(ox), oiy = (int)roundf(oy);
-                if (oix < 2 || (uint32_t)oix >= w - 2 || oiy < 2 || (uint32_t)oiy >= h - 2) {
+                /* frames narrower than 5 pixels reuse nothing: there the unsigned
+                   w - 2 of the reference's test can admit a corner outside the frame */
+                if (w < 5 || h < 5 || oix < 2 || (uint32_t)oix >= w - 2 || oiy < 2 || (uint32_t)oiy >= h - 2) {
                     reusing[l] = 0;
                 } else {
                     read_filtered(arith, in, in_pitch, ox, oy, &reused_v[l], &reused_w[l]);

@@ -162,4 +162,7 @@ def test_c1_cycles_skip_iterations_not_counts(cuda, tier):
     want_total, want_interior = (181_032_650, 175_986) if tier == 0 else (181_040_256, 176_008)
     assert int(total.item()) == want_total
     assert int((counts.cpu().numpy() == 1000).sum()) == want_interior
-    assert int(skipped.item()) > want_total // 2  # more than half of the work was interior cycles
+    # binary32 cycles show up sooner (fewer states; a checkpoint every 16 steps
+    # against every 128 in binary64): more than half, resp. a third, of the
+    # work (a numpy restatement of the binary64 checkpoints gives 69,847,176)
+    assert int(skipped.item()) > (want_total // 2 if tier == 0 else want_total // 3)

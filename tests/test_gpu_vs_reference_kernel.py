@@ -52,8 +52,29 @@ def _ours(parity):
     return os.path.join(cg.DROPIN_PARITY_DIR if parity else cg.DROPIN_DIR, "mandelbrot.ptx")
 
 
+def _timed(cuda, run, stream=None):
+    """Mean time of back-to-back launches of `run` (ms): one untimed launch,
+    then enough launches for ~50 ms (1 to 20) between one pair of events, so
+    that the host's launch gap before the first one weighs little on a
+    0.1 ms kernel."""
+    import time
+    cuda.cuda.synchronize()
+    t0 = time.perf_counter()
+    run()
+    cuda.cuda.synchronize()
+    reps = max(1, min(20, int(0.05 / max(time.perf_counter() - t0, 1e-6))))
+    e0, e1 = cuda.cuda.Event(enable_timing=True), cuda.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        run()
+    e1.record(stream)
+    cuda.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
 def _timed_main(drv, cuda, path, w, h, rect, max_iter, max_ss, flags, dbl):
-    """One untimed and one timed launch of fractalRenderMain{Float,Double}; (pixels, ms)."""
+    """fractalRenderMain{Float,Double} of a module in the Java launch shape on
+    the default stream; (pixels of the last launch, mean ms)."""
     mod = drv.load(path)
     try:
         drv.write_constant(mod, "VISUALIZE_SAMPLE_COUNT", b"\0")
@@ -63,13 +84,8 @@ def _timed_main(drv, cuda, path, w, h, rect, max_iter, max_ss, flags, dbl):
         params = main_params(buf.data_ptr(), pitch, w, h, rect, max_iter, max_ss, flags, dbl)
         drv.launch(fn, grid, block, params)
         buf.zero_()
-        e0, e1 = cuda.cuda.Event(enable_timing=True), cuda.cuda.Event(enable_timing=True)
-        cuda.cuda.synchronize()
-        e0.record()
-        drv.launch(fn, grid, block, params, sync=False)
-        e1.record()
-        cuda.cuda.synchronize()
-        return read_pixels(buf, w), e0.elapsed_time(e1)
+        ms = _timed(cuda, lambda: drv.launch(fn, grid, block, params, sync=False))
+        return read_pixels(buf, w), ms
     finally:
         drv.unload(mod)
 
@@ -88,13 +104,8 @@ def _timed_library(cuda, w, h, rect, max_iter, max_ss, flags, dbl):
 
     run()
     buf.zero_()
-    e0, e1 = cuda.cuda.Event(enable_timing=True), cuda.cuda.Event(enable_timing=True)
-    cuda.cuda.synchronize()
-    e0.record(stream)
-    run()
-    e1.record(stream)
-    cuda.cuda.synchronize()
-    return read_pixels(buf, w), e0.elapsed_time(e1)
+    ms = _timed(cuda, run, stream)
+    return read_pixels(buf, w), ms
 
 
 def _compare(drv, cuda, name, w, h, rect, max_iter, max_ss, flags, dbl):
