@@ -910,10 +910,11 @@ __device__ __forceinline__ void foveation(UInt2 p, UInt2 focus, float max_ss, fl
 // in two halves so that a warp can put the reads of several tiles in flight
 // before it filters any of them: reuse_fetch issues the four neighbours'
 // (value, weight) loads for the column and row terms of the lane's pixel,
-// reuse_filter combines them.  An origin outside the reusable range reads
-// record (0, 0) four times (a record of every non-empty frame; its value is
-// not used), so the loads need no branch.  AL8: the previous frame's base and
-// pitch are multiples of 8 bytes, and each pair is one 8-byte load.
+// reuse_filter combines them.  An origin outside the reusable range reads the
+// frame's top-left 2x2 records (values not used), so the loads need no
+// branch; callers fetch only for frames of at least 5x5 pixels (smaller ones
+// reuse nothing).  AL8: the previous frame's base and pitch are multiples of
+// 8 bytes, and each pair is one 8-byte load.
 struct ReuseFetch {
     float2 a, b, c, d;
     float alpha, beta;
@@ -935,12 +936,12 @@ __device__ __forceinline__ ReuseFetch reuse_fetch(ReuseAxis ax, ReuseAxis ay, co
     f.alpha = ax.frac;
     f.beta = ay.frac;
     const uint32_t i = f.in_range ? ax.at & 0x7fffffffu : 0u, j = f.in_range ? ay.at & 0x7fffffffu : 0u;
-    const long dx = f.in_range ? (long)sizeof(PixelInfo) : 0, dy = f.in_range ? in_pitch : 0;
     const char *q = reinterpret_cast<const char *>(pixel_ptr(in, in_pitch, i, j));
+    const char *q1 = q + in_pitch;
     f.a = load_value_weight<AL8>(q);
-    f.b = load_value_weight<AL8>(q + dx);
-    f.c = load_value_weight<AL8>(q + dy);
-    f.d = load_value_weight<AL8>(q + dy + dx);
+    f.b = load_value_weight<AL8>(q + sizeof(PixelInfo));
+    f.c = load_value_weight<AL8>(q1);
+    f.d = load_value_weight<AL8>(q1 + sizeof(PixelInfo));
     return f;
 }
 
@@ -1009,7 +1010,7 @@ __device__ __forceinline__ PixelInfo render_advanced_tile(const SampleGeometry<R
     bool valid = p.x < size.x && p.y < size.y;
     bool reusing = false;
     float reused_v = 0.f, reused_w = 0.f;
-    if (valid && (flags & FLAG_SAMPLE_REUSE)) {
+    if (valid && (flags & FLAG_SAMPLE_REUSE) && size.x >= 5u && size.y >= 5u) {
         const ReuseAxis ax = reuse_axis(warping_origin_x<R, A>(p.x, size, image, image_reused), size.x);
         const ReuseAxis ay = reuse_axis(warping_origin_y<R, A>(p.y, size, image, image_reused), size.y);
         const ReuseFetch f = ((reinterpret_cast<uintptr_t>(in) | (uintptr_t)in_pitch) & 7u) == 0

@@ -67,15 +67,26 @@ template <class R, int A, int F, int K> __global__ void __launch_bounds__(PERSIS
     CycleWatch<R> cw;  // exact cycle detection (see CycleWatch)
     const unsigned long long t_start = a.budget_ns ? global_ns() : 0ull;
 
+    // the grid's first pixels go out without a claim (warp w takes 32w..32w+31),
+    // so the launch does not start with every warp's atomic on one counter;
+    // claims then count from there
+    const uint32_t n_warps = gridDim.x * (blockDim.x >> 5);
+    bool first = true;
+
     for (;;) {
         // a time limit: the warp stops where it is (its samples in flight stay unwritten)
         if (out_of_time(a.budget_ns, t_start, a.status, lane)) break;
         uint32_t need_mask = __ballot_sync(FULL, need);
         if (need_mask) {
-            uint32_t leader = __ffs(need_mask) - 1u;
             uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(a.counter, (uint32_t)__popc(need_mask));
-            base = __shfl_sync(FULL, base, leader);
+            if (first) {
+                base = 32u * (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
+                first = false;
+            } else {
+                const uint32_t leader = __ffs(need_mask) - 1u;
+                if (lane == leader) base = 32u * n_warps + atomicAdd(a.counter, (uint32_t)__popc(need_mask));
+                base = __shfl_sync(FULL, base, leader);
+            }
             if (need) {
                 pix = base + (uint32_t)__popc(need_mask & lt_mask);
                 need = false;

@@ -67,6 +67,7 @@ template <class D> struct PerturbArgs {
     const typename Vec2T<D>::type *orbit;  // Z_0 .. Z_{orbit_last}
     const double2 *orbit64;                // the same orbit in binary64 (rescaled glitch test)
     const float2 *orbit2;                  // 2 Z_m in binary32 (rescaled linear steps)
+    const float4 *bla16;                   // the 16 rescaled linear steps from m composed: (P, Q), w' = P w + Q u
     const uint32_t *next_event;            // first index >= m where a rescaled step's test can fire
     const double2 *orbit2_64;              // 2 Z_m in binary64 (binary64 linear steps)
     const uint32_t *next_event64;          // first index >= m where a binary64 linear step may not be exact
@@ -228,15 +229,14 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                         const float ux = (float)dcx, uy = (float)dcy;
                         const float2 *Z2p = a.orbit2 + m;
                         if (n == B) {
-                            // the usual case: a whole block, no per-step bound
-#pragma unroll
-                            for (uint32_t j = 0; j < B; j++) {
-                                const float2 Z2 = Z2p[j];
-                                const float nx = __fmaf_rn(Z2.x, wx, __fmaf_rn(-Z2.y, wy, ux));
-                                const float ny = __fmaf_rn(Z2.x, wy, __fmaf_rn(Z2.y, wx, uy));
-                                wx = nx;
-                                wy = ny;
-                            }
+                            // the usual case: a whole block, its 16 steps composed on the host
+                            // into w' = P w + Q u (one 16-byte load, eight operations)
+                            const float4 pq = a.bla16[m];
+                            const float nx =
+                                __fmaf_rn(pq.x, wx, __fmaf_rn(-pq.y, wy, __fmaf_rn(pq.z, ux, -pq.w * uy)));
+                            const float ny = __fmaf_rn(pq.x, wy, __fmaf_rn(pq.y, wx, __fmaf_rn(pq.z, uy, pq.w * ux)));
+                            wx = nx;
+                            wy = ny;
                         } else {
                             for (uint32_t j = 0; j < n; j++) {
                                 const float2 Z2 = Z2p[j];
@@ -492,6 +492,7 @@ struct chaos_orbit {
     float2 *z32 = nullptr;
     double2 *z64 = nullptr;
     float2 *z2 = nullptr;              // 2 Z in binary32
+    float4 *bla16 = nullptr;           // see the rescaled linear steps of k_perturb
     uint32_t *next_event = nullptr;    // see the rescaled linear steps of k_perturb
     double2 *z2_64 = nullptr;          // 2 Z in binary64
     uint32_t *next_event64 = nullptr;  // see the binary64 linear steps of k_perturb
@@ -555,6 +556,23 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
         z32[k] = make_float2((float)z64[k].x, (float)z64[k].y);
         z2[k] = make_float2(2.f * z32[k].x, 2.f * z32[k].y);
     }
+    // bla16[m]: the 16 rescaled linear steps w <- 2Z_j w + u, j = m..m+15 (with
+    // 2Z_j as the kernel holds it, binary32), composed in binary64 into
+    // w <- P w + Q u and rounded to binary32 once
+    std::vector<float4> bla16(z64.size(), make_float4(0.f, 0.f, 0.f, 0.f));
+    for (size_t m = 0; m + 16 <= z2.size(); m++) {
+        double px = 1.0, py = 0.0, qx = 0.0, qy = 0.0;
+        for (size_t j = m; j < m + 16; j++) {
+            const double ax = z2[j].x, ay = z2[j].y;
+            const double npx = ax * px - ay * py, npy = ax * py + ay * px;
+            const double nqx = ax * qx - ay * qy + 1.0, nqy = ax * qy + ay * qx;
+            px = npx;
+            py = npy;
+            qx = nqx;
+            qy = nqy;
+        }
+        bla16[m] = make_float4((float)px, (float)py, (float)qx, (float)qy);
+    }
     // next_event[m]: first index j >= m where a rescaled step's test can fire,
     // evaluated as the kernel does (binary32 |Z_j|^2 with one fused add)
     std::vector<uint32_t> next_event(z64.size());
@@ -600,6 +618,8 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
     if (e == cudaSuccess) e = cudaMemcpy(o->z32, z32.data(), z32.size() * sizeof(float2), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&o->z2, z2.size() * sizeof(float2));
     if (e == cudaSuccess) e = cudaMemcpy(o->z2, z2.data(), z2.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&o->bla16, bla16.size() * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMemcpy(o->bla16, bla16.data(), bla16.size() * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&o->next_event, next_event.size() * sizeof(uint32_t));
     if (e == cudaSuccess)
         e = cudaMemcpy(o->next_event, next_event.data(), next_event.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
@@ -614,6 +634,7 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
         if (o->z64) cudaFree(o->z64);
         if (o->z32) cudaFree(o->z32);
         if (o->z2) cudaFree(o->z2);
+        if (o->bla16) cudaFree(o->bla16);
         if (o->next_event) cudaFree(o->next_event);
         if (o->z2_64) cudaFree(o->z2_64);
         if (o->next_event64) cudaFree(o->next_event64);
@@ -639,6 +660,7 @@ int chaos_orbit_destroy(chaos_orbit *o)
     if (o->z64) cudaFree(o->z64);
     if (o->z32) cudaFree(o->z32);
     if (o->z2) cudaFree(o->z2);
+    if (o->bla16) cudaFree(o->bla16);
     if (o->next_event) cudaFree(o->next_event);
     if (o->z2_64) cudaFree(o->z2_64);
     if (o->next_event64) cudaFree(o->next_event64);
@@ -672,6 +694,7 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
     a.orbit_last = orb->last;
     a.orbit64 = orb->z64;
     a.orbit2 = orb->z2;
+    a.bla16 = orb->bla16;
     a.next_event = orb->next_event;
     a.orbit2_64 = orb->z2_64;
     a.next_event64 = orb->next_event64;

@@ -177,8 +177,9 @@ __global__ void __launch_bounds__(PERSIST_THREADS)
             SampleGeometry<R> g = make_geometry(fr.a.m.image, fr.a.m.size, fr.a.m.max_iter, fr.a.m.jcx, fr.a.m.jcy);
             const uint32_t t_first = (job - s_begin[f]) * fr.chunk;
             const uint32_t t_end = min(t_first + fr.chunk, fr.a.m.n_tiles);
-            for (uint32_t t = t_first; t < t_end; t++) {
-                const uint32_t x0 = 8u * (t % fr.a.m.tiles_x), y0 = 4u * (t / fr.a.m.tiles_x);
+            TileCursor c(t_first, fr.a.m.tiles_x);
+            for (uint32_t t = t_first; t < t_end; t++, c.next(fr.a.m.tiles_x)) {
+                const uint32_t x0 = c.x0(), y0 = c.y0();
                 PixelInfo rec;
                 if constexpr (ADV)
                     rec = render_advanced_tile<R, A, F>(g, fr.a.m.image, fr.a.image_reused, fr.a.m.out, fr.a.m.pitch,
