@@ -1273,7 +1273,7 @@ def run_reuse(args):
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                          # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the same
                          # 7680x4320 reuse frame, from the committed ncu summary (k_advanced_reuse_8k)
-                         "traffic": 1022.0e6, "traffic_unit": "bytes per launch (ncu capture)",
+                         "traffic": 1022.8e6, "traffic_unit": "bytes per launch (ncu capture)",
                          "peak_source": src, "bytes_per_pixel": 32},
             "gpu_launches": args.steps, "clocks": clk}
     print(json.dumps(line), flush=True)

@@ -120,76 +120,62 @@ template <class R, int A, int F> __global__ void __launch_bounds__(PERSIST_THREA
 // rate, bound by the loads' latency and the issue of the divisions.  Two
 // tiles (eight 8-byte loads per lane) measured best: four need registers
 // that cost a fifth of the warps.
-constexpr uint32_t REUSE_BATCH = 2;
-
 // The strip [t0, t1) of a fractalRenderAdvanced frame, in groups of four
-// tiles.  The origin's column and row terms of a group are computed once per
-// column and row (lane l: the column l & 7 of the group's tile l >> 3, and
-// the row l & 3 of its tile (l >> 2) & 3) and taken by shuffles.  Within a
-// group, the previous-frame reads of REUSE_BATCH tiles are issued before the
-// first of them is filtered; the filtered (value, weight) pairs wait in the
-// warp's `stage` (REUSE_BATCH x 32 pairs of shared memory, the weight -1
-// where the origin is out of range), not in registers, while each tile is
-// finished (votes, samples, record) in order and handed to on_tile(x0, y0,
-// record).
-template <class R, int A, int F, bool AL8, class OnTile>
+// tiles (32x4 pixels).  The reuse reads of a group run in row order: lane l
+// takes column l & 7 of the group's tile l >> 3 and walks its four rows, so
+// that a warp's read of one row covers 32 consecutive pixels (contiguous
+// records under a near-identity warp), and the reads of all four rows are in
+// flight before the first is filtered.  The origin's column term is the
+// lane's own; its row terms are computed once per row (lane l: row l & 3 of
+// tile (l >> 2) & 3) and taken by shuffles.  The filtered (value, weight)
+// pairs (the weight -1 where the origin is out of range) go to the warp's
+// `stage` (4 x 32 pairs of shared memory), from which each tile is finished
+// in its own 8x4 lane layout (votes, samples, record).
+template <class R, int A, int F, bool AL8>
 __device__ __forceinline__ void advanced_strip(const AdvancedArgs<R> &a, const SampleGeometry<R> &g, uint32_t lane,
-                                               float2 *stage, uint32_t t0, uint32_t t1, unsigned long long &iters,
-                                               OnTile on_tile)
+                                               float2 *stage, uint32_t t0, uint32_t t1, unsigned long long &iters)
 {
-    static_assert(REUSE_BATCH == 1 || REUSE_BATCH == 2 || REUSE_BATCH == 4, "a power of two up to 4");
     // (frames smaller than 5x5 pixels reuse nothing, see reuse_axis)
     const bool reuse = (a.m.flags & FLAG_SAMPLE_REUSE) != 0 && a.m.size.x >= 5u && a.m.size.y >= 5u;
-    const uint32_t col = 4u * (lane >> 4) + (lane & 3u), row = (lane >> 2) & 3u;
+    const uint32_t col = 4u * (lane >> 4) + (lane & 3u), row = (lane >> 2) & 3u;  // the 8x4 tile layout
     const uint32_t tiles_x = a.m.tiles_x;
     TileCursor cur(t0, tiles_x);  // the next tile to finish
     for (uint32_t tg = t0; tg < t1; tg += 4u) {
         const uint32_t ng = min(4u, t1 - tg);
-        ReuseAxis mx{0u, 0.f}, my{0u, 0.f};
         if (reuse) {
-            // this lane's column and row terms (positions past the group's end repeat its last tile)
-            const TileCursor tc = cur.plus(min(lane >> 3, ng - 1u), tiles_x);
+            // this lane's column (of its tile k; lanes past the group's end repeat its last tile)
+            const uint32_t k = min(lane >> 3, ng - 1u);
+            const TileCursor tc = cur.plus(k, tiles_x);
             const TileCursor tr = cur.plus(min((lane >> 2) & 3u, ng - 1u), tiles_x);
-            mx = reuse_axis(warping_origin_x<R, A>(tc.x0() + (lane & 7u), a.m.size, a.m.image, a.image_reused),
-                            a.m.size.x);
-            my = reuse_axis(warping_origin_y<R, A>(tr.y0() + (lane & 3u), a.m.size, a.m.image, a.image_reused),
-                            a.m.size.y);
-        }
-        for (uint32_t kb = 0; kb < ng; kb += REUSE_BATCH) {
-            const uint32_t nb = min(REUSE_BATCH, ng - kb);
-            if (reuse) {
-                ReuseFetch f[REUSE_BATCH];
+            const uint32_t x = tc.x0() + (lane & 7u);
+            const ReuseAxis mx = reuse_axis(warping_origin_x<R, A>(x, a.m.size, a.m.image, a.image_reused), a.m.size.x);
+            const ReuseAxis my = reuse_axis(
+                warping_origin_y<R, A>(tr.y0() + (lane & 3u), a.m.size, a.m.image, a.image_reused), a.m.size.y);
+            ReuseFetch f[4];
 #pragma unroll
-                for (uint32_t k = 0; k < REUSE_BATCH; k++) {
-                    // tiles past the batch's end read its last tile's records again (unused)
-                    const uint32_t kk = kb + min(k, nb - 1u);
-                    ReuseAxis ax, ay;
-                    ax.at = __shfl_sync(FULL, mx.at, 8u * kk + col);
-                    ax.frac = __shfl_sync(FULL, mx.frac, 8u * kk + col);
-                    ay.at = __shfl_sync(FULL, my.at, 4u * kk + row);
-                    ay.frac = __shfl_sync(FULL, my.frac, 4u * kk + row);
-                    f[k] = reuse_fetch<AL8>(ax, ay, a.in, a.in_pitch);
-                }
-#pragma unroll
-                for (uint32_t k = 0; k < REUSE_BATCH; k++) {
-                    float v, w;
-                    reuse_filter<A>(f[k], v, w);
-                    stage[32u * k + lane] = make_float2(v, f[k].in_range ? w : -1.f);
-                }
-                __syncwarp();
+            for (uint32_t r = 0; r < 4u; r++) {
+                ReuseAxis ay;
+                ay.at = __shfl_sync(FULL, my.at, 4u * k + r);
+                ay.frac = __shfl_sync(FULL, my.frac, 4u * k + r);
+                f[r] = reuse_fetch<AL8>(mx, ay, a.in, a.in_pitch);
             }
-            for (uint32_t k = 0; k < nb; k++, cur.next(tiles_x)) {
-                const uint32_t x0 = cur.x0(), y0 = cur.y0();
-                const UInt2 p = tile_pixel(x0, y0, lane);
-                const bool valid = p.x < a.m.size.x && p.y < a.m.size.y;
-                const float2 vw = reuse ? stage[32u * k + lane] : make_float2(0.f, 0.f);
-                const PixelInfo rec = finish_advanced_tile<R, A, F>(
-                    g, a.m.out, a.m.pitch, a.m.size, a.focus, x0, y0, lane, a.m.max_ss, a.m.flags,
-                    valid && reuse && !(vw.y < 0.1f), vw.x, vw.y, iters);
-                on_tile(x0, y0, rec);
+#pragma unroll
+            for (uint32_t r = 0; r < 4u; r++) {
+                float vv, ww;
+                reuse_filter<A>(f[r], vv, ww);
+                stage[32u * r + lane] = make_float2(vv, f[r].in_range ? ww : -1.f);
             }
             __syncwarp();
         }
+        for (uint32_t k = 0; k < ng; k++, cur.next(tiles_x)) {
+            const uint32_t x0 = cur.x0(), y0 = cur.y0();
+            const UInt2 p = tile_pixel(x0, y0, lane);
+            const bool valid = p.x < a.m.size.x && p.y < a.m.size.y;
+            const float2 vw = reuse ? stage[32u * row + 8u * k + col] : make_float2(0.f, 0.f);
+            finish_advanced_tile<R, A, F>(g, a.m.out, a.m.pitch, a.m.size, a.focus, x0, y0, lane, a.m.max_ss,
+                                          a.m.flags, valid && reuse && !(vw.y < 0.1f), vw.x, vw.y, iters);
+        }
+        __syncwarp();
     }
 }
 
@@ -199,17 +185,16 @@ template <class R, int A, int F> __global__ void __launch_bounds__(PERSIST_THREA
     SampleGeometry<R> g = make_geometry(a.m.image, a.m.size, a.m.max_iter, a.m.jcx, a.m.jcy);
     g.newton = a.m.newton;
     unsigned long long iters = 0;
-    __shared__ float2 s_stage[PERSIST_THREADS / 32][REUSE_BATCH * 32];
+    __shared__ float2 s_stage[PERSIST_THREADS / 32][4 * 32];
     float2 *stage = s_stage[threadIdx.x >> 5];
     const bool al8 = ((reinterpret_cast<uintptr_t>(a.in) | (uintptr_t)a.in_pitch) & 7u) == 0;
-    auto none = [](uint32_t, uint32_t, const PixelInfo &) {};
     if (al8)
         for_each_strip(a.m.counter, a.m.n_tiles, a.m.tile_chunk, lane, [&](uint32_t t0, uint32_t t1) {
-            advanced_strip<R, A, F, true>(a, g, lane, stage, t0, t1, iters, none);
+            advanced_strip<R, A, F, true>(a, g, lane, stage, t0, t1, iters);
         });
     else
         for_each_strip(a.m.counter, a.m.n_tiles, a.m.tile_chunk, lane, [&](uint32_t t0, uint32_t t1) {
-            advanced_strip<R, A, F, false>(a, g, lane, stage, t0, t1, iters, none);
+            advanced_strip<R, A, F, false>(a, g, lane, stage, t0, t1, iters);
         });
     add_total(a.m.total, iters, lane);
 }
