@@ -137,6 +137,9 @@ __device__ __forceinline__ void advanced_strip(const AdvancedArgs<R> &a, const S
 {
     // (frames smaller than 5x5 pixels reuse nothing, see reuse_axis)
     const bool reuse = (a.m.flags & FLAG_SAMPLE_REUSE) != 0 && a.m.size.x >= 5u && a.m.size.y >= 5u;
+    // zooming in with foveation, a reusing pixel in the foveal region takes new samples
+    const bool fov =
+        (a.m.flags & FLAG_FOVEATION) && (a.m.flags & FLAG_IS_ZOOMING) && (a.m.flags & FLAG_ZOOMING_IN);
     const uint32_t col = 4u * (lane >> 4) + (lane & 3u), row = (lane >> 2) & 3u;  // the 8x4 tile layout
     const uint32_t tiles_x = a.m.tiles_x;
     TileCursor cur(t0, tiles_x);  // the next tile to finish
@@ -172,8 +175,19 @@ __device__ __forceinline__ void advanced_strip(const AdvancedArgs<R> &a, const S
             const UInt2 p = tile_pixel(x0, y0, lane);
             const bool valid = p.x < a.m.size.x && p.y < a.m.size.y;
             const float2 vw = reuse ? stage[32u * row + 8u * k + col] : make_float2(0.f, 0.f);
+            const bool reusing = valid && reuse && !(vw.y < 0.1f);
+            if (!fov && __all_sync(FULL, reusing || !valid)) {
+                // every pixel reuses and none takes new samples: the record is
+                // (value, weight, isReused = 1, 0), as the full path stores it
+                if (valid) {
+                    PixelInfo rec = make_pixel(vw.x, vw.y);
+                    rec.is_reused = 1;
+                    store_pixel(pixel_ptr(a.m.out, a.m.pitch, p.x, p.y), rec);
+                }
+                continue;
+            }
             finish_advanced_tile<R, A, F>(g, a.m.out, a.m.pitch, a.m.size, a.focus, x0, y0, lane, a.m.max_ss,
-                                          a.m.flags, valid && reuse && !(vw.y < 0.1f), vw.x, vw.y, iters);
+                                          a.m.flags, reusing, vw.x, vw.y, iters);
         }
         __syncwarp();
     }
