@@ -1021,6 +1021,22 @@ __device__ __forceinline__ PixelInfo render_advanced_tile(const SampleGeometry<R
             reusing = !(reused_w < 0.1f);
         }
     }
+    // a tile whose pixels all reuse and take no new samples (outside the
+    // foveal region, which is uniform over a tile, when zooming in with
+    // foveation) stores (value, weight, isReused = 1, 0) without the vote code
+    if (__all_sync(0xffffffffu, reusing || !valid)) {
+        bool sample = false;
+        if ((flags & FLAG_FOVEATION) && (flags & FLAG_IS_ZOOMING) && (flags & FLAG_ZOOMING_IN)) {
+            float advised;
+            foveation<A>(p, focus, max_ss, advised, sample);
+        }
+        if (!sample) {
+            PixelInfo rec = make_pixel(reused_v, reused_w);
+            rec.is_reused = 1;
+            if (valid) store_pixel(pixel_ptr(out, pitch, p.x, p.y), rec);
+            return rec;
+        }
+    }
     return finish_advanced_tile<R, A, F>(g, out, pitch, size, focus, x0, y0, lane, max_ss, flags, reusing, reused_v,
                                          reused_w, iters);
 }

@@ -376,8 +376,8 @@ def test_random_julia_views_against_both_reference_builds(drv, cuda, seed):
 @pytest.mark.parametrize("case", ["zoom_in_f32", "zoom_out_f32", "zoom_in_f64", "pan_f64"])
 def test_large_reuse_frames_match_both_reference_builds(drv, cuda, case):
     """Frames large enough for the library's persistent reuse kernel to claim
-    strips of tiles and stage each strip's source footprint in shared memory
-    (3840x2160: four tiles per claim) against the reference's own
+    strips of several tiles and read each group of four in row order
+    (3840x2160) against the reference's own
     fractalRenderAdvanced in the Java launch shape: the library with the
     rounded arithmetic against the --fmad=false build and with the
     contracted arithmetic against the default build, record for record.

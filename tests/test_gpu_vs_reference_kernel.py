@@ -13,7 +13,11 @@ pattern with warp votes):
   the 3840x2160 workload (bisection along the ray of seed 2), maxIter 20000,
   maxSS 4, adaptive sampling on; the central 1920x1080 of the frame;
 * C1 view: binary32, 1024x1024 over [-2, 1] x [-1.5, 1.5], maxIter 1000,
-  maxSS 1.
+  maxSS 1;
+* a renderFast frame (fractalRenderAdvancedFloat): 3840x2160 around the
+  premade view M1, zoomed in 1/0.977 at a seeded focus from the previous
+  frame, with sample reuse, foveation and adaptive sampling (the Java
+  renderer's flags while zooming in).
 
 The same frames also go through the C ABI (chaos_render_main_f64/_f32).
 Each kernel runs once untimed, then once between CUDA events.  The times are
@@ -26,7 +30,8 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-from tests.gpu_util import Driver, java_grid, main_params, pitched, read_pixels, same_pixels  # noqa: E402
+from tests.gpu_util import (Driver, advanced_params, java_grid, main_params, pitched, read_pixels,  # noqa: E402
+                            same_pixels, upload_pixels)
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REF_DIR = os.path.join(ROOT, "oracle", "_ref")
@@ -153,3 +158,62 @@ def test_c1_view_dropin_vs_reference_kernel(drv, cuda):
     assert line["records_differing"]["parity_vs_reference_nofma"] == 0.0
     assert line["records_differing"]["contracted_vs_reference_default"] == 0.0
     assert line["speedup"]["parity_vs_reference_nofma"] > 1.0
+
+
+def _timed_advanced(drv, cuda, path, w, h, rect, max_iter, max_ss, flags, old, in_ptr, in_pitch, focus):
+    """fractalRenderAdvancedFloat of a module in the Java launch shape; (pixels, mean ms)."""
+    mod = drv.load(path)
+    try:
+        drv.write_constant(mod, "VISUALIZE_SAMPLE_COUNT", b"\0")
+        fn = drv.function(mod, "fractalRenderAdvancedFloat")
+        buf, pitch = pitched(cuda, w, h)
+        grid, block = java_grid(w, h)
+        params = advanced_params(buf.data_ptr(), pitch, w, h, rect, max_iter, max_ss, flags, old, in_ptr, in_pitch,
+                                 focus, False)
+        drv.launch(fn, grid, block, params)
+        buf.zero_()
+        ms = _timed(cuda, lambda: drv.launch(fn, grid, block, params, sync=False))
+        return read_pixels(buf, w), ms
+    finally:
+        drv.unload(mod)
+
+
+def test_reuse_frame_dropin_vs_reference_kernel(drv, cuda):
+    """renderFast's kernel, fractalRenderAdvancedFloat, on a zoom-in frame that
+    reuses the previous one: the drop-in modules equal the reference's two
+    builds record for record, and each is faster than the build it mirrors."""
+    import chaos_gb300 as cg
+    from tests.test_gpu_reference_mode import M1, rect_for, zoom_at
+    w, h, mi, mss = 3840, 2160, 400, 2.0
+    focus = (1700, 900)
+    old = tuple(float(v) for v in np.float32(rect_for(M1[:2], M1[2], w, h)))
+    new = tuple(float(v) for v in np.float32(zoom_at(old, focus, w, h, into=True)))
+    flags = (cg.FLAG_SAMPLE_REUSE | cg.FLAG_IS_ZOOMING | cg.FLAG_ZOOMING_IN | cg.FLAG_ADAPTIVE_SS |
+             cg.FLAG_FOVEATION)
+    line = {"view": "renderFast 3840x2160 around M1, zoom-in 1/0.977 with reuse + foveation", "ms": {},
+            "speedup": {}, "records_differing": {}}
+    for parity in (True, False):
+        ref_path = _cubin("ref_mandelbrot_nofma.cubin" if parity else "ref_mandelbrot.cubin")
+        # the previous frame: the reference's own renderQuality of the old plane
+        mod = drv.load(ref_path)
+        try:
+            drv.write_constant(mod, "VISUALIZE_SAMPLE_COUNT", b"\0")
+            fn = drv.function(mod, "fractalRenderMainFloat")
+            prev, prev_pitch = pitched(cuda, w, h)
+            grid, block = java_grid(w, h)
+            drv.launch(fn, grid, block, main_params(prev.data_ptr(), prev_pitch, w, h, old, mi, mss, 1, False))
+        finally:
+            drv.unload(mod)
+        ref, t_ref = _timed_advanced(drv, cuda, ref_path, w, h, new, mi, mss, flags, old, prev.data_ptr(),
+                                     prev_pitch, focus)
+        ours, t_ours = _timed_advanced(drv, cuda, _ours(parity), w, h, new, mi, mss, flags, old, prev.data_ptr(),
+                                       prev_pitch, focus)
+        name = "parity_vs_reference_nofma" if parity else "contracted_vs_reference_default"
+        line["ms"][name] = [t_ours, t_ref]
+        line["speedup"][name] = t_ref / t_ours
+        line["records_differing"][name] = float(same_pixels(ours, ref).mean())
+        assert float(ours["is_reused"].mean()) > 0.5  # the reuse path carries the frame
+    print(json.dumps(line), flush=True)
+    for name in line["speedup"]:
+        assert line["records_differing"][name] == 0.0, name
+        assert line["speedup"][name] > 1.0, name
