@@ -20,8 +20,9 @@ pattern with warp votes):
   renderer's flags while zooming in).
 
 The same frames also go through the C ABI (chaos_render_main_f64/_f32).
-Each kernel runs once untimed, then once between CUDA events.  The times are
-printed as one JSON line per view (run pytest with -s to see them)."""
+Each kernel runs once untimed, then back to back (enough launches for
+~50 ms, at most 20) between CUDA events; the mean is reported.  The times
+are printed as one JSON line per view (run pytest with -s to see them)."""
 import json
 import os
 
