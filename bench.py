@@ -411,7 +411,7 @@ def run_ours(args):
         "wall_s_timed": wall,
     }
     if not args.headline_only and W == 3840:
-        # after the headline's timed region: the benchmark spec's other claims, each
+        # after the headline's timed region: the other claims of the path, each
         # with its own clock record (the reference's own GPU kernel on this machine,
         # the batched C4 forms, the served C5 trace)
         t_sub = time.perf_counter()
@@ -800,13 +800,13 @@ def measure_c4(workload="c4", steps=3, warmup=3, compact=False):
                           "escape_count_mismatch_vs_fp64_oracle": vs_oracle(plain_counts)},
         "plain_f64_dropin": dict(plain_forms["library"], what=(
             "fractalRenderMainDouble semantics (binary64, rounded arithmetic, 1 sample per pixel) viewport by "
-            "viewport through the C ABI (chaos_render_main_f64): the north-star's plain FP64 drop-in")),
+            "viewport through the C ABI (chaos_render_main_f64): the plain FP64 drop-in of the 3x target")),
         "plain_f64_java_shape": {
             "dropin_module": plain_forms.get("dropin_module"), "reference_module": ref_mod,
             "records_differing_dropin_vs_reference": records_differ / total if ref_mod else None,
             "what": "the same viewports through cudaKernels_parity/mandelbrot.ptx and the reference's own module "
                     "built --fmad=false, 32x32 blocks per viewport on the default stream", "clocks": vp_clk},
-        "north_star": {
+        "target_3x": {
             "bar": ">= 3x the plain FP64 drop-in at <= 0.1% escape-count mismatch vs the FP64 oracle",
             "within_bar_form": "rounded_f64_batch",
             "within_bar_speedup_of_plain_f64_dropin": rounded_value / dropin_value,
