@@ -27,7 +27,12 @@
 // alone (escape only where binary32 |Z|^2 >= 4, the glitch test only where it
 // is below 2^-100, the orbit's end), so the orbit carries, per index, the next
 // index where one of them can fire, and steps up to it run as a block of
-// 4 FFMA each on a stored 2Z.  Binary64 differences get the same treatment
+// 4 FFMA each on a stored 2Z; a whole block of 16 runs as one composed map
+// w' = P w + Q u.  The same composed map also stands in for 16 full steps of a
+// binary32 difference at e >= -126 or a plain one, while the difference stays
+// so far below the orbit over the block that the dropped d^2 term is below
+// binary32 rounding (a per-index exponent bound, lin_lim, set on the host from
+// |Z_j| and the partial products).  Binary64 differences get the same treatment
 // while |d| and |dc| stay below 2^-120 and both components of Z above 2^-20:
 // then 2Z + d rounds to 2Z and Z + d' to Z, so d' = 2Z d + dc (4 DFMA) is the
 // full step bit for bit, and its tests depend on the orbit index alone.
@@ -68,6 +73,7 @@ template <class D> struct PerturbArgs {
     const double2 *orbit64;                // the same orbit in binary64 (rescaled glitch test)
     const float2 *orbit2;                  // 2 Z_m in binary32 (rescaled linear steps)
     const float4 *bla16;                   // the 16 rescaled linear steps from m composed: (P, Q), w' = P w + Q u
+    const int8_t *lin_lim;                 // largest e + ilogb(max |w|, |u|) for which bla16[m] stands in for 16 steps
     const uint32_t *next_event;            // first index >= m where a rescaled step's test can fire
     const double2 *orbit2_64;              // 2 Z_m in binary64 (binary64 linear steps)
     const uint32_t *next_event64;          // first index >= m where a binary64 linear step may not be exact
@@ -133,6 +139,30 @@ __device__ __forceinline__ bool glitch_test(double zx, double zy, double dx, dou
 // 2^e as a binary32, or 0 below the normal range
 __device__ __forceinline__ float pow2f(int e) { return e >= -126 ? __int_as_float((e + 127) << 23) : 0.f; }
 
+// lin_lim[m] where no composed block may start at m
+constexpr int LIN_NONE = -128;
+
+// Keep the scaled difference's larger component within [2^-24, 2^24]: w and u
+// move by 2^-+24 and e the other way.  Past e > -100 the sample leaves the
+// rescaled form and holds d = w 2^e, dc = u 2^e directly.
+template <class D>
+__device__ __forceinline__ void renormalise(D &dx, D &dy, D &dcx, D &dcy, int &e, bool &scaled)
+{
+    const float mag = fmaxf(fabsf((float)dx), fabsf((float)dy));
+    if (mag > 0x1p24f) {
+        dx *= D(0x1p-24f), dy *= D(0x1p-24f), dcx *= D(0x1p-24f), dcy *= D(0x1p-24f);
+        e += 24;
+        if (e > -100) {
+            const float q = pow2f(e);
+            dx *= q, dy *= q, dcx *= q, dcy *= q;
+            scaled = false;
+        }
+    } else if (mag < 0x1p-24f && mag > 0.f && e > -1000) {
+        dx *= D(0x1p24f), dy *= D(0x1p24f), dcx *= D(0x1p24f), dcy *= D(0x1p24f);
+        e -= 24;
+    }
+}
+
 template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_perturb(PerturbArgs<D> a)
 {
     static_assert(!S || sizeof(D) == 4, "rescaling is for binary32 differences");
@@ -154,6 +184,7 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
     D dx = D(0), dy = D(0), dcx = D(0), dcy = D(0), Zx = D(0), Zy = D(0);
     int e = 0;
     bool scaled = false;
+    bool lin = true;  // composed blocks may still apply to this sample (binary32)
     bool need = true, begin = false;
     float acc_v = 0.f, acc[4] = {0.f, 0.f, 0.f, 0.f};
     unsigned long long iters = 0, rebases = 0;
@@ -215,6 +246,7 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                 Zy = D(0);
                 m = 0;
                 i = 0;
+                lin = true;
                 if (a.max_iter == 0) done = true;
             }
 #pragma unroll 1
@@ -264,6 +296,32 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                         continue;
                     }
                 }
+                if constexpr (sizeof(D) == 4) if (lin) {
+                    // a difference far below the orbit (rescaled at e >= -126, or plain):
+                    // over the next 16 steps (2Z_j + d_j) d_j stays within 2^-25 of
+                    // 2Z_j d_j, below binary32 rounding, and no escape, glitch or orbit
+                    // end can come, when e + ilogb(max |w|, |u|) <= lin_lim[m]; then the
+                    // composed block w' = P w + Q u stands in for the 16 steps
+                    const float big = fmaxf(fmaxf(fabsf((float)dx), fabsf((float)dy)),
+                                            fmaxf(fabsf((float)dcx), fabsf((float)dcy)));
+                    const int eb = (scaled ? e : 0) + (int)((__float_as_uint(big) >> 23) & 255u) - 127;
+                    const int lim = a.lin_lim[m];
+                    if (lim != LIN_NONE && eb <= lim && a.max_iter - i > 16u) {
+                        const float4 pq = a.bla16[m];
+                        const float wx = (float)dx, wy = (float)dy, ux = (float)dcx, uy = (float)dcy;
+                        dx = __fmaf_rn(pq.x, wx, __fmaf_rn(-pq.y, wy, __fmaf_rn(pq.z, ux, -pq.w * uy)));
+                        dy = __fmaf_rn(pq.x, wy, __fmaf_rn(pq.y, wx, __fmaf_rn(pq.z, uy, pq.w * ux)));
+                        m += 16;
+                        i += 16;
+                        const typename Vec2T<D>::type Z = a.orbit[m];
+                        Zx = Z.x;
+                        Zy = Z.y;
+                        if (scaled) renormalise(dx, dy, dcx, dcy, e, scaled);
+                        continue;
+                    }
+                    // lin_lim never exceeds -25: a plain difference that large stays out
+                    if (!scaled && eb > -25) lin = false;
+                }
                 if constexpr (S) if (scaled) {
                     // w' = (2Z + 2^e w) w + u
                     const float q = pow2f(e);
@@ -309,19 +367,7 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                     dy = nwy;
                     Zx = Z.x;
                     Zy = Z.y;
-                    const float mag = fmaxf(fabsf(nwx), fabsf(nwy));
-                    if (mag > 0x1p24f) {
-                        dx *= D(0x1p-24f), dy *= D(0x1p-24f), dcx *= D(0x1p-24f), dcy *= D(0x1p-24f);
-                        e += 24;
-                        if (e > -100) {
-                            const float q2 = pow2f(e);
-                            dx *= q2, dy *= q2, dcx *= q2, dcy *= q2;
-                            scaled = false;
-                        }
-                    } else if (mag < 0x1p-24f && mag > 0.f && e > -1000) {
-                        dx *= D(0x1p24f), dy *= D(0x1p24f), dcx *= D(0x1p24f), dcy *= D(0x1p24f);
-                        e -= 24;
-                    }
+                    renormalise(dx, dy, dcx, dcy, e, scaled);
                     continue;
                 }
                 if constexpr (!S && sizeof(D) == 8) {
@@ -493,6 +539,7 @@ struct chaos_orbit {
     double2 *z64 = nullptr;
     float2 *z2 = nullptr;              // 2 Z in binary32
     float4 *bla16 = nullptr;           // see the rescaled linear steps of k_perturb
+    int8_t *lin_lim = nullptr;         // see the composed blocks of k_perturb
     uint32_t *next_event = nullptr;    // see the rescaled linear steps of k_perturb
     double2 *z2_64 = nullptr;          // 2 Z in binary64
     uint32_t *next_event64 = nullptr;  // see the binary64 linear steps of k_perturb
@@ -559,10 +606,33 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
     // bla16[m]: the 16 rescaled linear steps w <- 2Z_j w + u, j = m..m+15 (with
     // 2Z_j as the kernel holds it, binary32), composed in binary64 into
     // w <- P w + Q u and rounded to binary32 once
+    //
+    // lin_lim[m]: where the block from m may also stand in for 16 quadratic
+    // steps.  With w_j = P_(m->j) w + Q_(m->j) u the difference at step j,
+    // |2^e w_j| < 2^(e + ilogb(M) + 1.5) (|P_j| + |Q_j|) for M = max(|w|, |u|)
+    // componentwise; the quadratic term is negligible when that stays below
+    // 2^-24 |Z_j| for j = m..m+16, i.e. e + ilogb(M) <= floor(h - 25.5) with
+    // h = min_j log2|Z_j| - log2(|P_j| + |Q_j|).  No test may fire inside:
+    // |Z_j|^2 < 3.99 and >= 2^-98 for j = m+1..m+16 (margins on the escape
+    // and rescaled glitch tests, which then see z_j = Z_j to binary32
+    // precision), the block ends before the orbit's last index, and Z_m != 0.
     std::vector<float4> bla16(z64.size(), make_float4(0.f, 0.f, 0.f, 0.f));
+    std::vector<int8_t> lin_lim(z64.size(), (int8_t)LIN_NONE);
     for (size_t m = 0; m + 16 <= z2.size(); m++) {
         double px = 1.0, py = 0.0, qx = 0.0, qy = 0.0;
-        for (size_t j = m; j < m + 16; j++) {
+        const bool room = m + 16 < z64.size() - 1;
+        bool ok = room;
+        double h = INFINITY;
+        for (size_t j = m; j <= m + 16 && j < z32.size(); j++) {
+            if (ok) {
+                const double az = std::hypot((double)z32[j].x, (double)z32[j].y);
+                const float r2 = std::fmaf(z32[j].x, z32[j].x, z32[j].y * z32[j].y);
+                if (!(az > 0.0) || (j > m && (!(r2 < 3.99f) || r2 < 0x1p-98f)))
+                    ok = false;
+                else
+                    h = std::min(h, std::log2(az) - std::log2(std::hypot(px, py) + std::hypot(qx, qy)));
+            }
+            if (j == m + 16) break;
             const double ax = z2[j].x, ay = z2[j].y;
             const double npx = ax * px - ay * py, npy = ax * py + ay * px;
             const double nqx = ax * qx - ay * qy + 1.0, nqy = ax * qy + ay * qx;
@@ -572,6 +642,7 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
             qy = nqy;
         }
         bla16[m] = make_float4((float)px, (float)py, (float)qx, (float)qy);
+        if (ok && std::isfinite(h)) lin_lim[m] = (int8_t)std::max(-127.0, std::min(127.0, std::floor(h - 25.5)));
     }
     // next_event[m]: first index j >= m where a rescaled step's test can fire,
     // evaluated as the kernel does (binary32 |Z_j|^2 with one fused add)
@@ -620,6 +691,8 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
     if (e == cudaSuccess) e = cudaMemcpy(o->z2, z2.data(), z2.size() * sizeof(float2), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&o->bla16, bla16.size() * sizeof(float4));
     if (e == cudaSuccess) e = cudaMemcpy(o->bla16, bla16.data(), bla16.size() * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&o->lin_lim, lin_lim.size());
+    if (e == cudaSuccess) e = cudaMemcpy(o->lin_lim, lin_lim.data(), lin_lim.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&o->next_event, next_event.size() * sizeof(uint32_t));
     if (e == cudaSuccess)
         e = cudaMemcpy(o->next_event, next_event.data(), next_event.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
@@ -635,6 +708,7 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
         if (o->z32) cudaFree(o->z32);
         if (o->z2) cudaFree(o->z2);
         if (o->bla16) cudaFree(o->bla16);
+        if (o->lin_lim) cudaFree(o->lin_lim);
         if (o->next_event) cudaFree(o->next_event);
         if (o->z2_64) cudaFree(o->z2_64);
         if (o->next_event64) cudaFree(o->next_event64);
@@ -661,6 +735,7 @@ int chaos_orbit_destroy(chaos_orbit *o)
     if (o->z32) cudaFree(o->z32);
     if (o->z2) cudaFree(o->z2);
     if (o->bla16) cudaFree(o->bla16);
+    if (o->lin_lim) cudaFree(o->lin_lim);
     if (o->next_event) cudaFree(o->next_event);
     if (o->z2_64) cudaFree(o->z2_64);
     if (o->next_event64) cudaFree(o->next_event64);
@@ -695,6 +770,7 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
     a.orbit64 = orb->z64;
     a.orbit2 = orb->z2;
     a.bla16 = orb->bla16;
+    a.lin_lim = orb->lin_lim;
     a.next_event = orb->next_event;
     a.orbit2_64 = orb->z2_64;
     a.next_event64 = orb->next_event64;
