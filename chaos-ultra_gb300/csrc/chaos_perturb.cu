@@ -73,7 +73,9 @@ template <class D> struct PerturbArgs {
     const double2 *orbit64;                // the same orbit in binary64 (rescaled glitch test)
     const float2 *orbit2;                  // 2 Z_m in binary32 (rescaled linear steps)
     const float4 *bla16;                   // the 16 rescaled linear steps from m composed: (P, Q), w' = P w + Q u
-    const int8_t *lin_lim;                 // largest e + ilogb(max |w|, |u|) for which bla16[m] stands in for 16 steps
+    const float4 *bla64;                   // the same for 64 steps
+    const char2 *lin_lim;                  // largest e + ilogb(max |w|, |u|) for which bla16[m] (x) and bla64[m] (y)
+                                           // stand in for full steps
     const uint32_t *next_event;            // first index >= m where a rescaled step's test can fire
     const double2 *orbit2_64;              // 2 Z_m in binary64 (binary64 linear steps)
     const uint32_t *next_event64;          // first index >= m where a binary64 linear step may not be exact
@@ -143,15 +145,19 @@ __device__ __forceinline__ float pow2f(int e) { return e >= -126 ? __int_as_floa
 constexpr int LIN_NONE = -128;
 
 // Keep the scaled difference's larger component within [2^-24, 2^24]: w and u
-// move by 2^-+24 and e the other way.  Past e > -100 the sample leaves the
+// move by multiples of 2^24 and e the other way.  Past e > -100 the sample leaves the
 // rescaled form and holds d = w 2^e, dc = u 2^e directly.
 template <class D>
 __device__ __forceinline__ void renormalise(D &dx, D &dy, D &dcx, D &dcy, int &e, bool &scaled)
 {
     const float mag = fmaxf(fabsf((float)dx), fabsf((float)dy));
     if (mag > 0x1p24f) {
-        dx *= D(0x1p-24f), dy *= D(0x1p-24f), dcx *= D(0x1p-24f), dcy *= D(0x1p-24f);
-        e += 24;
+        // by the multiple of 24 that brings |w| below 2^24 (more than one after a
+        // 64-step block; |w| < 2^128 so k <= 120)
+        const int k = 24 * (((int)((__float_as_uint(mag) >> 23) & 255u) - 127) / 24);
+        const float sc = __int_as_float((127 - k) << 23);
+        dx *= D(sc), dy *= D(sc), dcx *= D(sc), dcy *= D(sc);
+        e += k;
         if (e > -100) {
             const float q = pow2f(e);
             dx *= q, dy *= q, dcx *= q, dcy *= q;
@@ -251,6 +257,35 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
             }
 #pragma unroll 1
             for (int k = 0; k < K && !done; k++) {
+                if constexpr (sizeof(D) == 4) if (lin) {
+                    // a difference far below the orbit: over the next 64 (16) steps
+                    // (2Z_j + d_j) d_j stays within 2^-25 of 2Z_j d_j, below binary32
+                    // rounding, and no escape, glitch or orbit end can come, when
+                    // e + ilogb(max |w|, |u|) <= lin_lim[m].y (.x); then the composed
+                    // map w' = P w + Q u stands in for those steps
+                    const float big = fmaxf(fmaxf(fabsf((float)dx), fabsf((float)dy)),
+                                            fmaxf(fabsf((float)dcx), fabsf((float)dcy)));
+                    const int eb = (scaled ? e : 0) + (int)((__float_as_uint(big) >> 23) & 255u) - 127;
+                    const char2 lim = a.lin_lim[m];
+                    const uint32_t left = a.max_iter - i;
+                    const bool b64 = lim.y != LIN_NONE && eb <= lim.y && left > 64u;
+                    if (b64 || (lim.x != LIN_NONE && eb <= lim.x && left > 16u)) {
+                        const float4 pq = (b64 ? a.bla64 : a.bla16)[m];
+                        const float wx = (float)dx, wy = (float)dy, ux = (float)dcx, uy = (float)dcy;
+                        dx = __fmaf_rn(pq.x, wx, __fmaf_rn(-pq.y, wy, __fmaf_rn(pq.z, ux, -pq.w * uy)));
+                        dy = __fmaf_rn(pq.x, wy, __fmaf_rn(pq.y, wx, __fmaf_rn(pq.z, uy, pq.w * ux)));
+                        const uint32_t L = b64 ? 64u : 16u;
+                        m += L;
+                        i += L;
+                        const typename Vec2T<D>::type Z = a.orbit[m];
+                        Zx = Z.x;
+                        Zy = Z.y;
+                        if (scaled) renormalise(dx, dy, dcx, dcy, e, scaled);
+                        continue;
+                    }
+                    // lin_lim never exceeds -25: a plain difference that large stays out
+                    if (!scaled && eb > -25) lin = false;
+                }
                 if constexpr (S) if (scaled && e < -126) {
                     // linear steps up to (not onto) the next index whose tests can fire
                     constexpr uint32_t B = 16;  // |w| <= 2^24 grows at most 4^16-fold: below 2^56
@@ -285,42 +320,9 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                         Zy = Z.y;
                         dx = wx;
                         dy = wy;
-                        const float mag = fmaxf(fabsf(wx), fabsf(wy));
-                        if (mag > 0x1p24f) {
-                            dx *= D(0x1p-24f), dy *= D(0x1p-24f), dcx *= D(0x1p-24f), dcy *= D(0x1p-24f);
-                            e += 24;
-                        } else if (mag < 0x1p-24f && mag > 0.f && e > -1000) {
-                            dx *= D(0x1p24f), dy *= D(0x1p24f), dcx *= D(0x1p24f), dcy *= D(0x1p24f);
-                            e -= 24;
-                        }
+                        renormalise(dx, dy, dcx, dcy, e, scaled);
                         continue;
                     }
-                }
-                if constexpr (sizeof(D) == 4) if (lin) {
-                    // a difference far below the orbit (rescaled at e >= -126, or plain):
-                    // over the next 16 steps (2Z_j + d_j) d_j stays within 2^-25 of
-                    // 2Z_j d_j, below binary32 rounding, and no escape, glitch or orbit
-                    // end can come, when e + ilogb(max |w|, |u|) <= lin_lim[m]; then the
-                    // composed block w' = P w + Q u stands in for the 16 steps
-                    const float big = fmaxf(fmaxf(fabsf((float)dx), fabsf((float)dy)),
-                                            fmaxf(fabsf((float)dcx), fabsf((float)dcy)));
-                    const int eb = (scaled ? e : 0) + (int)((__float_as_uint(big) >> 23) & 255u) - 127;
-                    const int lim = a.lin_lim[m];
-                    if (lim != LIN_NONE && eb <= lim && a.max_iter - i > 16u) {
-                        const float4 pq = a.bla16[m];
-                        const float wx = (float)dx, wy = (float)dy, ux = (float)dcx, uy = (float)dcy;
-                        dx = __fmaf_rn(pq.x, wx, __fmaf_rn(-pq.y, wy, __fmaf_rn(pq.z, ux, -pq.w * uy)));
-                        dy = __fmaf_rn(pq.x, wy, __fmaf_rn(pq.y, wx, __fmaf_rn(pq.z, uy, pq.w * ux)));
-                        m += 16;
-                        i += 16;
-                        const typename Vec2T<D>::type Z = a.orbit[m];
-                        Zx = Z.x;
-                        Zy = Z.y;
-                        if (scaled) renormalise(dx, dy, dcx, dcy, e, scaled);
-                        continue;
-                    }
-                    // lin_lim never exceeds -25: a plain difference that large stays out
-                    if (!scaled && eb > -25) lin = false;
                 }
                 if constexpr (S) if (scaled) {
                     // w' = (2Z + 2^e w) w + u
@@ -539,7 +541,8 @@ struct chaos_orbit {
     double2 *z64 = nullptr;
     float2 *z2 = nullptr;              // 2 Z in binary32
     float4 *bla16 = nullptr;           // see the rescaled linear steps of k_perturb
-    int8_t *lin_lim = nullptr;         // see the composed blocks of k_perturb
+    float4 *bla64 = nullptr;           // see the composed blocks of k_perturb
+    char2 *lin_lim = nullptr;          // see the composed blocks of k_perturb
     uint32_t *next_event = nullptr;    // see the rescaled linear steps of k_perturb
     double2 *z2_64 = nullptr;          // 2 Z in binary64
     uint32_t *next_event64 = nullptr;  // see the binary64 linear steps of k_perturb
@@ -603,46 +606,71 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
         z32[k] = make_float2((float)z64[k].x, (float)z64[k].y);
         z2[k] = make_float2(2.f * z32[k].x, 2.f * z32[k].y);
     }
-    // bla16[m]: the 16 rescaled linear steps w <- 2Z_j w + u, j = m..m+15 (with
-    // 2Z_j as the kernel holds it, binary32), composed in binary64 into
-    // w <- P w + Q u and rounded to binary32 once
+    // bla16[m], bla64[m]: the 16 (64) rescaled linear steps w <- 2Z_j w + u
+    // from j = m (with 2Z_j as the kernel holds it, binary32), composed in
+    // binary64 into w <- P w + Q u and rounded to binary32 once
     //
-    // lin_lim[m]: where the block from m may also stand in for 16 quadratic
-    // steps.  With w_j = P_(m->j) w + Q_(m->j) u the difference at step j,
-    // |2^e w_j| < 2^(e + ilogb(M) + 1.5) (|P_j| + |Q_j|) for M = max(|w|, |u|)
-    // componentwise; the quadratic term is negligible when that stays below
-    // 2^-24 |Z_j| for j = m..m+16, i.e. e + ilogb(M) <= floor(h - 25.5) with
-    // h = min_j log2|Z_j| - log2(|P_j| + |Q_j|).  No test may fire inside:
-    // |Z_j|^2 < 3.99 and >= 2^-98 for j = m+1..m+16 (margins on the escape
-    // and rescaled glitch tests, which then see z_j = Z_j to binary32
-    // precision), the block ends before the orbit's last index, and Z_m != 0.
+    // lin_lim[m] = (l16, l64): where those blocks also stand in for 16 (64)
+    // full steps.  With w_j = P_(m->j) w + Q_(m->j) u the difference at step
+    // j and M = max(|w|, |u|) componentwise,
+    //     |2^e w_j| < 2^(e + ilogb(M) + 1.5) (|P_j| + |Q_j|)
+    //              <= 2^(e + ilogb(M) + 1.5) sqrt(2 (|P_j|^2 + |Q_j|^2)),
+    // and the quadratic term of step j is negligible when that stays below
+    // 2^-24 |Z_j|: for j = m..m+L that holds when
+    //     e + ilogb(M) <= floor(log2(rho) / 2 - 25.5),
+    //     rho = min_j |Z_j|^2 / (2 (|P_j|^2 + |Q_j|^2)).
+    // No test may fire inside: |Z_j|^2 < 3.99 and >= 2^-98 for j = m+1..m+L
+    // (margins on the escape and rescaled glitch tests, which then see
+    // z_j = Z_j to binary32 precision), the block ends before the orbit's last
+    // index, and Z_m != 0.  A 64-step block also keeps |w| below 2^127 at its
+    // end (|w|, |u| <= 2^25 before it): 2 (|P|^2 + |Q|^2) <= 2^200.
     std::vector<float4> bla16(z64.size(), make_float4(0.f, 0.f, 0.f, 0.f));
-    std::vector<int8_t> lin_lim(z64.size(), (int8_t)LIN_NONE);
-    for (size_t m = 0; m + 16 <= z2.size(); m++) {
-        double px = 1.0, py = 0.0, qx = 0.0, qy = 0.0;
-        const bool room = m + 16 < z64.size() - 1;
-        bool ok = room;
-        double h = INFINITY;
-        for (size_t j = m; j <= m + 16 && j < z32.size(); j++) {
-            if (ok) {
-                const double az = std::hypot((double)z32[j].x, (double)z32[j].y);
-                const float r2 = std::fmaf(z32[j].x, z32[j].x, z32[j].y * z32[j].y);
-                if (!(az > 0.0) || (j > m && (!(r2 < 3.99f) || r2 < 0x1p-98f)))
-                    ok = false;
-                else
-                    h = std::min(h, std::log2(az) - std::log2(std::hypot(px, py) + std::hypot(qx, qy)));
+    std::vector<float4> bla64(z64.size(), make_float4(0.f, 0.f, 0.f, 0.f));
+    std::vector<char2> lin_lim(z64.size(), make_char2((signed char)LIN_NONE, (signed char)LIN_NONE));
+    {
+        const size_t n = z32.size(), last = n - 1;
+        std::vector<double> zz(n);
+        for (size_t j = 0; j < n; j++) zz[j] = (double)z32[j].x * z32[j].x + (double)z32[j].y * z32[j].y;
+        auto event = [&](size_t j) {
+            const float r2 = std::fmaf(z32[j].x, z32[j].x, z32[j].y * z32[j].y);
+            return !(r2 < 3.99f) || r2 < 0x1p-98f;
+        };
+        auto lim_of = [](double rho) {
+            if (!(rho > 0.0) || !std::isfinite(rho)) return (int)LIN_NONE;
+            return (int)std::max(-127.0, std::min(127.0, std::floor(0.5 * std::log2(rho) - 25.5)));
+        };
+        for (size_t m = 0; m + 16 <= n; m++) {
+            double px = 1.0, py = 0.0, qx = 0.0, qy = 0.0;
+            bool ok16 = m + 16 < last && zz[m] > 0.0, ok64 = m + 64 < last && zz[m] > 0.0;
+            double rho = INFINITY, rho16 = INFINITY;
+            for (size_t j = m; j <= m + 64 && j < n; j++) {
+                if (j > m && event(j)) {
+                    if (j <= m + 16) ok16 = false;
+                    ok64 = false;
+                }
+                if (!ok64 && j > m + 16) break;
+                rho = std::min(rho, zz[j] / (2.0 * (px * px + py * py + qx * qx + qy * qy)));
+                if (j == m + 16) {
+                    rho16 = rho;
+                    bla16[m] = make_float4((float)px, (float)py, (float)qx, (float)qy);
+                    if (!ok64) break;
+                }
+                if (j == m + 64) {
+                    if (!(2.0 * (px * px + py * py + qx * qx + qy * qy) <= 0x1p200)) ok64 = false;
+                    bla64[m] = make_float4((float)px, (float)py, (float)qx, (float)qy);
+                    break;
+                }
+                const double ax = z2[j].x, ay = z2[j].y;
+                const double npx = ax * px - ay * py, npy = ax * py + ay * px;
+                const double nqx = ax * qx - ay * qy + 1.0, nqy = ax * qy + ay * qx;
+                px = npx;
+                py = npy;
+                qx = nqx;
+                qy = nqy;
             }
-            if (j == m + 16) break;
-            const double ax = z2[j].x, ay = z2[j].y;
-            const double npx = ax * px - ay * py, npy = ax * py + ay * px;
-            const double nqx = ax * qx - ay * qy + 1.0, nqy = ax * qy + ay * qx;
-            px = npx;
-            py = npy;
-            qx = nqx;
-            qy = nqy;
+            lin_lim[m] = make_char2((signed char)(ok16 ? lim_of(rho16) : LIN_NONE),
+                                    (signed char)(ok64 ? lim_of(rho) : LIN_NONE));
         }
-        bla16[m] = make_float4((float)px, (float)py, (float)qx, (float)qy);
-        if (ok && std::isfinite(h)) lin_lim[m] = (int8_t)std::max(-127.0, std::min(127.0, std::floor(h - 25.5)));
     }
     // next_event[m]: first index j >= m where a rescaled step's test can fire,
     // evaluated as the kernel does (binary32 |Z_j|^2 with one fused add)
@@ -691,8 +719,11 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
     if (e == cudaSuccess) e = cudaMemcpy(o->z2, z2.data(), z2.size() * sizeof(float2), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&o->bla16, bla16.size() * sizeof(float4));
     if (e == cudaSuccess) e = cudaMemcpy(o->bla16, bla16.data(), bla16.size() * sizeof(float4), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&o->lin_lim, lin_lim.size());
-    if (e == cudaSuccess) e = cudaMemcpy(o->lin_lim, lin_lim.data(), lin_lim.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&o->bla64, bla64.size() * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMemcpy(o->bla64, bla64.data(), bla64.size() * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&o->lin_lim, lin_lim.size() * sizeof(char2));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(o->lin_lim, lin_lim.data(), lin_lim.size() * sizeof(char2), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&o->next_event, next_event.size() * sizeof(uint32_t));
     if (e == cudaSuccess)
         e = cudaMemcpy(o->next_event, next_event.data(), next_event.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
@@ -708,6 +739,7 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
         if (o->z32) cudaFree(o->z32);
         if (o->z2) cudaFree(o->z2);
         if (o->bla16) cudaFree(o->bla16);
+        if (o->bla64) cudaFree(o->bla64);
         if (o->lin_lim) cudaFree(o->lin_lim);
         if (o->next_event) cudaFree(o->next_event);
         if (o->z2_64) cudaFree(o->z2_64);
@@ -735,6 +767,7 @@ int chaos_orbit_destroy(chaos_orbit *o)
     if (o->z32) cudaFree(o->z32);
     if (o->z2) cudaFree(o->z2);
     if (o->bla16) cudaFree(o->bla16);
+    if (o->bla64) cudaFree(o->bla64);
     if (o->lin_lim) cudaFree(o->lin_lim);
     if (o->next_event) cudaFree(o->next_event);
     if (o->z2_64) cudaFree(o->z2_64);
@@ -770,6 +803,7 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
     a.orbit64 = orb->z64;
     a.orbit2 = orb->z2;
     a.bla16 = orb->bla16;
+    a.bla64 = orb->bla64;
     a.lin_lim = orb->lin_lim;
     a.next_event = orb->next_event;
     a.orbit2_64 = orb->z2_64;
