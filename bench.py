@@ -1081,9 +1081,10 @@ def run_deep(args):
 
     # roofline: FP32 pipe against the plain escape step's 6 FP32-pipe
     # instructions per pixel-iteration (the headline unit of every tier).  The
-    # perturbation steps themselves cost: linear rescaled step 4 FFMA + 1 load
-    # of 2Z; quadratic rescaled step 12; plain-difference step 16 (6 for the
-    # difference, 2 for z, 2 for |z|^2, 2 for |d|^2, compares).
+    # perturbation steps themselves cost: a composed block of 16 or 64 linear
+    # steps 8 FP32 operations + one 16-byte load; an event-bounded linear step
+    # 4 FFMA + 1 load of 2Z; quadratic rescaled step 12; plain-difference step
+    # 16 (6 for the difference, 2 for z, 2 for |z|^2, 2 for |d|^2, compares).
     peak = cg.measure_fma_peak(cg.TIER_F32)
     ops = 6
     achieved = iters / (kernel_ms / 1e3) * ops
@@ -1091,8 +1092,9 @@ def run_deep(args):
             "frac": achieved / (peak / 2), "traffic": None,
             "peak_source": "measured in this run: chaos_measure_fma_peak (full-occupancy FFMA chains)",
             "ops_per_iteration": ops,
-            "step_costs": {"rescaled_linear": 4, "rescaled_quadratic": 12, "plain_difference": 16},
-            "kernel": "k_perturb<float,16,rescaled>"}
+            "step_costs": {"composed_block_16_or_64": 8, "rescaled_linear": 4, "rescaled_quadratic": 12,
+                           "plain_difference": 16},
+            "kernel": "k_perturb<float,64,rescaled>"}
 
     # CPU leg: the oracle's multi-word direct iteration on a bounded sample of pixels
     from oracle.oracle import Oracle
