@@ -76,6 +76,8 @@ template <class D> struct PerturbArgs {
     const float4 *bla64;                   // the same for 64 steps
     const char2 *lin_lim;                  // largest e + ilogb(max |w|, |u|) for which bla16[m] (x) and bla64[m] (y)
                                            // stand in for full steps
+    const double2 *bla16d, *bla64d;        // the same for binary64 differences: P at [2m], Q at [2m + 1]
+    const char2 *lin_limd;                 // their bounds on ilogb(max |d|, |dc|)
     const uint32_t *next_event;            // first index >= m where a rescaled step's test can fire
     const double2 *orbit2_64;              // 2 Z_m in binary64 (binary64 linear steps)
     const uint32_t *next_event64;          // first index >= m where a binary64 linear step may not be exact
@@ -372,6 +374,33 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                     renormalise(dx, dy, dcx, dcy, e, scaled);
                     continue;
                 }
+                if constexpr (sizeof(D) == 8) if (lin) {
+                    // the composed blocks for binary64 differences: over the next 64 (16)
+                    // steps the dropped d^2 term stays below binary64 rounding and no
+                    // test can fire when ilogb(max |d|, |dc|) <= lin_limd[m].y (.x)
+                    const double big = fmax(fmax(fabs((double)dx), fabs((double)dy)),
+                                            fmax(fabs((double)dcx), fabs((double)dcy)));
+                    const int eb = (int)(((uint32_t)__double2hiint(big) >> 20) & 0x7ffu) - 1023;
+                    const char2 lim = a.lin_limd[m];
+                    const uint32_t left = a.max_iter - i;
+                    const bool b64 = lim.y != LIN_NONE && eb <= lim.y && left > 64u;
+                    if (b64 || (lim.x != LIN_NONE && eb <= lim.x && left > 16u)) {
+                        const double2 *pq = (b64 ? a.bla64d : a.bla16d) + 2u * m;
+                        const double2 P = pq[0], Q = pq[1];
+                        const double wx = (double)dx, wy = (double)dy, ux = (double)dcx, uy = (double)dcy;
+                        dx = (D)__fma_rn(P.x, wx, __fma_rn(-P.y, wy, __fma_rn(Q.x, ux, -Q.y * uy)));
+                        dy = (D)__fma_rn(P.x, wy, __fma_rn(P.y, wx, __fma_rn(Q.x, uy, Q.y * ux)));
+                        const uint32_t L = b64 ? 64u : 16u;
+                        m += L;
+                        i += L;
+                        const typename Vec2T<D>::type Z = a.orbit[m];
+                        Zx = Z.x;
+                        Zy = Z.y;
+                        continue;
+                    }
+                    // lin_limd never exceeds -54: a difference that large stays out
+                    if (eb > -54) lin = false;
+                }
                 if constexpr (!S && sizeof(D) == 8) {
                     // binary64 differences far below the orbit (|d|, |dc| < 2^-120 while
                     // both components of Z stay above 2^-20): 2Z + d rounds to 2Z and
@@ -543,6 +572,9 @@ struct chaos_orbit {
     float4 *bla16 = nullptr;           // see the rescaled linear steps of k_perturb
     float4 *bla64 = nullptr;           // see the composed blocks of k_perturb
     char2 *lin_lim = nullptr;          // see the composed blocks of k_perturb
+    double2 *bla16d = nullptr;         // the same blocks for binary64 differences ((P, Q) as two double2)
+    double2 *bla64d = nullptr;
+    char2 *lin_limd = nullptr;
     uint32_t *next_event = nullptr;    // see the rescaled linear steps of k_perturb
     double2 *z2_64 = nullptr;          // 2 Z in binary64
     uint32_t *next_event64 = nullptr;  // see the binary64 linear steps of k_perturb
@@ -578,6 +610,75 @@ int api_orbit_create_d(double center_x, double center_y, uint32_t bits, uint32_t
 }
 }  // namespace chaos
 
+// A composed block: L linear steps w <- a_j w + u (a_j = 2Z_j) from m as
+// w <- P w + Q u.
+struct BlockMap {
+    double px = 0, py = 0, qx = 0, qy = 0;
+};
+
+// The 16- and 64-step blocks from every index m, composed in binary64 from
+// a2[j] = 2Z_j as the kernel holds it, and where each may stand in for full
+// steps (lim[m] = (l16, l64)).  With w_j = P_(m->j) w + Q_(m->j) u the
+// difference at step j and M = max(|w|, |u|) componentwise,
+//     |2^e w_j| < 2^(e + ilogb(M) + 1.5) (|P_j| + |Q_j|)
+//              <= 2^(e + ilogb(M) + 1.5) sqrt(2 (|P_j|^2 + |Q_j|^2)),
+// and the quadratic term of step j is below the arithmetic's rounding (2^-p
+// relative) when that stays below 2^-p |Z_j| (p = slack - 1.5): for
+// j = m..m+L that holds when
+//     e + ilogb(M) <= floor(log2(rho) / 2 - slack),
+//     rho = min_j |Z_j|^2 / (2 (|P_j|^2 + |Q_j|^2))   (zz[j] = |Z_j|^2).
+// No test may fire inside: ev[j] is false for j = m+1..m+L (the caller sets
+// it where |Z_j|^2 >= 3.99 or < 2^-98, margins on the escape and glitch tests,
+// which then see z_j = Z_j to the arithmetic's precision), the block ends
+// before the orbit's last index, and Z_m != 0.  A 64-step block also keeps
+// |w| below 2^127 at its end (|w|, |u| <= 2^25 before it):
+// 2 (|P|^2 + |Q|^2) <= 2^200.  A bound below -127 is stored as none.
+static void compose_blocks(const std::vector<double2> &a2, const std::vector<double> &zz,
+                           const std::vector<char> &ev, double slack, std::vector<BlockMap> &b16,
+                           std::vector<BlockMap> &b64, std::vector<char2> &lim)
+{
+    const size_t n = a2.size(), last = n - 1;
+    b16.assign(n, BlockMap());
+    b64.assign(n, BlockMap());
+    lim.assign(n, make_char2((signed char)LIN_NONE, (signed char)LIN_NONE));
+    auto lim_of = [slack](double rho) {
+        if (!(rho > 0.0) || !std::isfinite(rho)) return (int)LIN_NONE;
+        const double l = std::floor(0.5 * std::log2(rho) - slack);
+        return l < -127.0 ? (int)LIN_NONE : (int)std::min(127.0, l);
+    };
+    for (size_t m = 0; m + 16 <= n; m++) {
+        double px = 1.0, py = 0.0, qx = 0.0, qy = 0.0;
+        bool ok16 = m + 16 < last && zz[m] > 0.0, ok64 = m + 64 < last && zz[m] > 0.0;
+        double rho = INFINITY, rho16 = INFINITY;
+        for (size_t j = m; j <= m + 64 && j < n; j++) {
+            if (j > m && ev[j]) {
+                if (j <= m + 16) ok16 = false;
+                ok64 = false;
+            }
+            if (!ok64 && j > m + 16) break;
+            rho = std::min(rho, zz[j] / (2.0 * (px * px + py * py + qx * qx + qy * qy)));
+            if (j == m + 16) {
+                rho16 = rho;
+                b16[m] = BlockMap{px, py, qx, qy};
+                if (!ok64) break;
+            }
+            if (j == m + 64) {
+                if (!(2.0 * (px * px + py * py + qx * qx + qy * qy) <= 0x1p200)) ok64 = false;
+                b64[m] = BlockMap{px, py, qx, qy};
+                break;
+            }
+            const double ax = a2[j].x, ay = a2[j].y;
+            const double npx = ax * px - ay * py, npy = ax * py + ay * px;
+            const double nqx = ax * qx - ay * qy + 1.0, nqy = ax * qy + ay * qx;
+            px = npx;
+            py = npy;
+            qx = nqx;
+            qy = nqy;
+        }
+        lim[m] = make_char2((signed char)(ok16 ? lim_of(rho16) : LIN_NONE), (signed char)(ok64 ? lim_of(rho) : LIN_NONE));
+    }
+}
+
 static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t max_iterations, chaos_orbit **out)
 {
 
@@ -606,70 +707,26 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
         z32[k] = make_float2((float)z64[k].x, (float)z64[k].y);
         z2[k] = make_float2(2.f * z32[k].x, 2.f * z32[k].y);
     }
-    // bla16[m], bla64[m]: the 16 (64) rescaled linear steps w <- 2Z_j w + u
-    // from j = m (with 2Z_j as the kernel holds it, binary32), composed in
-    // binary64 into w <- P w + Q u and rounded to binary32 once
-    //
-    // lin_lim[m] = (l16, l64): where those blocks also stand in for 16 (64)
-    // full steps.  With w_j = P_(m->j) w + Q_(m->j) u the difference at step
-    // j and M = max(|w|, |u|) componentwise,
-    //     |2^e w_j| < 2^(e + ilogb(M) + 1.5) (|P_j| + |Q_j|)
-    //              <= 2^(e + ilogb(M) + 1.5) sqrt(2 (|P_j|^2 + |Q_j|^2)),
-    // and the quadratic term of step j is negligible when that stays below
-    // 2^-24 |Z_j|: for j = m..m+L that holds when
-    //     e + ilogb(M) <= floor(log2(rho) / 2 - 25.5),
-    //     rho = min_j |Z_j|^2 / (2 (|P_j|^2 + |Q_j|^2)).
-    // No test may fire inside: |Z_j|^2 < 3.99 and >= 2^-98 for j = m+1..m+L
-    // (margins on the escape and rescaled glitch tests, which then see
-    // z_j = Z_j to binary32 precision), the block ends before the orbit's last
-    // index, and Z_m != 0.  A 64-step block also keeps |w| below 2^127 at its
-    // end (|w|, |u| <= 2^25 before it): 2 (|P|^2 + |Q|^2) <= 2^200.
+    // the composed 16- and 64-step blocks of binary32 differences, from 2Z_j
+    // as that kernel holds it (binary32) and its |Z_j|^2 and tests
     std::vector<float4> bla16(z64.size(), make_float4(0.f, 0.f, 0.f, 0.f));
     std::vector<float4> bla64(z64.size(), make_float4(0.f, 0.f, 0.f, 0.f));
-    std::vector<char2> lin_lim(z64.size(), make_char2((signed char)LIN_NONE, (signed char)LIN_NONE));
+    std::vector<char2> lin_lim;
     {
-        const size_t n = z32.size(), last = n - 1;
-        std::vector<double> zz(n);
-        for (size_t j = 0; j < n; j++) zz[j] = (double)z32[j].x * z32[j].x + (double)z32[j].y * z32[j].y;
-        auto event = [&](size_t j) {
+        std::vector<double2> a2(z64.size());
+        std::vector<double> zz(z64.size());
+        std::vector<char> ev(z64.size());
+        for (size_t j = 0; j < z64.size(); j++) {
+            a2[j] = make_double2(z2[j].x, z2[j].y);
+            zz[j] = (double)z32[j].x * z32[j].x + (double)z32[j].y * z32[j].y;
             const float r2 = std::fmaf(z32[j].x, z32[j].x, z32[j].y * z32[j].y);
-            return !(r2 < 3.99f) || r2 < 0x1p-98f;
-        };
-        auto lim_of = [](double rho) {
-            if (!(rho > 0.0) || !std::isfinite(rho)) return (int)LIN_NONE;
-            return (int)std::max(-127.0, std::min(127.0, std::floor(0.5 * std::log2(rho) - 25.5)));
-        };
-        for (size_t m = 0; m + 16 <= n; m++) {
-            double px = 1.0, py = 0.0, qx = 0.0, qy = 0.0;
-            bool ok16 = m + 16 < last && zz[m] > 0.0, ok64 = m + 64 < last && zz[m] > 0.0;
-            double rho = INFINITY, rho16 = INFINITY;
-            for (size_t j = m; j <= m + 64 && j < n; j++) {
-                if (j > m && event(j)) {
-                    if (j <= m + 16) ok16 = false;
-                    ok64 = false;
-                }
-                if (!ok64 && j > m + 16) break;
-                rho = std::min(rho, zz[j] / (2.0 * (px * px + py * py + qx * qx + qy * qy)));
-                if (j == m + 16) {
-                    rho16 = rho;
-                    bla16[m] = make_float4((float)px, (float)py, (float)qx, (float)qy);
-                    if (!ok64) break;
-                }
-                if (j == m + 64) {
-                    if (!(2.0 * (px * px + py * py + qx * qx + qy * qy) <= 0x1p200)) ok64 = false;
-                    bla64[m] = make_float4((float)px, (float)py, (float)qx, (float)qy);
-                    break;
-                }
-                const double ax = z2[j].x, ay = z2[j].y;
-                const double npx = ax * px - ay * py, npy = ax * py + ay * px;
-                const double nqx = ax * qx - ay * qy + 1.0, nqy = ax * qy + ay * qx;
-                px = npx;
-                py = npy;
-                qx = nqx;
-                qy = nqy;
-            }
-            lin_lim[m] = make_char2((signed char)(ok16 ? lim_of(rho16) : LIN_NONE),
-                                    (signed char)(ok64 ? lim_of(rho) : LIN_NONE));
+            ev[j] = !(r2 < 3.99f) || r2 < 0x1p-98f;
+        }
+        std::vector<BlockMap> b16, b64;
+        compose_blocks(a2, zz, ev, 25.5, b16, b64, lin_lim);
+        for (size_t m = 0; m < z64.size(); m++) {
+            bla16[m] = make_float4((float)b16[m].px, (float)b16[m].py, (float)b16[m].qx, (float)b16[m].qy);
+            bla64[m] = make_float4((float)b64[m].px, (float)b64[m].py, (float)b64[m].qx, (float)b64[m].qy);
         }
     }
     // next_event[m]: first index j >= m where a rescaled step's test can fire,
@@ -701,6 +758,27 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
             next_event64[j] = next;
         }
     }
+    // the same blocks for binary64 differences, from the binary64 orbit, with
+    // binary64 rounding (2^-53 in place of 2^-24)
+    std::vector<double2> bla16d(2 * z64.size()), bla64d(2 * z64.size());
+    std::vector<char2> lin_limd;
+    {
+        std::vector<double> zz(z64.size());
+        std::vector<char> ev(z64.size());
+        for (size_t j = 0; j < z64.size(); j++) {
+            zz[j] = z64[j].x * z64[j].x + z64[j].y * z64[j].y;
+            const double r2 = std::fma(z64[j].x, z64[j].x, z64[j].y * z64[j].y);
+            ev[j] = !(r2 < 3.99) || r2 < 0x1p-98;
+        }
+        std::vector<BlockMap> b16, b64;
+        compose_blocks(z2_64, zz, ev, 54.5, b16, b64, lin_limd);
+        for (size_t m = 0; m < z64.size(); m++) {
+            bla16d[2 * m] = make_double2(b16[m].px, b16[m].py);
+            bla16d[2 * m + 1] = make_double2(b16[m].qx, b16[m].qy);
+            bla64d[2 * m] = make_double2(b64[m].px, b64[m].py);
+            bla64d[2 * m + 1] = make_double2(b64[m].qx, b64[m].qy);
+        }
+    }
 
     chaos_orbit *o = new (std::nothrow) chaos_orbit();
     if (!o) return api_fail(CHAOS_ERR_OUT_OF_MEMORY, "out of host memory");
@@ -727,6 +805,15 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
     if (e == cudaSuccess) e = cudaMalloc(&o->next_event, next_event.size() * sizeof(uint32_t));
     if (e == cudaSuccess)
         e = cudaMemcpy(o->next_event, next_event.data(), next_event.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&o->bla16d, bla16d.size() * sizeof(double2));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(o->bla16d, bla16d.data(), bla16d.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&o->bla64d, bla64d.size() * sizeof(double2));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(o->bla64d, bla64d.data(), bla64d.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&o->lin_limd, lin_limd.size() * sizeof(char2));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(o->lin_limd, lin_limd.data(), lin_limd.size() * sizeof(char2), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&o->z2_64, z2_64.size() * sizeof(double2));
     if (e == cudaSuccess)
         e = cudaMemcpy(o->z2_64, z2_64.data(), z2_64.size() * sizeof(double2), cudaMemcpyHostToDevice);
@@ -742,6 +829,9 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
         if (o->bla64) cudaFree(o->bla64);
         if (o->lin_lim) cudaFree(o->lin_lim);
         if (o->next_event) cudaFree(o->next_event);
+        if (o->bla16d) cudaFree(o->bla16d);
+        if (o->bla64d) cudaFree(o->bla64d);
+        if (o->lin_limd) cudaFree(o->lin_limd);
         if (o->z2_64) cudaFree(o->z2_64);
         if (o->next_event64) cudaFree(o->next_event64);
         delete o;
@@ -770,6 +860,9 @@ int chaos_orbit_destroy(chaos_orbit *o)
     if (o->bla64) cudaFree(o->bla64);
     if (o->lin_lim) cudaFree(o->lin_lim);
     if (o->next_event) cudaFree(o->next_event);
+    if (o->bla16d) cudaFree(o->bla16d);
+    if (o->bla64d) cudaFree(o->bla64d);
+    if (o->lin_limd) cudaFree(o->lin_limd);
     if (o->z2_64) cudaFree(o->z2_64);
     if (o->next_event64) cudaFree(o->next_event64);
     delete o;
@@ -805,6 +898,9 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
     a.bla16 = orb->bla16;
     a.bla64 = orb->bla64;
     a.lin_lim = orb->lin_lim;
+    a.bla16d = orb->bla16d;
+    a.bla64d = orb->bla64d;
+    a.lin_limd = orb->lin_limd;
     a.next_event = orb->next_event;
     a.orbit2_64 = orb->z2_64;
     a.next_event64 = orb->next_event64;
