@@ -32,7 +32,9 @@
 // binary32 difference at e >= -126 or a plain one, while the difference stays
 // so far below the orbit over the block that the dropped d^2 term is below
 // binary32 rounding (a per-index exponent bound, lin_lim, set on the host from
-// |Z_j| and the partial products).  Binary64 differences get the same treatment
+// |Z_j| and the partial products); 64-step maps go first where their bound
+// allows.  Binary64 differences have their own 16- and 64-step maps and bounds
+// (binary64 rounding); where those do not apply, short linear steps run
 // while |d| and |dc| stay below 2^-120 and both components of Z above 2^-20:
 // then 2Z + d rounds to 2Z and Z + d' to Z, so d' = 2Z d + dc (4 DFMA) is the
 // full step bit for bit, and its tests depend on the orbit index alone.
