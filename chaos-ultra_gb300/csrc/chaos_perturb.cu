@@ -259,8 +259,45 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                 lin = true;
                 if (a.max_iter == 0) done = true;
             }
+            // d' = (2Z + d) d + dc with its tests; true when the sample is done
+            auto plain_step = [&]() -> bool {
+                D wx = O::fma(D(2), Zx, dx), wy = O::fma(D(2), Zy, dy);
+                D ndx = O::fma(wx, dx, O::fma(-wy, dy, dcx));
+                D ndy = O::fma(wx, dy, O::fma(wy, dx, dcy));
+                ++m;
+                ++i;
+                typename Vec2T<D>::type Z = a.orbit[m];
+                D zx = O::add(Z.x, ndx), zy = O::add(Z.y, ndy);
+                r2 = O::fma(zx, zx, O::mul(zy, zy));
+                if (!(r2 < D(4)) || i == a.max_iter) return true;
+                if (m == a.orbit_last || glitch_test(zx, zy, ndx, ndy, r2)) {
+                    dx = zx;
+                    dy = zy;
+                    Zx = D(0);
+                    Zy = D(0);
+                    m = 0;
+                    ++rebases;
+                } else {
+                    dx = ndx;
+                    dy = ndy;
+                    Zx = Z.x;
+                    Zy = Z.y;
+                }
+                return false;
+            };
 #pragma unroll 1
             for (int k = 0; k < K && !done; k++) {
+                if (!lin && !scaled) {
+                    // past every composed and linear form (a plain difference too large
+                    // for them, for good): plain steps for the rest of the round
+#pragma unroll 1
+                    for (; k < K; k++)
+                        if (plain_step()) {
+                            done = true;
+                            break;
+                        }
+                    break;
+                }
                 if constexpr (sizeof(D) == 4) if (lin) {
                     // a difference far below the orbit: over the next 64 (16) steps
                     // (2Z_j + d_j) d_j stays within 2^-25 of 2Z_j d_j, below binary32
@@ -448,31 +485,9 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                         }
                     }
                 }
-                // d' = (2Z + d) d + dc
-                D wx = O::fma(D(2), Zx, dx), wy = O::fma(D(2), Zy, dy);
-                D ndx = O::fma(wx, dx, O::fma(-wy, dy, dcx));
-                D ndy = O::fma(wx, dy, O::fma(wy, dx, dcy));
-                ++m;
-                ++i;
-                typename Vec2T<D>::type Z = a.orbit[m];
-                D zx = O::add(Z.x, ndx), zy = O::add(Z.y, ndy);
-                r2 = O::fma(zx, zx, O::mul(zy, zy));
-                if (!(r2 < D(4)) || i == a.max_iter) {
+                if (plain_step()) {
                     done = true;
                     break;
-                }
-                if (m == a.orbit_last || glitch_test(zx, zy, ndx, ndy, r2)) {
-                    dx = zx;
-                    dy = zy;
-                    Zx = D(0);
-                    Zy = D(0);
-                    m = 0;
-                    ++rebases;
-                } else {
-                    dx = ndx;
-                    dy = ndy;
-                    Zx = Z.x;
-                    Zy = Z.y;
                 }
             }
         }
