@@ -324,8 +324,10 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                         if (scaled) renormalise(dx, dy, dcx, dcy, e, scaled);
                         continue;
                     }
-                    // lin_lim never exceeds -25: a plain difference that large stays out
-                    if (!scaled && eb > -25) lin = false;
+                    // lin_lim never exceeds -25: a plain difference that large stays out;
+                    // one 8 binades past this index's bound (it grows ~1 binade a step,
+                    // and the bound moves by a few between indices) is taken as out too
+                    if (!scaled && (eb > -25 || (lim.x != LIN_NONE && eb > lim.x + 8))) lin = false;
                 }
                 if constexpr (S) if (scaled && e < -126) {
                     // linear steps up to (not onto) the next index whose tests can fire
@@ -437,8 +439,9 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                         Zy = Z.y;
                         continue;
                     }
-                    // lin_limd never exceeds -54: a difference that large stays out
-                    if (eb > -54) lin = false;
+                    // lin_limd never exceeds -54: a difference that large stays out (and,
+                    // as for binary32, one 8 binades past this index's bound)
+                    if (eb > -54 || (lim.x != LIN_NONE && eb > lim.x + 8)) lin = false;
                 }
                 if constexpr (!S && sizeof(D) == 8) {
                     // binary64 differences far below the orbit (|d|, |dc| < 2^-120 while
@@ -519,13 +522,13 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                 divmod_magic(pix, a.w, w_magic, py, px);
                 if (a.pixels)
                     store_pixel(pixel_ptr(a.pixels, a.pixels_pitch, px, py),
-                                make_pixel(__fdiv_rn(acc_v, (float)a.spp), (float)a.spp));
+                                make_pixel(a.spp == 1u ? acc_v : __fdiv_rn(acc_v, (float)a.spp), (float)a.spp));
                 if (a.rgba) {
                     uint32_t out = 0;
                     float n = (float)a.spp;
 #pragma unroll
                     for (int k = 0; k < 4; k++) {
-                        float v = __fadd_rn(__fdiv_rn(acc[k], n), 0.5f);
+                        float v = __fadd_rn(a.spp == 1u ? acc[k] : __fdiv_rn(acc[k], n), 0.5f);
                         v = v < 255.f ? v : 255.f;
                         out |= ((uint32_t)v & 255u) << (8 * k);
                     }
