@@ -97,6 +97,12 @@ template <class D> struct PerturbArgs {
     uint32_t *counter;
     unsigned long long budget_ns;  // 0, or the run time after which warps stop (RUN_STATUS_TIMEOUT into *status)
     uint32_t *status;
+    // binary32 set-up of rescaled samples at pixel centres (dc_fast): with
+    // t = p - (half - 1/2), exact in binary32, dc 2^-dc_e = t ps' + off' where
+    // ps' = ps 2^-dc_e in [1, 2) and off' = off 2^-dc_e are binary32 pairs
+    bool dc_fast;
+    int dc_e;
+    float dc_hw, dc_hh, dc_ps_hi, dc_ps_lo, dc_ox_hi, dc_ox_lo, dc_oy_hi, dc_oy_lo;
 };
 
 __device__ __forceinline__ double unit53(uint64_t h) { return (double)(h >> 11) * 0x1p-53; }
@@ -228,26 +234,54 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                 begin = false;
                 uint32_t px, py;
                 divmod_magic(pix, a.w, w_magic, py, px);
-                double ox = 0.5, oy = 0.5;
-                if (a.mode == SAMPLES_JITTER) {
-                    ox = unit53(sample_hash(a.seed, pix, s, 0));
-                    oy = unit53(sample_hash(a.seed, pix, s, 1));
-                }
-                double ddx = __fma_rn(__dsub_rn(__dadd_rn((double)px, ox), a.half_w), a.ps, a.off_x);
-                double ddy = __fma_rn(-__dsub_rn(__dadd_rn((double)py, oy), a.half_h), a.ps, a.off_y);
-                dcx = (D)ddx;
-                dcy = (D)ddy;
                 scaled = false;
-                if constexpr (S) {
-                    // exponent of the larger component (binary64 field), u = dc 2^-e
-                    double big = fmax(fabs(ddx), fabs(ddy));
-                    int e0 = (int)((__double_as_longlong(big) >> 52) & 0x7ff) - 1023;
-                    if (big != 0.0 && e0 < -100) {
-                        double k = __longlong_as_double((long long)(1023 - e0) << 52);
-                        dcx = (D)(ddx * k);
-                        dcy = (D)(ddy * k);
-                        e = e0;
-                        scaled = true;
+                bool wide = true;  // the binary64 set-up
+                if constexpr (S) if (a.dc_fast) {
+                    // on the FP32 pipe: the binary64 one costs each sample a chain of
+                    // seven dependent binary64 operations
+                    const float tx = __fsub_rn((float)px, a.dc_hw), ty = __fsub_rn(a.dc_hh, (float)py);
+                    const float vx =
+                        __fmaf_rn(tx, a.dc_ps_hi, __fadd_rn(__fmaf_rn(tx, a.dc_ps_lo, a.dc_ox_lo), a.dc_ox_hi));
+                    const float vy =
+                        __fmaf_rn(ty, a.dc_ps_hi, __fadd_rn(__fmaf_rn(ty, a.dc_ps_lo, a.dc_oy_lo), a.dc_oy_hi));
+                    const float big = fmaxf(fabsf(vx), fabsf(vy));
+                    if (big >= 0x1p-100f) {  // |v| < 2^102 by the host's bound on off'
+                        const int k = (int)((__float_as_uint(big) >> 23) & 255u) - 127;
+                        const float sk = __int_as_float((127 - k) << 23);  // 2^-k, exact
+                        const int e0 = a.dc_e + k;
+                        dcx = (D)(vx * sk);
+                        dcy = (D)(vy * sk);
+                        if (e0 < -100) {
+                            e = e0;
+                            scaled = true;
+                        } else {
+                            const float s0 = __int_as_float((127 + e0) << 23);  // 2^e0, normal
+                            dcx *= D(s0), dcy *= D(s0);
+                        }
+                        wide = false;
+                    }
+                }
+                if (wide) {
+                    double ox = 0.5, oy = 0.5;
+                    if (a.mode == SAMPLES_JITTER) {
+                        ox = unit53(sample_hash(a.seed, pix, s, 0));
+                        oy = unit53(sample_hash(a.seed, pix, s, 1));
+                    }
+                    double ddx = __fma_rn(__dsub_rn(__dadd_rn((double)px, ox), a.half_w), a.ps, a.off_x);
+                    double ddy = __fma_rn(-__dsub_rn(__dadd_rn((double)py, oy), a.half_h), a.ps, a.off_y);
+                    dcx = (D)ddx;
+                    dcy = (D)ddy;
+                    if constexpr (S) {
+                        // exponent of the larger component (binary64 field), u = dc 2^-e
+                        double big = fmax(fabs(ddx), fabs(ddy));
+                        int e0 = (int)((__double_as_longlong(big) >> 52) & 0x7ff) - 1023;
+                        if (big != 0.0 && e0 < -100) {
+                            double k = __longlong_as_double((long long)(1023 - e0) << 52);
+                            dcx = (D)(ddx * k);
+                            dcy = (D)(ddy * k);
+                            e = e0;
+                            scaled = true;
+                        }
                     }
                 }
                 dx = D(0);
@@ -908,6 +942,26 @@ static int perturb_impl(const chaos_frame_desc *d, const chaos_orbit *orb, const
     a.off_x = d->center_x;
     a.off_y = d->center_y;
     a.half_h = 0.5 * d->height;
+    a.dc_fast = false;
+    if (std::is_same<D, float>::value && d->pixel_size < 1e-30 && d->sample_mode == SAMPLES_CENTER &&
+        d->width < (1u << 22) && d->height < (1u << 22)) {
+        // the binary32 set-up of the rescaled kernel (see PerturbArgs::dc_fast)
+        const int E = std::ilogb(d->pixel_size);
+        const double psn = std::ldexp(d->pixel_size, -E), oxn = std::ldexp(d->center_x, -E),
+                     oyn = std::ldexp(d->center_y, -E);
+        if (std::isfinite(oxn) && std::isfinite(oyn) && std::fabs(oxn) < 0x1p100 && std::fabs(oyn) < 0x1p100) {
+            a.dc_fast = true;
+            a.dc_e = E;
+            a.dc_hw = (float)(a.half_w - 0.5);
+            a.dc_hh = (float)(a.half_h - 0.5);
+            a.dc_ps_hi = (float)psn;
+            a.dc_ps_lo = (float)(psn - (double)a.dc_ps_hi);
+            a.dc_ox_hi = (float)oxn;
+            a.dc_ox_lo = (float)(oxn - (double)a.dc_ox_hi);
+            a.dc_oy_hi = (float)oyn;
+            a.dc_oy_lo = (float)(oyn - (double)a.dc_oy_hi);
+        }
+    }
     if (std::is_same<D, float>::value)
         a.orbit = reinterpret_cast<const typename Vec2T<D>::type *>(orb->z32);
     else
