@@ -179,7 +179,10 @@ __device__ __forceinline__ void renormalise(D &dx, D &dy, D &dcx, D &dcy, int &e
     }
 }
 
-template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_perturb(PerturbArgs<D> a)
+// Five blocks of 256 per SM for binary32 differences (48 registers: the
+// kernel is issue-bound and a sixth warp per scheduler hides more of the
+// orbit loads than extra registers save), four for binary64 (64 registers)
+template <class D, int K, bool S> __global__ void __launch_bounds__(256, sizeof(D) == 4 ? 5 : 4) k_perturb(PerturbArgs<D> a)
 {
     static_assert(!S || sizeof(D) == 4, "rescaling is for binary32 differences");
     using O = Op<D>;
@@ -200,7 +203,8 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
     D dx = D(0), dy = D(0), dcx = D(0), dcy = D(0), Zx = D(0), Zy = D(0);
     int e = 0;
     bool scaled = false;
-    bool lin = true;  // composed blocks may still apply to this sample (binary32)
+    bool lin = true;      // composed blocks may still apply to this sample
+    uint32_t lin_at = 0;  // the iteration from which to check for them again
     bool need = true, begin = false;
     float acc_v = 0.f, acc[4] = {0.f, 0.f, 0.f, 0.f};
     unsigned long long iters = 0, rebases = 0;
@@ -291,6 +295,7 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                 m = 0;
                 i = 0;
                 lin = true;
+                lin_at = 0;
                 if (a.max_iter == 0) done = true;
             }
             // d' = (2Z + d) d + dc with its tests; true when the sample is done
@@ -321,9 +326,12 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
             };
 #pragma unroll 1
             for (int k = 0; k < K && !done; k++) {
-                if (!lin && !scaled) {
-                    // past every composed and linear form (a plain difference too large
-                    // for them, for good): plain steps for the rest of the round
+                // the lanes still stepping this round, together here (k is the same on all)
+                if (__all_sync(__activemask(), !scaled && (!lin || lin_at >= i + (uint32_t)(K - k)))) {
+                    // every one past the composed and linear forms for this round (a
+                    // plain difference too large for them): plain steps for the rest of
+                    // the round.  Taken by the whole group only: a lane that entered
+                    // alone would run its loop while the others wait, and then they theirs.
 #pragma unroll 1
                     for (; k < K; k++)
                         if (plain_step()) {
@@ -332,7 +340,7 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                         }
                     break;
                 }
-                if constexpr (sizeof(D) == 4) if (lin) {
+                if constexpr (sizeof(D) == 4) if (lin && i >= lin_at) {
                     // a difference far below the orbit: over the next 64 (16) steps
                     // (2Z_j + d_j) d_j stays within 2^-25 of 2Z_j d_j, below binary32
                     // rounding, and no escape, glitch or orbit end can come, when
@@ -361,7 +369,11 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                     // lin_lim never exceeds -25: a plain difference that large stays out;
                     // one 8 binades past this index's bound (it grows ~1 binade a step,
                     // and the bound moves by a few between indices) is taken as out too
-                    if (!scaled && (eb > -25 || (lim.x != LIN_NONE && eb > lim.x + 8))) lin = false;
+                    if (!scaled && (eb > -25 || (lim.x != LIN_NONE && eb > lim.x + 8)))
+                        lin = false;
+                    else if (lim.x != LIN_NONE)
+                        lin_at = i + K;  // near the bound: a difference that hovers there
+                                         // (interior samples) is checked once a round
                 }
                 if constexpr (S) if (scaled && e < -126) {
                     // linear steps up to (not onto) the next index whose tests can fire
@@ -449,7 +461,7 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                     renormalise(dx, dy, dcx, dcy, e, scaled);
                     continue;
                 }
-                if constexpr (sizeof(D) == 8) if (lin) {
+                if constexpr (sizeof(D) == 8) if (lin && i >= lin_at) {
                     // the composed blocks for binary64 differences: over the next 64 (16)
                     // steps the dropped d^2 term stays below binary64 rounding and no
                     // test can fire when ilogb(max |d|, |dc|) <= lin_limd[m].y (.x)
@@ -475,7 +487,10 @@ template <class D, int K, bool S> __global__ void __launch_bounds__(256) k_pertu
                     }
                     // lin_limd never exceeds -54: a difference that large stays out (and,
                     // as for binary32, one 8 binades past this index's bound)
-                    if (eb > -54 || (lim.x != LIN_NONE && eb > lim.x + 8)) lin = false;
+                    if (eb > -54 || (lim.x != LIN_NONE && eb > lim.x + 8))
+                        lin = false;
+                    else if (lim.x != LIN_NONE)
+                        lin_at = i + K;
                 }
                 if constexpr (!S && sizeof(D) == 8) {
                     // binary64 differences far below the orbit (|d|, |dc| < 2^-120 while
