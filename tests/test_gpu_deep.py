@@ -8,7 +8,7 @@ Bars: escape-count mismatch rate at most 0.1% (the workload's bar); for
 matching escaped samples the smooth count within 1e-3 of the oracle's on every
 sample with binary64 differences.  With binary32 differences the median
 deviation is at most 1e-4 and at most 2% of samples deviate by more than 1e-3:
-measured 0.8% (1e-60) and 1.5% (1e-200), up to 0.19, where binary64
+measured 0.9% (1e-60) and 1.4% (1e-200), up to 0.18, where binary64
 differences of the same samples stay within 3e-5: binary32 rounding of the
 differences, not the method."""
 import numpy as np
