@@ -43,6 +43,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/chaos_gb300.h"
@@ -635,6 +636,7 @@ struct chaos_orbit {
     uint32_t escaped_at = 0;  // iteration at which the reference escaped, or max_iter
     uint32_t bits = 0;
     double center_x = 0, center_y = 0;  // rounded centre, for reporting
+    unsigned char *arena = nullptr;     // the one device allocation that holds every table below
     float2 *z32 = nullptr;
     double2 *z64 = nullptr;
     float2 *z2 = nullptr;              // 2 Z in binary32
@@ -715,37 +717,55 @@ static void compose_blocks(const std::vector<double2> &a2, const std::vector<dou
         const double l = std::floor(0.5 * std::log2(rho) - slack);
         return l < -127.0 ? (int)LIN_NONE : (int)std::min(127.0, l);
     };
-    for (size_t m = 0; m + 16 <= n; m++) {
-        double px = 1.0, py = 0.0, qx = 0.0, qy = 0.0;
-        bool ok16 = m + 16 < last && zz[m] > 0.0, ok64 = m + 64 < last && zz[m] > 0.0;
-        double rho = INFINITY, rho16 = INFINITY;
-        for (size_t j = m; j <= m + 64 && j < n; j++) {
-            if (j > m && ev[j]) {
-                if (j <= m + 16) ok16 = false;
-                ok64 = false;
+    auto part = [&](size_t m0, size_t m1) {
+        for (size_t m = m0; m < m1; m++) {
+            double px = 1.0, py = 0.0, qx = 0.0, qy = 0.0;
+            bool ok16 = m + 16 < last && zz[m] > 0.0, ok64 = m + 64 < last && zz[m] > 0.0;
+            double rho = INFINITY, rho16 = INFINITY;
+            for (size_t j = m; j <= m + 64 && j < n; j++) {
+                if (j > m && ev[j]) {
+                    if (j <= m + 16) ok16 = false;
+                    ok64 = false;
+                }
+                if (!ok64 && j > m + 16) break;
+                rho = std::min(rho, zz[j] / (2.0 * (px * px + py * py + qx * qx + qy * qy)));
+                if (j == m + 16) {
+                    rho16 = rho;
+                    b16[m] = BlockMap{px, py, qx, qy};
+                    if (!ok64) break;
+                }
+                if (j == m + 64) {
+                    if (!(2.0 * (px * px + py * py + qx * qx + qy * qy) <= 0x1p200)) ok64 = false;
+                    b64[m] = BlockMap{px, py, qx, qy};
+                    break;
+                }
+                const double ax = a2[j].x, ay = a2[j].y;
+                const double npx = ax * px - ay * py, npy = ax * py + ay * px;
+                const double nqx = ax * qx - ay * qy + 1.0, nqy = ax * qy + ay * qx;
+                px = npx;
+                py = npy;
+                qx = nqx;
+                qy = nqy;
             }
-            if (!ok64 && j > m + 16) break;
-            rho = std::min(rho, zz[j] / (2.0 * (px * px + py * py + qx * qx + qy * qy)));
-            if (j == m + 16) {
-                rho16 = rho;
-                b16[m] = BlockMap{px, py, qx, qy};
-                if (!ok64) break;
-            }
-            if (j == m + 64) {
-                if (!(2.0 * (px * px + py * py + qx * qx + qy * qy) <= 0x1p200)) ok64 = false;
-                b64[m] = BlockMap{px, py, qx, qy};
-                break;
-            }
-            const double ax = a2[j].x, ay = a2[j].y;
-            const double npx = ax * px - ay * py, npy = ax * py + ay * px;
-            const double nqx = ax * qx - ay * qy + 1.0, nqy = ax * qy + ay * qx;
-            px = npx;
-            py = npy;
-            qx = nqx;
-            qy = nqy;
+            lim[m] = make_char2((signed char)(ok16 ? lim_of(rho16) : LIN_NONE), (signed char)(ok64 ? lim_of(rho) : LIN_NONE));
         }
-        lim[m] = make_char2((signed char)(ok16 ? lim_of(rho16) : LIN_NONE), (signed char)(ok64 ? lim_of(rho) : LIN_NONE));
+    };
+    // the indices are independent: they are split over up to 8 host threads
+    // (one per 256 indices); a thread that cannot start leaves its share here
+    const size_t count = n >= 16 ? n - 15 : 0;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t parts = std::min<size_t>(std::min(8u, hw), std::max<size_t>(1, count / 256));
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < parts; t++) {
+        const size_t m0 = count * t / parts, m1 = count * (t + 1) / parts;
+        try {
+            pool.emplace_back(part, m0, m1);
+        } catch (...) {
+            part(m0, m1);
+        }
     }
+    part(0, count / parts);
+    for (std::thread &th : pool) th.join();
 }
 
 static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t max_iterations, chaos_orbit **out)
@@ -758,8 +778,10 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
     uint32_t n = 0;
     uint32_t escaped = max_iterations;
     while (n < max_iterations) {
-        BigFix xx = bigfix_mul(zx, zx), yy = bigfix_mul(zy, zy), xy = bigfix_mul(zx, zy);
-        BigFix nx = bigfix_add(bigfix_sub(xx, yy), cx);
+        // x^2 - y^2 as (x + y)(x - y): two products a step instead of three (the
+        // binary64 orbit of the deep-zoom centre comes out the same, value for value)
+        BigFix d2 = bigfix_mul(bigfix_add(zx, zy), bigfix_sub(zx, zy)), xy = bigfix_mul(zx, zy);
+        BigFix nx = bigfix_add(d2, cx);
         BigFix ny = bigfix_add(bigfix_mul2(xy), cy);
         zx = nx;
         zy = ny;
@@ -858,54 +880,41 @@ static int orbit_compute(const BigFix &cx, const BigFix &cy, int limbs, uint32_t
     o->bits = (uint32_t)(64 * limbs);
     o->center_x = bigfix_to_double(cx);
     o->center_y = bigfix_to_double(cy);
-    cudaError_t e = cudaMalloc(&o->z64, z64.size() * sizeof(double2));
-    if (e == cudaSuccess) e = cudaMalloc(&o->z32, z32.size() * sizeof(float2));
-    if (e == cudaSuccess) e = cudaMemcpy(o->z64, z64.data(), z64.size() * sizeof(double2), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(o->z32, z32.data(), z32.size() * sizeof(float2), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&o->z2, z2.size() * sizeof(float2));
-    if (e == cudaSuccess) e = cudaMemcpy(o->z2, z2.data(), z2.size() * sizeof(float2), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&o->bla16, bla16.size() * sizeof(float4));
-    if (e == cudaSuccess) e = cudaMemcpy(o->bla16, bla16.data(), bla16.size() * sizeof(float4), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&o->bla64, bla64.size() * sizeof(float4));
-    if (e == cudaSuccess) e = cudaMemcpy(o->bla64, bla64.data(), bla64.size() * sizeof(float4), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&o->lin_lim, lin_lim.size() * sizeof(char2));
-    if (e == cudaSuccess)
-        e = cudaMemcpy(o->lin_lim, lin_lim.data(), lin_lim.size() * sizeof(char2), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&o->next_event, next_event.size() * sizeof(uint32_t));
-    if (e == cudaSuccess)
-        e = cudaMemcpy(o->next_event, next_event.data(), next_event.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&o->bla16d, bla16d.size() * sizeof(double2));
-    if (e == cudaSuccess)
-        e = cudaMemcpy(o->bla16d, bla16d.data(), bla16d.size() * sizeof(double2), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&o->bla64d, bla64d.size() * sizeof(double2));
-    if (e == cudaSuccess)
-        e = cudaMemcpy(o->bla64d, bla64d.data(), bla64d.size() * sizeof(double2), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&o->lin_limd, lin_limd.size() * sizeof(char2));
-    if (e == cudaSuccess)
-        e = cudaMemcpy(o->lin_limd, lin_limd.data(), lin_limd.size() * sizeof(char2), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&o->z2_64, z2_64.size() * sizeof(double2));
-    if (e == cudaSuccess)
-        e = cudaMemcpy(o->z2_64, z2_64.data(), z2_64.size() * sizeof(double2), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&o->next_event64, next_event64.size() * sizeof(uint32_t));
-    if (e == cudaSuccess)
-        e = cudaMemcpy(o->next_event64, next_event64.data(), next_event64.size() * sizeof(uint32_t),
-                       cudaMemcpyHostToDevice);
+    // every table in one device allocation, filled by one copy from one host
+    // image (256-byte aligned parts): an orbit is made per zoom step or batch
+    std::vector<unsigned char> image;
+    image.reserve(z64.size() * 160 + 12 * 256);
+    auto stage = [&image](const auto &v) -> size_t {
+        const size_t at = image.size(), bytes = v.size() * sizeof(v[0]);
+        image.resize((at + bytes + 255) & ~(size_t)255);
+        if (bytes) std::memcpy(image.data() + at, v.data(), bytes);
+        return at;
+    };
+    const size_t at_z64 = stage(z64), at_z32 = stage(z32), at_z2 = stage(z2), at_bla16 = stage(bla16),
+                 at_bla64 = stage(bla64), at_lim = stage(lin_lim), at_ev = stage(next_event),
+                 at_bla16d = stage(bla16d), at_bla64d = stage(bla64d), at_limd = stage(lin_limd),
+                 at_z2_64 = stage(z2_64), at_ev64 = stage(next_event64);
+    unsigned char *dev = nullptr;
+    cudaError_t e = cudaMalloc(&dev, image.size());
+    if (e == cudaSuccess) e = cudaMemcpy(dev, image.data(), image.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
-        if (o->z64) cudaFree(o->z64);
-        if (o->z32) cudaFree(o->z32);
-        if (o->z2) cudaFree(o->z2);
-        if (o->bla16) cudaFree(o->bla16);
-        if (o->bla64) cudaFree(o->bla64);
-        if (o->lin_lim) cudaFree(o->lin_lim);
-        if (o->next_event) cudaFree(o->next_event);
-        if (o->bla16d) cudaFree(o->bla16d);
-        if (o->bla64d) cudaFree(o->bla64d);
-        if (o->lin_limd) cudaFree(o->lin_limd);
-        if (o->z2_64) cudaFree(o->z2_64);
-        if (o->next_event64) cudaFree(o->next_event64);
+        if (dev) cudaFree(dev);
         delete o;
         return api_fail(CHAOS_ERR_CUDA, "reference orbit upload: %s", cudaGetErrorString(e));
     }
+    o->arena = dev;
+    o->z64 = reinterpret_cast<double2 *>(dev + at_z64);
+    o->z32 = reinterpret_cast<float2 *>(dev + at_z32);
+    o->z2 = reinterpret_cast<float2 *>(dev + at_z2);
+    o->bla16 = reinterpret_cast<float4 *>(dev + at_bla16);
+    o->bla64 = reinterpret_cast<float4 *>(dev + at_bla64);
+    o->lin_lim = reinterpret_cast<char2 *>(dev + at_lim);
+    o->next_event = reinterpret_cast<uint32_t *>(dev + at_ev);
+    o->bla16d = reinterpret_cast<double2 *>(dev + at_bla16d);
+    o->bla64d = reinterpret_cast<double2 *>(dev + at_bla64d);
+    o->lin_limd = reinterpret_cast<char2 *>(dev + at_limd);
+    o->z2_64 = reinterpret_cast<double2 *>(dev + at_z2_64);
+    o->next_event64 = reinterpret_cast<uint32_t *>(dev + at_ev64);
     *out = o;
     return CHAOS_OK;
 }
@@ -922,18 +931,7 @@ int chaos_orbit_info(const chaos_orbit *o, uint32_t *stored, uint32_t *escaped_a
 int chaos_orbit_destroy(chaos_orbit *o)
 {
     if (!o) return CHAOS_OK;
-    if (o->z64) cudaFree(o->z64);
-    if (o->z32) cudaFree(o->z32);
-    if (o->z2) cudaFree(o->z2);
-    if (o->bla16) cudaFree(o->bla16);
-    if (o->bla64) cudaFree(o->bla64);
-    if (o->lin_lim) cudaFree(o->lin_lim);
-    if (o->next_event) cudaFree(o->next_event);
-    if (o->bla16d) cudaFree(o->bla16d);
-    if (o->bla64d) cudaFree(o->bla64d);
-    if (o->lin_limd) cudaFree(o->lin_limd);
-    if (o->z2_64) cudaFree(o->z2_64);
-    if (o->next_event64) cudaFree(o->next_event64);
+    if (o->arena) cudaFree(o->arena);
     delete o;
     return CHAOS_OK;
 }
