@@ -413,9 +413,10 @@ def run_ours(args):
     if not args.headline_only and W == 3840:
         # after the headline's timed region: the other claims of the path, each
         # with its own clock record (the reference's own GPU kernel on this machine,
-        # the batched C4 forms, the served C5 trace)
+        # the C3 deep zoom, the batched C4 forms, the served C5 trace)
         t_sub = time.perf_counter()
         line["vs_reference_kernel"] = measure_vs_reference_kernel()
+        line["c3"] = measure_c3(steps=3, warmup=1, compact=True)
         line["c4"] = measure_c4("c4", steps=3, warmup=1, compact=True)
         line["c5"] = measure_c5(seconds=C5_BENCH_SECONDS, compact=True)
         line["wall_s_sub_objects"] = time.perf_counter() - t_sub
@@ -982,12 +983,18 @@ DEEP_W, DEEP_H, DEEP_MAX_ITER, DEEP_SPANS, DEEP_ORBIT_BITS = 1920, 1080, 100000,
 
 
 def run_deep(args):
+    """`--workload c3`: the C3 line (measure_c3) with its CPU leg."""
+    print(json.dumps(measure_c3(args.steps, args.warmup, args.min_seconds)), flush=True)
+
+
+def measure_c3(steps=3, warmup=3, min_seconds=None, compact=False):
     """C3: perturbation deep zoom, 1920x1080, spans 1e-60 and 1e-200, maxIter
     100000, centre = the committed seeded Misiurewicz point (1024-bit fixed
     point), one sample per pixel at pixel centres.  One step = both spans'
     frames with binary32 differences (rescaled by 2^e at these depths); the
     reference orbit (1088 bits) is computed once, outside the timed region of
-    `value`, and inside the e2e loop."""
+    `value`, and inside the e2e loop.  `compact` (the default bench line's C3
+    object) leaves out the CPU leg and runs 20 e2e steps."""
     import numpy as np
     import torch
 
@@ -1051,12 +1058,12 @@ def run_deep(args):
         span_iters.append(int(total.item()))
 
     # the timed region lasts at least MIN_TIMED_S (more steps than --steps when needed)
-    _, probe_ms, _ = timed(cg.TIER_PERTURB_F32, 2, args.warmup)
-    min_s = MIN_TIMED_S if args.min_seconds is None else args.min_seconds
-    args.steps = max(args.steps, math.ceil(min_s * 1e3 / max(sum(probe_ms) / 2, 1e-3)))
+    _, probe_ms, _ = timed(cg.TIER_PERTURB_F32, 2, warmup)
+    min_s = MIN_TIMED_S if min_seconds is None else min_seconds
+    steps = max(steps, math.ceil(min_s * 1e3 / max(sum(probe_ms) / 2, 1e-3)))
     clocks = ClockSampler(0)
     clocks.start()
-    iters, span_ms, rb = timed(cg.TIER_PERTURB_F32, args.steps, 1)
+    iters, span_ms, rb = timed(cg.TIER_PERTURB_F32, steps, 1)
     clk = clocks.stop()
     kernel_ms = sum(span_ms)
     value = iters / (kernel_ms / 1e3) / 1e9
@@ -1066,7 +1073,7 @@ def run_deep(args):
     host = torch.empty(n, dtype=torch.int32, pin_memory=True)
     e0 = time.perf_counter()
     e2e_iters = 0
-    e2e_steps = min(args.steps, 100)
+    e2e_steps = min(steps, 20 if compact else 100)
     for _ in range(e2e_steps):
         o2 = cg.Orbit(d["center_x"], d["center_y"], DEEP_ORBIT_BITS, DEEP_MAX_ITER)
         pal.copy_(torch.from_numpy(pal_host.view(np.int32)), non_blocking=False)
@@ -1097,41 +1104,43 @@ def run_deep(args):
             "kernel": "k_perturb<float,64,rescaled>"}
 
     # CPU leg: the oracle's multi-word direct iteration on a bounded sample of pixels
-    from oracle.oracle import Oracle
-    o = Oracle()
-    rng = np.random.default_rng(5)
-    nsamp = 64
-    while True:
-        pix = rng.choice(n, nsamp, replace=False)
-        parts = [o.frame_offsets(DEEP_W, DEEP_H, 1, cg.SAMPLES_CENTER, 0, DEEP_SPANS[1] / DEEP_W, int(p), 1)
-                 for p in pix]
-        dcx = np.concatenate([p[0] for p in parts])
-        dcy = np.concatenate([p[1] for p in parts])
-        t0 = time.perf_counter()
-        cc, _ = o.hp_escape_batch(d["center_x"], d["center_y"], dcx, dcy, DEEP_ORBIT_BITS, DEEP_MAX_ITER)
-        dt = time.perf_counter() - t0
-        if dt > 3.0 or nsamp >= 1 << 16:
-            break
-        nsamp = min(1 << 16, int(nsamp * max(2.0, 3.0 / max(dt, 1e-3))))
-    cpu = {"value": float(cc.astype(np.int64).sum()) / dt / 1e9, "unit": "Gpixel-iter/s", "cores": o.max_threads(),
-           "kind": "port",
-           "sample": f"{nsamp} seeded pixels of the span-1e-200 frame, direct iteration at {DEEP_ORBIT_BITS} bits "
-                     f"(the oracle; the reference has no multi-word path), {int(cc.sum())} pixel-iterations "
-                     f"in {dt:.2f} s"}
+    cpu = None
+    if not compact:
+        from oracle.oracle import Oracle
+        o = Oracle()
+        rng = np.random.default_rng(5)
+        nsamp = 64
+        while True:
+            pix = rng.choice(n, nsamp, replace=False)
+            parts = [o.frame_offsets(DEEP_W, DEEP_H, 1, cg.SAMPLES_CENTER, 0, DEEP_SPANS[1] / DEEP_W, int(p), 1)
+                     for p in pix]
+            dcx = np.concatenate([p[0] for p in parts])
+            dcy = np.concatenate([p[1] for p in parts])
+            t0 = time.perf_counter()
+            cc, _ = o.hp_escape_batch(d["center_x"], d["center_y"], dcx, dcy, DEEP_ORBIT_BITS, DEEP_MAX_ITER)
+            dt = time.perf_counter() - t0
+            if dt > 3.0 or nsamp >= 1 << 16:
+                break
+            nsamp = min(1 << 16, int(nsamp * max(2.0, 3.0 / max(dt, 1e-3))))
+        cpu = {"value": float(cc.astype(np.int64).sum()) / dt / 1e9, "unit": "Gpixel-iter/s",
+               "cores": o.max_threads(), "kind": "port",
+               "sample": f"{nsamp} seeded pixels of the span-1e-200 frame, direct iteration at {DEEP_ORBIT_BITS} "
+                         f"bits (the oracle; the reference has no multi-word path), {int(cc.sum())} "
+                         f"pixel-iterations in {dt:.2f} s"}
 
     line = {"metric": "Gpixel-iter/s (perturbation deep zoom)", "value": value, "unit": "Gpixel-iter/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms / args.steps,
+            "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": kernel_ms / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (rescaled differences)",
             "data": "synthetic: seeded Misiurewicz centre (1024-bit), seeded palette",
             "config": {"workload": f"C3: Mandelbrot {DEEP_W}x{DEEP_H}, spans 1e-60 and 1e-200 (one frame each per "
                                    f"step), maxIter {DEEP_MAX_ITER}, 1 sample per pixel centre, perturbation",
                        "centre": {"preperiod": d["preperiod"], "period": d["period"], "approx": d["approx"]},
                        "orbit_bits": DEEP_ORBIT_BITS, "l2": "flushed between steps"},
-            "pixel_iterations_per_step": iters // args.steps,
-            "per_span": {f"{sp:g}": {"pixel_iterations": it, "ms": ms / args.steps,
-                                     "Gpixel_iter_s": it / (ms / args.steps / 1e3) / 1e9}
+            "pixel_iterations_per_step": iters // steps,
+            "per_span": {f"{sp:g}": {"pixel_iterations": it, "ms": ms / steps,
+                                     "Gpixel_iter_s": it / (ms / steps / 1e3) / 1e9}
                          for sp, it, ms in zip(DEEP_SPANS, span_iters, span_ms)},
-            "rebases_per_step": rb // args.steps,
+            "rebases_per_step": rb // steps,
             "f64_differences": {"value": f64_iters / (sum(f64_ms) / 1e3) / 1e9, "ms_per_step": sum(f64_ms),
                                 "per_span_ms": f64_ms, "rebases": f64_rb},
             "orbit_seconds": t_orbit,
@@ -1140,9 +1149,9 @@ def run_deep(args):
                     "d2h_bytes_per_step": 2 * 4 * n,
                     "call": "chaos_orbit_create + chaos_render_frame_perturb x2 + image reads",
                     "seconds_per_step": e2e_s / e2e_steps, "steps": e2e_steps},
-            "gpu_launches": 2 * args.steps, "clocks": clk}
-    print(json.dumps(line), flush=True)
+            "gpu_launches": 2 * steps, "clocks": clk}
     orbit.close()
+    return line
 
 
 def run_compose(args):
