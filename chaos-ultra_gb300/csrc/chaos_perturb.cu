@@ -18,8 +18,8 @@
 // d = w 2^e, dc = u 2^e with w, u binary32 near 1 and e an integer per sample,
 //     w' = (2 Z + 2^e w) w + u
 // (the 2^e w term is dropped once 2^e is below the binary32 normal range, where
-// it is below binary32 resolution against 2 Z), renormalised by 2^24 when |w|
-// leaves [2^-24, 2^24].  Once 2^e reaches 2^-100 the sample continues with
+// it is below binary32 resolution against 2 Z), renormalised by powers of 2^24
+// when |w| leaves [2^-24, 2^24].  Once 2^e reaches 2^-100 the sample continues with
 // plain binary32 differences d = w 2^e.  While rescaled, |d| < 2^-76, so a
 // glitch needs |Z_m| below 2^-50: that rare case is tested on the binary64
 // orbit in units of 2^e.  While 2^e is below the normal range the step is
@@ -38,6 +38,9 @@
 // while |d| and |dc| stay below 2^-120 and both components of Z above 2^-20:
 // then 2Z + d rounds to 2Z and Z + d' to Z, so d' = 2Z d + dc (4 DFMA) is the
 // full step bit for bit, and its tests depend on the orbit index alone.
+// A sample past all of these forms for the rest of a round (a plain difference
+// too large for the blocks) runs its steps in a tight loop, entered by all the
+// warp's stepping lanes together or by none.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
